@@ -1,0 +1,396 @@
+#!/usr/bin/env python
+"""Headline benchmark of the GB300 sumcheck prover.
+
+Workload: InnerProductProver (MSB), num_vars = 26 -- two tables of 2^26
+seeded uniform Goldilocks values (512 MiB each) -- with Fp3 challenges from
+the Keccak device transcript; 26 rounds + finalize + final value, the whole
+protocol on the device, replayed as one CUDA graph per proof.
+
+One step = one proof.  `value` is input evaluations per second
+(2 * 2^26 per proof) with the tables resident in HBM; `e2e` is the same
+metric through the C ABI from pinned host buffers (H2D of both tables inside
+the step, D2H of the proof).  The inputs (1 GiB) are larger than L2, so no
+flush runs between steps.
+
+`--impl reference` times the CPU implementation of the same path (the C
+restatement in oracle/, all host threads; the Rust reference crate cannot be
+built here) on the same workload and metric.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "efficient-sumcheck_gb300")
+for _p in (ROOT, PKG):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+SEED = 0x5EED_2026
+LABEL = b"effsc-gpu/ip/v1"
+METRIC = "evals/s"
+UNIT = "evals/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--num-vars", type=int, default=26)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--e2e-steps", type=int, default=10)
+    return ap.parse_args()
+
+
+def config(n_vars, world, impl="ours"):
+    how = ("whole protocol on the device, replayed as one CUDA graph" if impl == "ours"
+           else "CPU implementation, all host threads")
+    return {
+        "workload": "InnerProductProver MSB, num_vars=%d: a, b = 2^%d seeded uniform Goldilocks "
+                    "values each, Fp3 challenges from the Keccak transcript, %d rounds + "
+                    "finalize; %s" % (n_vars, n_vars, n_vars, how),
+        "num_vars": n_vars,
+        "tables": 2,
+        "challenge_field": "Fp3 (F64Ext3)",
+        "transcript": "Keccak-f[1600] duplex, label %s" % LABEL.decode(),
+        "l2": "inputs (2 x %d MiB) larger than L2 (129 MB); no flush" % ((8 << n_vars) >> 20),
+        "parallelism": "replicas x%d" % world,
+    }
+
+
+# ---------------------------------------------------------------------------
+# clocks
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return []
+        self.proc.terminate()
+        try:
+            out, _ = self.proc.communicate(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+            out, _ = self.proc.communicate()
+        rows = []
+        for line in out.splitlines():
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                rows.append({"sm": float(parts[1]), "max": float(parts[2]), "power": float(parts[3]),
+                             "hw": parts[5], "hwt": parts[6], "swt": parts[7], "pcap": parts[8]})
+            except ValueError:
+                continue
+        return rows
+
+
+def summarize_clocks(rows):
+    if not rows:
+        return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"], "samples": 0}
+    busy = [r for r in rows if r["power"] > 300] or rows
+    reasons = set()
+    for r in busy:
+        if r["hw"].lower().startswith("active"):
+            reasons.add("hw_slowdown")
+        if r["hwt"].lower().startswith("active"):
+            reasons.add("hw_thermal_slowdown")
+        if r["swt"].lower().startswith("active"):
+            reasons.add("sw_thermal_slowdown")
+        if r["pcap"].lower().startswith("active"):
+            reasons.add("sw_power_cap")
+    return {"sm_mhz": statistics.median(r["sm"] for r in busy), "sm_max_mhz": max(r["max"] for r in rows),
+            "reasons": sorted(reasons), "samples": len(busy), "power_w_max": max(r["power"] for r in rows)}
+
+
+# ---------------------------------------------------------------------------
+# reference arm: the CPU implementation, all host threads
+# ---------------------------------------------------------------------------
+def cpu_proof_seconds(n_vars, check_against=None):
+    """One oracle IP proof at num_vars; returns (seconds, proof)."""
+    from oracle import oracle as O
+    n = 1 << n_vars
+    a = O.gen_table(O.table_seed(SEED, 0), n)
+    b = O.gen_table(O.table_seed(SEED, 1), n)
+    pr = O.Prover(O.IP, O.MSB, 3, [a, b])
+    t0 = time.perf_counter()
+    rp, ch, fv = O.sumcheck(pr, n_vars, O.Transcript(3, label=LABEL))
+    dt = time.perf_counter() - t0
+    return dt, (rp, ch, fv)
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    from oracle import oracle as O
+    cores = os.cpu_count() or 1
+    O.set_threads(cores)
+    n_vars = args.num_vars
+    # bound a step to a few seconds: calibrate on a smaller case first
+    probe = min(n_vars, 20)
+    dt, _ = cpu_proof_seconds(probe)
+    est = dt * (1 << (n_vars - probe))
+    sample_vars = n_vars
+    while est > 8.0 and sample_vars > 16:
+        sample_vars -= 1
+        est /= 2
+    times = []
+    for i in range(args.warmup + args.steps):
+        dt, _ = cpu_proof_seconds(sample_vars)
+        if i >= args.warmup:
+            times.append(dt)
+    total = sum(times)
+    value = args.steps * 2 * (1 << sample_vars) / total
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "u64 (Goldilocks Fp / Fp3)", "data": "synthetic: seeded uniform Goldilocks tables",
+        "config": config(n_vars, args.gpus, "reference"),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": "full protocol (IP MSB, Fp3 challenges, Keccak transcript) at "
+                                   "num_vars=%d per step; C restatement of the reference algorithms "
+                                   "(oracle/), not the Rust reference binary" % sample_vars},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------
+# our arm
+# ---------------------------------------------------------------------------
+def run_ours(args):
+    import numpy as np
+    import torch
+    import effsc_gpu as E
+    from effsc_gpu import _lib
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    L = E.load()
+    ctx = E.Context(local)
+    stream = torch.cuda.current_stream()
+    ctx.set_stream(stream.cuda_stream)
+    n_vars = args.num_vars
+    n = 1 << n_vars
+
+    # inputs generated on the device (seeded), resident in HBM
+    a_dev = torch.empty(n, dtype=torch.int64, device="cuda")
+    b_dev = torch.empty(n, dtype=torch.int64, device="cuda")
+    seed = SEED + 7919 * rank
+    for t, buf in enumerate((a_dev, b_dev)):
+        _lib.check(L.effsc_gen_uniform(ctx.h, E.table_seed(seed, t), n,
+                                       _lib.ctypes.cast(_lib.ctypes.c_void_p(buf.data_ptr()), _lib.u64p), None))
+    prover = E.InnerProductProver.from_device([a_dev.data_ptr(), b_dev.data_ptr()], [n, n], [1, 1], field=E.FP3, ctx=ctx)
+
+    def one_proof(use_graph=True):
+        prover.reset()
+        return prover.prove(n_vars, E.Transcript.keccak(E.FP3, LABEL), use_graph=use_graph)
+
+    for _ in range(max(args.warmup, 3)):
+        one_proof()
+    torch.cuda.synchronize()
+
+    # ---- timed region (device-resident inputs) ----
+    sampler = ClockSampler(local)
+    sampler.start()
+    E.launch_count_reset()
+    barrier()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    w0 = time.perf_counter()
+    ev0.record(stream)
+    for _ in range(args.steps):
+        proof = one_proof()
+    ev1.record(stream)
+    barrier()
+    wall = time.perf_counter() - w0
+    launches = E.launch_count()
+    ms = ev0.elapsed_time(ev1)
+    # keep the GPU busy a little longer if the timed region was too short to sample clocks
+    extra = 0
+    t_end = time.perf_counter() + 1.5
+    while wall < 1.5 and time.perf_counter() < t_end:
+        one_proof()
+        extra += 1
+    torch.cuda.synchronize()
+    clocks = summarize_clocks(sampler.stop())
+    if extra:
+        clocks["sampled_during"] = "timed region + %d more identical steps" % extra
+    if dist is not None:
+        tt = torch.tensor([ms], device="cuda", dtype=torch.float64)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        ms = float(tt.item())
+    evals_per_step = 2 * n
+    value = world * args.steps * evals_per_step / (ms * 1e-3)
+
+    # ---- per-kernel timing (one proof outside the graph) -> roofline ----
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        pass
+    hbm_peak = peaks.get("hbm_gbs") or 6800.0
+    peak_src = "measured" if peaks.get("hbm_gbs") else "fallback"
+    L.effsc_profile_clear()
+    L.effsc_profile_enable(1)
+    one_proof(use_graph=False)
+    L.effsc_profile_enable(0)
+    torch.cuda.synchronize()
+    per = {}
+    nrec = L.effsc_profile_count()
+    for i in range(nrec):
+        name = _lib.ctypes.create_string_buffer(64)
+        msv = _lib.ctypes.c_double()
+        by = _lib.ctypes.c_uint64()
+        _lib.check(L.effsc_profile_get(i, name, 64, _lib.ctypes.byref(msv), _lib.ctypes.byref(by)))
+        k = name.value.decode()
+        d = per.setdefault(k, {"launches": 0, "ms": 0.0, "bytes": 0})
+        d["launches"] += 1
+        d["ms"] += msv.value
+        d["bytes"] += by.value
+    L.effsc_profile_clear()
+    dom = max(per, key=lambda k: per[k]["ms"])
+    d = per[dom]
+    achieved = d["bytes"] / (d["ms"] * 1e-3) / 1e9
+    kernel_ms = sum(v["ms"] for v in per.values())
+    alg_bytes_proof = sum(v["bytes"] for v in per.values())
+    roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                "frac": achieved / hbm_peak, "traffic": None,
+                "peak_source": peak_src + " (MEASURED_PEAKS.json hbm_gbs, burst copy)",
+                "launches_per_proof": d["launches"], "bytes_per_launch_avg": d["bytes"] / d["launches"],
+                "ms_per_launch_avg": d["ms"] / d["launches"]}
+    mm = _lib.ctypes.c_double()
+    f3 = _lib.ctypes.c_double()
+    _lib.check(L.effsc_diag_mulmod_rate(ctx.h, _lib.ctypes.byref(mm), _lib.ctypes.byref(f3)))
+    mulmods = 20 * n   # algorithmic 64-bit modular products of the protocol (Fp3 x Fp3 = 8)
+    ms_proof = ms / args.steps
+    int_roof_ms = mulmods / mm.value * 1e3
+    hbm_roof_ms = alg_bytes_proof / (hbm_peak * 1e9) * 1e3
+
+    # ---- e2e through the C ABI from pinned host buffers ----
+    a_host = torch.empty(n, dtype=torch.int64, pin_memory=True)
+    b_host = torch.empty(n, dtype=torch.int64, pin_memory=True)
+    a_host.copy_(a_dev.cpu())
+    b_host.copy_(b_dev.cpu())
+    an = a_host.numpy().view(np.uint64)
+    bn = b_host.numpy().view(np.uint64)
+
+    def e2e_step():
+        pr = E.InnerProductProver(an, bn, field=E.FP3, ctx=ctx)
+        pf = pr.prove(n_vars, E.Transcript.keccak(E.FP3, LABEL), use_graph=False)
+        del pr
+        return pf
+
+    e2e_step()
+    barrier()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.e2e_steps):
+        pf_e2e = e2e_step()
+    e1.record(stream)
+    barrier()
+    e2e_ms = e0.elapsed_time(e1)
+    if dist is not None:
+        tt = torch.tensor([e2e_ms], device="cuda", dtype=torch.float64)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        e2e_ms = float(tt.item())
+    e2e_value = world * args.e2e_steps * evals_per_step / (e2e_ms * 1e-3)
+    proof_words = n_vars * 2 * 3 + n_vars * 3 + 3
+    d2h = 8 * proof_words + 216 + 2 * 24
+    assert (pf_e2e.round_polys == proof.round_polys).all(), "e2e proof differs from the device-resident proof"
+
+    # ---- CPU baseline (rank 0, N=1) and full-size bit-exactness ----
+    cpu = None
+    bit_exact = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        from oracle import oracle as O
+        cores = os.cpu_count() or 1
+        O.set_threads(cores)
+        pr_o = O.Prover(O.IP, O.MSB, 3, [an, bn])
+        t0 = time.perf_counter()
+        rp, ch, fv = O.sumcheck(pr_o, n_vars, O.Transcript(3, label=LABEL))
+        dt = time.perf_counter() - t0
+        bit_exact = bool((rp == proof.round_polys).all() and (ch == proof.challenges).all()
+                         and (fv == proof.final_value).all())
+        cpu = {"value": 2 * n / dt, "unit": UNIT, "cores": cores, "kind": "port",
+               "sample": "one full proof at num_vars=%d (same inputs and transcript), %.1f s; C restatement "
+                         "of the reference algorithms (oracle/), not the Rust binary" % (n_vars, dt)}
+        assert bit_exact, "GPU proof differs from the oracle at full size"
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_proof, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "u64 (Goldilocks Fp / Fp3, exact modular)",
+            "data": "synthetic: seeded uniform Goldilocks tables (SplitMix64), generated on device",
+            "config": config(n_vars, world),
+            "roofline": roofline,
+            "cpu_baseline": cpu,
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 16 * n, "d2h_bytes_per_step": d2h,
+                    "ms_per_step": e2e_ms / args.e2e_steps,
+                    "path": "effsc_prover_create (pinned host tables) + effsc_prove + proof D2H"},
+            "gpu_launches": launches,
+            "clocks": clocks,
+            "hbm_gbs_per_sumcheck": alg_bytes_proof / (ms_proof * 1e-3) / 1e9,
+            "algorithmic_bytes_per_proof": alg_bytes_proof,
+            "kernel_ms_per_proof": kernel_ms,
+            "int_roofline": {"mulmod_per_s": mm.value, "fp3_mul_per_s": f3.value,
+                             "algorithmic_mulmods": mulmods, "roofline_ms": int_roof_ms},
+            "hbm_roofline_ms": hbm_roof_ms,
+            "frac_of_lower_roofline": max(hbm_roof_ms, int_roof_ms) / ms_proof,
+            "per_kernel": {k: {"launches": v["launches"], "ms": round(v["ms"], 4),
+                               "GB/s": v["bytes"] / (v["ms"] * 1e-3) / 1e9 if v["ms"] else None}
+                           for k, v in per.items()},
+            "bit_exact_vs_oracle": bit_exact,
+        }
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

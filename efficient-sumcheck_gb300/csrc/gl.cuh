@@ -1,0 +1,229 @@
+// gl.cuh -- Goldilocks (p = 2^64 - 2^32 + 1) base field and its cubic extension
+// Fp3 = Fp[X]/(X^3 - W) on sm_103a.
+//
+// Values live in HBM in canonical form (0 <= x < p).  The reference crate keeps
+// arkworks Montgomery residues (src/field.rs:314-375); the boundary converts.
+// W is the canonical value of the crate's F64Ext3 non-residue F64::from_raw(7)
+// (src/tests/fields.rs:73-100), i.e. 7 * 2^-64 mod p = -7 * 2^32 mod p.
+//
+// Products are formed as 128-bit integers and reduced with 2^64 = 2^32 - 1 and
+// 2^96 = -1 (mod p).  Sums of many products are accumulated lazily in 160-bit
+// accumulators (lo, hi, top) and reduced once, using 2^128 = -2^32 (mod p).
+#pragma once
+#include <cstdint>
+
+typedef unsigned long long u64;
+typedef unsigned int u32;
+
+#define GL_P 0xFFFFFFFF00000001ULL
+#define GL_EPS 0x00000000FFFFFFFFULL
+#define GL_W 0xFFFFFFF800000001ULL
+
+__device__ __forceinline__ u64 gl_add(u64 a, u64 b) {
+    u64 s = a + b;
+    if (s < a) return s + GL_EPS;            // carry: 2^64 = eps; result already < p
+    return s >= GL_P ? s - GL_P : s;
+}
+__device__ __forceinline__ u64 gl_sub(u64 a, u64 b) {
+    u64 d = a - b;
+    return a < b ? d - GL_EPS : d;           // borrow: add p (mod 2^64)
+}
+__device__ __forceinline__ u64 gl_neg(u64 a) { return a ? GL_P - a : 0; }
+
+// (hi:lo) mod p, canonical
+__device__ __forceinline__ u64 gl_reduce128(u64 lo, u64 hi) {
+    u64 hh = hi >> 32, hl = hi & GL_EPS;
+    u64 t0 = lo - hh;
+    if (lo < hh) t0 -= GL_EPS;
+    u64 t1 = (hl << 32) - hl;
+    u64 t2 = t0 + t1;
+    if (t2 < t1) t2 += GL_EPS;
+    return t2 >= GL_P ? t2 - GL_P : t2;
+}
+__device__ __forceinline__ void gl_mul128(u64 a, u64 b, u64& lo, u64& hi) {
+    lo = a * b;
+    hi = __umul64hi(a, b);
+}
+__device__ __forceinline__ u64 gl_mul(u64 a, u64 b) {
+    u64 lo, hi;
+    gl_mul128(a, b, lo, hi);
+    return gl_reduce128(lo, hi);
+}
+
+// ---- lazy 160-bit accumulator -------------------------------------------------
+struct Acc {
+    u64 lo, hi;
+    u32 top;
+};
+__device__ __forceinline__ Acc acc_zero() { Acc a; a.lo = 0; a.hi = 0; a.top = 0; return a; }
+__device__ __forceinline__ void acc_add128(Acc& a, u64 lo, u64 hi) {
+    asm("add.cc.u64 %0, %0, %3;\n\t"
+        "addc.cc.u64 %1, %1, %4;\n\t"
+        "addc.u32 %2, %2, 0;"
+        : "+l"(a.lo), "+l"(a.hi), "+r"(a.top)
+        : "l"(lo), "l"(hi));
+}
+__device__ __forceinline__ void acc_add64(Acc& a, u64 v) {
+    asm("add.cc.u64 %0, %0, %3;\n\t"
+        "addc.cc.u64 %1, %1, 0;\n\t"
+        "addc.u32 %2, %2, 0;"
+        : "+l"(a.lo), "+l"(a.hi), "+r"(a.top)
+        : "l"(v));
+}
+__device__ __forceinline__ void acc_mac(Acc& a, u64 x, u64 y) {
+    u64 lo, hi;
+    gl_mul128(x, y, lo, hi);
+    acc_add128(a, lo, hi);
+}
+__device__ __forceinline__ u64 acc_reduce(const Acc& a) {
+    u64 r = gl_reduce128(a.lo, a.hi);
+    return gl_sub(r, ((u64)a.top) << 32);     // top * 2^128 = -top * 2^32
+}
+
+// ---- Fp3 ---------------------------------------------------------------------
+// E == false: only c0 is meaningful (a base-field value embedded as (c0,0,0)).
+struct F3 {
+    u64 c0, c1, c2;
+};
+__device__ __forceinline__ F3 f3_zero() { F3 r; r.c0 = r.c1 = r.c2 = 0; return r; }
+__device__ __forceinline__ F3 f3_make(u64 a, u64 b, u64 c) { F3 r; r.c0 = a; r.c1 = b; r.c2 = c; return r; }
+
+template <bool E>
+__device__ __forceinline__ F3 f3_add(const F3& a, const F3& b) {
+    F3 r;
+    r.c0 = gl_add(a.c0, b.c0);
+    if (E) { r.c1 = gl_add(a.c1, b.c1); r.c2 = gl_add(a.c2, b.c2); } else { r.c1 = r.c2 = 0; }
+    return r;
+}
+template <bool E>
+__device__ __forceinline__ F3 f3_sub(const F3& a, const F3& b) {
+    F3 r;
+    r.c0 = gl_sub(a.c0, b.c0);
+    if (E) { r.c1 = gl_sub(a.c1, b.c1); r.c2 = gl_sub(a.c2, b.c2); } else { r.c1 = r.c2 = 0; }
+    return r;
+}
+// Mixed add where the second operand may be base (EB false).
+template <bool EA, bool EB>
+__device__ __forceinline__ F3 f3_add_mixed(const F3& a, const F3& b) {
+    F3 r;
+    r.c0 = gl_add(a.c0, b.c0);
+    if (EA && EB) { r.c1 = gl_add(a.c1, b.c1); r.c2 = gl_add(a.c2, b.c2); }
+    else if (EA) { r.c1 = a.c1; r.c2 = a.c2; }
+    else if (EB) { r.c1 = b.c1; r.c2 = b.c2; }
+    else { r.c1 = r.c2 = 0; }
+    return r;
+}
+
+// A multiplier prepared for repeated use: (m0, m1, m2, W*m1, W*m2).
+struct Mul3 {
+    u64 m0, m1, m2, w1, w2;
+};
+template <bool E>
+__device__ __forceinline__ Mul3 mul3_prepare(const F3& m) {
+    Mul3 r;
+    r.m0 = m.c0;
+    if (E) { r.m1 = m.c1; r.m2 = m.c2; r.w1 = gl_mul(GL_W, m.c1); r.w2 = gl_mul(GL_W, m.c2); }
+    else { r.m1 = r.m2 = r.w1 = r.w2 = 0; }
+    return r;
+}
+// x * m (+ add), reduced.  EX: x is Fp3; EM: m is Fp3; EADD: add is Fp3.
+// (d0 + d1 X + d2 X^2)(m0 + m1 X + m2 X^2) mod X^3 - W:
+//   c0 = d0 m0 + d1 (W m2) + d2 (W m1)
+//   c1 = d0 m1 + d1 m0 + d2 (W m2)
+//   c2 = d0 m2 + d1 m1 + d2 m0
+template <bool EX, bool EM, bool EADD, bool HAS_ADD>
+__device__ __forceinline__ F3 f3_mul_add(const F3& x, const Mul3& m, const F3& add) {
+    F3 r;
+    if (!EX && !EM) {
+        u64 p = gl_mul(x.c0, m.m0);
+        r.c0 = HAS_ADD ? gl_add(p, add.c0) : p;
+        if (HAS_ADD && EADD) { r.c1 = add.c1; r.c2 = add.c2; } else { r.c1 = r.c2 = 0; }
+        return r;
+    }
+    if (EX != EM) {
+        // one side base: three independent products
+        u64 b = EX ? m.m0 : x.c0;
+        u64 e0 = EX ? x.c0 : m.m0, e1 = EX ? x.c1 : m.m1, e2 = EX ? x.c2 : m.m2;
+        r.c0 = gl_mul(e0, b);
+        r.c1 = gl_mul(e1, b);
+        r.c2 = gl_mul(e2, b);
+        if (HAS_ADD) {
+            r.c0 = gl_add(r.c0, add.c0);
+            if (EADD) { r.c1 = gl_add(r.c1, add.c1); r.c2 = gl_add(r.c2, add.c2); }
+        }
+        return r;
+    }
+    Acc a0 = acc_zero(), a1 = acc_zero(), a2 = acc_zero();
+    acc_mac(a0, x.c0, m.m0); acc_mac(a0, x.c1, m.w2); acc_mac(a0, x.c2, m.w1);
+    acc_mac(a1, x.c0, m.m1); acc_mac(a1, x.c1, m.m0); acc_mac(a1, x.c2, m.w2);
+    acc_mac(a2, x.c0, m.m2); acc_mac(a2, x.c1, m.m1); acc_mac(a2, x.c2, m.m0);
+    if (HAS_ADD) {
+        acc_add64(a0, add.c0);
+        if (EADD) { acc_add64(a1, add.c1); acc_add64(a2, add.c2); }
+    }
+    r.c0 = acc_reduce(a0); r.c1 = acc_reduce(a1); r.c2 = acc_reduce(a2);
+    return r;
+}
+template <bool EA, bool EB>
+__device__ __forceinline__ F3 f3_mul(const F3& a, const F3& b) {
+    Mul3 m = mul3_prepare<EB>(b);
+    return f3_mul_add<EA, EB, false, false>(a, m, f3_zero());
+}
+
+// Lazy sum of products: accumulates sum a*b with a in F<EA>, b in F<EB>.
+template <bool EA, bool EB>
+struct ProdAcc {
+    Acc s0, s0w, s1, s1w, s2;
+    __device__ __forceinline__ void init() { s0 = s0w = s1 = s1w = s2 = acc_zero(); }
+    __device__ __forceinline__ void mac(const F3& a, const F3& b) {
+        acc_mac(s0, a.c0, b.c0);
+        if (EA && EB) {
+            acc_mac(s0w, a.c1, b.c2); acc_mac(s0w, a.c2, b.c1);
+            acc_mac(s1, a.c0, b.c1); acc_mac(s1, a.c1, b.c0);
+            acc_mac(s1w, a.c2, b.c2);
+            acc_mac(s2, a.c0, b.c2); acc_mac(s2, a.c1, b.c1); acc_mac(s2, a.c2, b.c0);
+        } else if (EA) {
+            acc_mac(s1, a.c1, b.c0); acc_mac(s2, a.c2, b.c0);
+        } else if (EB) {
+            acc_mac(s1, a.c0, b.c1); acc_mac(s2, a.c0, b.c2);
+        }
+    }
+    __device__ __forceinline__ F3 result() const {
+        F3 r;
+        r.c0 = acc_reduce(s0);
+        if (EA || EB) {
+            r.c1 = acc_reduce(s1);
+            r.c2 = acc_reduce(s2);
+            if (EA && EB) {
+                r.c0 = gl_add(r.c0, gl_mul(GL_W, acc_reduce(s0w)));
+                r.c1 = gl_add(r.c1, gl_mul(GL_W, acc_reduce(s1w)));
+            }
+        } else {
+            r.c1 = r.c2 = 0;
+        }
+        return r;
+    }
+};
+// Lazy sum of field elements.
+template <bool E>
+struct SumAcc {
+    Acc s0, s1, s2;
+    __device__ __forceinline__ void init() { s0 = s1 = s2 = acc_zero(); }
+    __device__ __forceinline__ void add(const F3& a) {
+        acc_add64(s0, a.c0);
+        if (E) { acc_add64(s1, a.c1); acc_add64(s2, a.c2); }
+    }
+    __device__ __forceinline__ F3 result() const {
+        F3 r;
+        r.c0 = acc_reduce(s0);
+        if (E) { r.c1 = acc_reduce(s1); r.c2 = acc_reduce(s2); } else { r.c1 = r.c2 = 0; }
+        return r;
+    }
+};
+
+// Fold: lo + (hi - lo) * r  with r prepared as Mul3.
+template <bool EIN, bool ECH>
+__device__ __forceinline__ F3 f3_fold(const F3& lo, const F3& hi, const Mul3& r) {
+    F3 d = f3_sub<EIN>(hi, lo);
+    return f3_mul_add<EIN, ECH, EIN, true>(d, r, lo);
+}

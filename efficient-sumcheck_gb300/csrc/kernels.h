@@ -1,0 +1,81 @@
+// kernels.h -- launch interface between the host runtime and the sumcheck
+// round kernels.  Internal to the library (not part of the C ABI).
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+typedef unsigned long long u64;
+typedef unsigned int u32;
+
+namespace effsc {
+
+// Threads per block of every round kernel.
+constexpr int KERNEL_TPB = 256;
+
+// Fold / evaluate semantics.
+//  SEM_MSB_PAD  : half = next_pow2(L)/2, unpaired tail folds as v*(1-w)
+//                 (reference src/inner_product_sumcheck.rs:143-176)
+//  SEM_MSB_FLOOR: half = L/2, no tail (src/provers/coefficient.rs:131-140)
+//  SEM_LSB      : pairs (2k, 2k+1), floor(L/2) outputs
+//                 (src/provers/multilinear_lsb.rs:141-166)
+enum Sem { SEM_MSB_PAD = 0, SEM_MSB_FLOOR = 1, SEM_LSB = 2 };
+
+// Round-polynomial policies (what is accumulated per pair).
+//  POL_ML  : s0 = sum lo, s1 = sum hi                       (1 table)
+//  POL_IP  : q0 = sum lo_a lo_b, qinf = sum (da)(db)        (2 tables)
+//  POL_C1..3: coefficients of prod_i (lo_i + x d_i)         (1..3 tables)
+//  POL_EQFR: POL_IP on (eq_r, p), times the scalar eq_l[0]  (2 tables)
+enum Pol { POL_ML = 0, POL_IP = 1, POL_C1 = 2, POL_C2 = 3, POL_C3 = 4, POL_EQFR = 5, POL_EQFL = 6 };
+
+struct TabIO {
+    const u64* in[3];   // SoA component arrays; [1],[2] null for base tables
+    u64* out[3];
+};
+
+// Optional transcript step performed by the last block of a round kernel.
+struct TxIO {
+    void* tx;              // DevTranscript* (null: no transcript step)
+    const uint8_t* hook;   // bytes absorbed after the round's messages
+    u32 hook_len;
+    u64* proof_wire;       // where the round's wire values go (d * 3 words)
+    u64* proof_chal;       // where the squeezed challenge goes (3 words)
+    u64* chal_next;        // challenge slot read by the next round (3 words)
+};
+
+struct RoundArgs {
+    TabIO t[3];
+    u64 L;                 // length before folding (fold/fused) or current length (eval)
+    u32 m_shift;           // EqFactored left phase: log2 |eq_r|
+    u64 el_len;            // EqFactored left phase: current |eq_l|
+    const u64* chal_ptr;   // challenge in device memory, or null to use `chal`
+    u64 chal[3];
+    const u64* scalar[3];  // EqFactored right phase: eq_l[0] (c1, c2 null if base)
+    u64* partials;         // gridDim * 12 words
+    u32* counter;          // zero between launches (the last block resets it)
+    u64* result;           // wire (d*3 words) then aux pair (6 words)
+    u32* status;           // device status word (non-zero: error code)
+    TxIO tx;
+};
+
+int pol_ntables(int pol);
+int pol_nraw(int pol);
+int pol_nwire(int pol);
+
+// Returns false if no kernel is instantiated for this combination.
+bool launch_fold(int sem, bool ein, bool ech, const RoundArgs& a, int t, int grid, cudaStream_t s);
+bool launch_eval(int pol, int sem, u32 mask, const RoundArgs& a, int grid, cudaStream_t s);
+bool launch_fused(int pol, int sem, u32 mask, bool ech, const RoundArgs& a, int grid, cudaStream_t s);
+bool launch_eqf_left(bool fused, u32 mask, bool ech, const RoundArgs& a, int grid, cudaStream_t s);
+
+// Utility kernels.
+void launch_split_aos(const u64* aos, u64 n, int ncomp, u64* c0, u64* c1, u64* c2, int from_mont, u32* ext_flag, cudaStream_t s);
+void launch_join_aos(const u64* c0, const u64* c1, const u64* c2, u64 n, int ncomp, u64* aos, int to_mont, cudaStream_t s);
+void launch_copy(const u64* src, u64* dst, u64 n, cudaStream_t s);
+void launch_fill(u64* dst, u64 n, u64 v, cudaStream_t s);
+bool launch_build_eq(const u64* w, u32 v, int ext, u64* c0, u64* c1, u64* c2, cudaStream_t s);
+void launch_gen_uniform(u64 seed, u64 n, u64* out, cudaStream_t s);
+bool diag_mulmod_rate(cudaStream_t s, double* mulmod_per_s, double* fp3_mul_per_s);
+int max_grid(void);
+void kernels_init(int device);
+
+}  // namespace effsc

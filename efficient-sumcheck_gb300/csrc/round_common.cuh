@@ -1,0 +1,516 @@
+// round_common.cuh -- building blocks of the sumcheck round kernels.
+//
+// One round of every prover is a single pass over its tables:
+//   fold with the previous challenge (new = lo + (hi - lo) * r) and accumulate
+//   the next round polynomial, each element read once and written once.
+// Per-thread sums are kept unreduced (gl.cuh Acc), reduced once per thread,
+// combined across the warp with shuffles, across the block in shared memory,
+// and across the grid by the last block to finish (atomic ticket), which also
+// turns the raw sums into the EvalsInfty wire values (reference
+// src/sumcheck_prover.rs:40-59) and, on the device-resident path, runs the
+// transcript step: absorb the wire values and the hook bytes, squeeze the
+// next challenge (reference src/runner.rs:39-55).
+#pragma once
+#include "gl.cuh"
+#include "keccak.cuh"
+#include "kernels.h"
+
+namespace effsc {
+
+constexpr int TPB = KERNEL_TPB;
+constexpr int NWARP = TPB / 32;
+constexpr int RAW_WORDS = 12;   // up to 4 Fp3 raw values per block partial
+
+template <u32 M>
+__device__ __forceinline__ constexpr bool ext_of(int t) { return (M >> t) & 1u; }
+
+template <bool E>
+__device__ __forceinline__ F3 ld(const u64* const* p, u64 i) {
+    F3 r;
+    r.c0 = p[0][i];
+    if (E) { r.c1 = p[1][i]; r.c2 = p[2][i]; } else { r.c1 = r.c2 = 0; }
+    return r;
+}
+template <bool E>
+__device__ __forceinline__ void st(u64* const* p, u64 i, const F3& v) {
+    p[0][i] = v.c0;
+    if (E) { p[1][i] = v.c1; p[2][i] = v.c2; }
+}
+// Table t of a kernel whose ext mask is M (t is a compile-time constant after
+// unrolling, so the branch folds away).
+template <u32 M>
+__device__ __forceinline__ F3 ldm(const u64* const* p, u64 i, int t) {
+    return ((M >> t) & 1u) ? ld<true>(p, i) : ld<false>(p, i);
+}
+__device__ __forceinline__ u64 next_pow2_dev(u64 n) {
+    return n <= 1 ? 1 : (1ULL << (64 - __clzll(n - 1)));
+}
+
+// ---------------------------------------------------------------------------
+// Policies: what a round accumulates for each (lo, hi) pair of table entries.
+//   pair(lo, hi): a regular pair
+//   tail(lo)    : MSB tail entry whose hi is an implicit zero
+//   single(lo)  : an entry with no partner that only feeds h(0) (LSB remainder,
+//                 and the length-1 case)
+// ---------------------------------------------------------------------------
+template <int POL, u32 M>
+struct Policy;
+
+// MultilinearProver: s0 = sum lo, s1 = sum hi (src/multilinear_sumcheck.rs:86-124,
+// src/provers/multilinear_lsb.rs:60-96).
+template <u32 M>
+struct Policy<POL_ML, M> {
+    static constexpr int NT = 1, NRAW = 2;
+    static constexpr bool LSB_REMAINDER = true;
+    static constexpr bool E0 = ext_of<M>(0);
+    SumAcc<E0> s0, s1;
+    __device__ __forceinline__ void init() { s0.init(); s1.init(); }
+    __device__ __forceinline__ void pair(const F3* lo, const F3* hi) { s0.add(lo[0]); s1.add(hi[0]); }
+    __device__ __forceinline__ void tail(const F3* lo) { s0.add(lo[0]); }
+    __device__ __forceinline__ void single(const F3* lo) { s0.add(lo[0]); }
+    __device__ __forceinline__ void result(F3* o) const { o[0] = s0.result(); o[1] = s1.result(); }
+};
+
+// InnerProductProver: q0 = sum a_lo b_lo, qinf = sum (a_hi - a_lo)(b_hi - b_lo);
+// MSB tail adds a*b to both (src/provers/inner_product.rs:94-110), the LSB
+// remainder to q0 only (src/provers/inner_product_lsb.rs:131-139).
+template <u32 M>
+struct IpLike {
+    static constexpr int NT = 2, NRAW = 2;
+    static constexpr bool LSB_REMAINDER = true;
+    static constexpr bool E0 = ext_of<M>(0), E1 = ext_of<M>(1);
+    ProdAcc<E0, E1> q0, qi;
+    __device__ __forceinline__ void init() { q0.init(); qi.init(); }
+    __device__ __forceinline__ void pair(const F3* lo, const F3* hi) {
+        q0.mac(lo[0], lo[1]);
+        qi.mac(f3_sub<E0>(hi[0], lo[0]), f3_sub<E1>(hi[1], lo[1]));
+    }
+    __device__ __forceinline__ void tail(const F3* lo) { q0.mac(lo[0], lo[1]); qi.mac(lo[0], lo[1]); }
+    __device__ __forceinline__ void single(const F3* lo) { q0.mac(lo[0], lo[1]); }
+    __device__ __forceinline__ void result(F3* o) const { o[0] = q0.result(); o[1] = qi.result(); }
+};
+template <u32 M> struct Policy<POL_IP, M> : IpLike<M> {};
+// EqFactored right phase (src/provers/eq_factored.rs:178-209): tables (eq_r, p).
+template <u32 M> struct Policy<POL_EQFR, M> : IpLike<M> {};
+
+// CoefficientProver with the product evaluator: coefficients of
+// prod_i (lo_i + x (hi_i - lo_i)).  k = 1 is Degree1Eval
+// (src/provers/coefficient.rs:341-351), k = 3 is TripleProductEval
+// (tests/adversarial_verifier.rs:444-466).  No tails: the coefficient provers
+// fold with floor(L/2) (src/provers/coefficient.rs:131-140).
+template <u32 M>
+struct Policy<POL_C1, M> {
+    static constexpr int NT = 1, NRAW = 2;
+    static constexpr bool LSB_REMAINDER = false;
+    static constexpr bool E0 = ext_of<M>(0);
+    SumAcc<E0> c0, c1;
+    __device__ __forceinline__ void init() { c0.init(); c1.init(); }
+    __device__ __forceinline__ void pair(const F3* lo, const F3* hi) {
+        c0.add(lo[0]);
+        c1.add(f3_sub<E0>(hi[0], lo[0]));
+    }
+    __device__ __forceinline__ void tail(const F3*) {}
+    __device__ __forceinline__ void single(const F3*) {}
+    __device__ __forceinline__ void result(F3* o) const { o[0] = c0.result(); o[1] = c1.result(); }
+};
+template <u32 M>
+struct Policy<POL_C2, M> {
+    static constexpr int NT = 2, NRAW = 3;
+    static constexpr bool LSB_REMAINDER = false;
+    static constexpr bool E0 = ext_of<M>(0), E1 = ext_of<M>(1);
+    ProdAcc<E0, E1> c0, c1, c2;
+    __device__ __forceinline__ void init() { c0.init(); c1.init(); c2.init(); }
+    __device__ __forceinline__ void pair(const F3* lo, const F3* hi) {
+        F3 da = f3_sub<E0>(hi[0], lo[0]), db = f3_sub<E1>(hi[1], lo[1]);
+        c0.mac(lo[0], lo[1]);
+        c1.mac(lo[0], db);
+        c1.mac(da, lo[1]);
+        c2.mac(da, db);
+    }
+    __device__ __forceinline__ void tail(const F3*) {}
+    __device__ __forceinline__ void single(const F3*) {}
+    __device__ __forceinline__ void result(F3* o) const { o[0] = c0.result(); o[1] = c1.result(); o[2] = c2.result(); }
+};
+template <u32 M>
+struct Policy<POL_C3, M> {
+    static constexpr int NT = 3, NRAW = 4;
+    static constexpr bool LSB_REMAINDER = false;
+    static constexpr bool E0 = ext_of<M>(0), E1 = ext_of<M>(1), E2 = ext_of<M>(2);
+    static constexpr bool EU = E0 || E1;
+    ProdAcc<EU, E2> c0, c1, c2, c3;
+    __device__ __forceinline__ void init() { c0.init(); c1.init(); c2.init(); c3.init(); }
+    __device__ __forceinline__ void pair(const F3* lo, const F3* hi) {
+        F3 da = f3_sub<E0>(hi[0], lo[0]), db = f3_sub<E1>(hi[1], lo[1]), dc = f3_sub<E2>(hi[2], lo[2]);
+        // (la + x da)(lb + x db) = u0 + u1 x + u2 x^2
+        F3 u0 = f3_mul<E0, E1>(lo[0], lo[1]);
+        ProdAcc<E0, E1> t;
+        t.init();
+        t.mac(lo[0], db);
+        t.mac(da, lo[1]);
+        F3 u1 = t.result();
+        F3 u2 = f3_mul<E0, E1>(da, db);
+        c0.mac(u0, lo[2]);
+        c1.mac(u0, dc);
+        c1.mac(u1, lo[2]);
+        c2.mac(u1, dc);
+        c2.mac(u2, lo[2]);
+        c3.mac(u2, dc);
+    }
+    __device__ __forceinline__ void tail(const F3*) {}
+    __device__ __forceinline__ void single(const F3*) {}
+    __device__ __forceinline__ void result(F3* o) const {
+        o[0] = c0.result(); o[1] = c1.result(); o[2] = c2.result(); o[3] = c3.result();
+    }
+};
+
+// ---------------------------------------------------------------------------
+// Finalisation by the last block.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ F3 ld_scalar(const u64* const* p) {
+    F3 r;
+    r.c0 = p[0] ? p[0][0] : 0;
+    r.c1 = p[1] ? p[1][0] : 0;
+    r.c2 = p[2] ? p[2][0] : 0;
+    return r;
+}
+
+__device__ __forceinline__ int pol_nwire_dev(int pol) {
+    switch (pol) {
+    case POL_ML: case POL_C1: return 1;
+    case POL_C3: return 3;
+    default: return 2;
+    }
+}
+
+// raw: NRAW Fp3 values in shared memory (3 words each).  Run by warp 0.
+static __device__ __noinline__ void finalize_warp(int pol, const u64* raw, const RoundArgs& a) {
+    __shared__ u64 s_wire[9];
+    __shared__ u64 s_aux[6];
+    __shared__ u64 s_chal[3];
+    __shared__ uint8_t s_scratch[64];
+    const int lane = threadIdx.x & 31;
+    int nwire = pol_nwire_dev(pol);
+    if (lane == 0) {
+        F3 r[4];
+        for (int i = 0; i < 4; i++) r[i] = f3_make(raw[3 * i], raw[3 * i + 1], raw[3 * i + 2]);
+        F3 w[3];
+        if (pol == POL_EQFR) {
+            F3 sc = ld_scalar(a.scalar);
+            r[0] = f3_mul<true, true>(r[0], sc);
+            r[1] = f3_mul<true, true>(r[1], sc);
+        }
+        switch (pol) {
+        case POL_ML: case POL_C1:
+            w[0] = r[0];
+            break;
+        case POL_C2:
+            w[0] = r[0]; w[1] = r[2];
+            break;
+        case POL_C3: {
+            w[0] = r[0]; w[1] = r[3];
+            // h(2) by Horner: ((c3*2 + c2)*2 + c1)*2 + c0
+            F3 h = r[3];
+            h = f3_add<true>(f3_add<true>(h, h), r[2]);
+            h = f3_add<true>(f3_add<true>(h, h), r[1]);
+            h = f3_add<true>(f3_add<true>(h, h), r[0]);
+            w[2] = h;
+            break;
+        }
+        default:   // IP, EQF
+            w[0] = r[0]; w[1] = r[1];
+            break;
+        }
+        for (int i = 0; i < nwire; i++) { s_wire[3 * i] = w[i].c0; s_wire[3 * i + 1] = w[i].c1; s_wire[3 * i + 2] = w[i].c2; }
+        s_aux[0] = r[0].c0; s_aux[1] = r[0].c1; s_aux[2] = r[0].c2;
+        s_aux[3] = r[1].c0; s_aux[4] = r[1].c1; s_aux[5] = r[1].c2;
+    }
+    __syncwarp();
+    if (a.result) {
+        for (int i = lane; i < 3 * nwire; i += 32) a.result[i] = s_wire[i];
+        if (lane < 6) a.result[3 * nwire + lane] = s_aux[lane];
+    }
+    if (a.tx.tx) {
+        DevTranscript* T = (DevTranscript*)a.tx.tx;
+        WarpTx w = tx_load(T, lane);
+        tx_send_elems(w, lane, s_wire, nwire);
+        if (a.tx.hook_len) {
+            const uint8_t* hk = a.tx.hook;
+            tx_absorb(w, lane, a.tx.hook_len, [&](u32 k) -> uint8_t { return hk[k]; });
+        }
+        tx_challenge(w, lane, s_chal, s_scratch);
+        tx_store(T, w, lane);
+        if (lane < 3) {
+            if (a.tx.chal_next) a.tx.chal_next[lane] = s_chal[lane];
+            if (a.tx.proof_chal) a.tx.proof_chal[lane] = s_chal[lane];
+        }
+        if (a.tx.proof_wire)
+            for (int i = lane; i < 3 * nwire; i += 32) a.tx.proof_wire[i] = s_wire[i];
+    }
+}
+
+// Block + grid reduction of NRAW Fp3 values; the last block finalises.
+template <int NRAW>
+__device__ __forceinline__ void reduce_and_finalize(F3 (&v)[NRAW], const RoundArgs& a, int pol) {
+    __shared__ u64 s_red[NWARP][RAW_WORDS];
+    __shared__ u64 s_tot[RAW_WORDS];
+    __shared__ int s_last;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int off = 16; off; off >>= 1) {
+#pragma unroll
+        for (int i = 0; i < NRAW; i++) {
+            v[i].c0 = gl_add(v[i].c0, __shfl_down_sync(0xffffffffu, v[i].c0, off));
+            v[i].c1 = gl_add(v[i].c1, __shfl_down_sync(0xffffffffu, v[i].c1, off));
+            v[i].c2 = gl_add(v[i].c2, __shfl_down_sync(0xffffffffu, v[i].c2, off));
+        }
+    }
+    if (lane == 0) {
+#pragma unroll
+        for (int i = 0; i < NRAW; i++) { s_red[warp][3 * i] = v[i].c0; s_red[warp][3 * i + 1] = v[i].c1; s_red[warp][3 * i + 2] = v[i].c2; }
+    }
+    __syncthreads();
+    if (threadIdx.x < 3 * NRAW) {
+        u64 s = 0;
+#pragma unroll
+        for (int w = 0; w < NWARP; w++) s = gl_add(s, s_red[w][threadIdx.x]);
+        if (gridDim.x == 1) s_tot[threadIdx.x] = s;
+        else a.partials[(u64)blockIdx.x * RAW_WORDS + threadIdx.x] = s;
+    }
+    if (gridDim.x > 1) {
+        __threadfence();
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            u32 t = atomicAdd(a.counter, 1u);
+            s_last = (t == gridDim.x - 1);
+        }
+        __syncthreads();
+        if (!s_last) return;
+        __threadfence();
+        // every thread owns one of the 3*NRAW words and walks the partials
+        u64 acc[RAW_WORDS];
+        for (int i = 0; i < 3 * NRAW; i++) acc[i] = 0;
+        for (u32 b = threadIdx.x; b < gridDim.x; b += TPB)
+            for (int i = 0; i < 3 * NRAW; i++) acc[i] = gl_add(acc[i], __ldcg(&a.partials[(u64)b * RAW_WORDS + i]));
+#pragma unroll
+        for (int off = 16; off; off >>= 1)
+            for (int i = 0; i < 3 * NRAW; i++) acc[i] = gl_add(acc[i], __shfl_down_sync(0xffffffffu, acc[i], off));
+        __syncthreads();
+        if (lane == 0)
+            for (int i = 0; i < 3 * NRAW; i++) s_red[warp][i] = acc[i];
+        __syncthreads();
+        if (threadIdx.x < 3 * NRAW) {
+            u64 s = 0;
+            for (int w = 0; w < NWARP; w++) s = gl_add(s, s_red[w][threadIdx.x]);
+            s_tot[threadIdx.x] = s;
+        }
+        if (threadIdx.x == 0) *a.counter = 0;
+    }
+    __syncthreads();
+    if (NRAW < 4 && threadIdx.x < 3 * (4 - NRAW)) s_tot[3 * NRAW + threadIdx.x] = 0;
+    __syncthreads();
+    if (warp == 0) finalize_warp(pol, s_tot, a);
+}
+
+__device__ __forceinline__ Mul3 load_challenge_mul(const RoundArgs& a, F3& r) {
+    if (a.chal_ptr) r = f3_make(a.chal_ptr[0], a.chal_ptr[1], a.chal_ptr[2]);
+    else r = f3_make(a.chal[0], a.chal[1], a.chal[2]);
+    return mul3_prepare<true>(r);
+}
+
+// ---------------------------------------------------------------------------
+// Kernels
+// ---------------------------------------------------------------------------
+
+// Unfused evaluation of the round polynomial on the current tables.
+template <int POL, int SEM, u32 M>
+__global__ void __launch_bounds__(TPB) k_eval(RoundArgs a) {
+    using P = Policy<POL, M>;
+    P acc;
+    acc.init();
+    const u64 L = a.L;
+    const u64 tid = (u64)blockIdx.x * TPB + threadIdx.x, stride = (u64)gridDim.x * TPB;
+    F3 lo[3], hi[3];
+    if (SEM == SEM_MSB_PAD) {
+        if (L == 1) {
+            if (tid == 0) {
+#pragma unroll
+                for (int t = 0; t < P::NT; t++) lo[t] = ldm<M>(a.t[t].in, 0, t);
+                acc.single(lo);
+            }
+        } else if (L > 1) {
+            const u64 half = next_pow2_dev(L) >> 1, paired = L - half;
+            for (u64 j = tid; j < half; j += stride) {
+#pragma unroll
+                for (int t = 0; t < P::NT; t++) lo[t] = ldm<M>(a.t[t].in, j, t);
+                if (j < paired) {
+#pragma unroll
+                    for (int t = 0; t < P::NT; t++) hi[t] = ldm<M>(a.t[t].in, j + half, t);
+                    acc.pair(lo, hi);
+                } else {
+                    acc.tail(lo);
+                }
+            }
+        }
+    } else if (SEM == SEM_MSB_FLOOR) {
+        const u64 half = L / 2;
+        for (u64 j = tid; j < half; j += stride) {
+#pragma unroll
+            for (int t = 0; t < P::NT; t++) {
+                lo[t] = ldm<M>(a.t[t].in, j, t);
+                hi[t] = ldm<M>(a.t[t].in, j + half, t);
+            }
+            acc.pair(lo, hi);
+        }
+    } else {
+        const u64 n = P::LSB_REMAINDER ? (L + 1) / 2 : L / 2;
+        for (u64 j = tid; j < n; j += stride) {
+#pragma unroll
+            for (int t = 0; t < P::NT; t++) lo[t] = ldm<M>(a.t[t].in, 2 * j, t);
+            if (2 * j + 1 < L) {
+#pragma unroll
+                for (int t = 0; t < P::NT; t++) hi[t] = ldm<M>(a.t[t].in, 2 * j + 1, t);
+                acc.pair(lo, hi);
+            } else {
+                acc.single(lo);
+            }
+        }
+    }
+    F3 raw[P::NRAW];
+    acc.result(raw);
+    reduce_and_finalize<P::NRAW>(raw, a, POL);
+}
+
+// Fused fold + evaluate.  Requires L % 4 == 0 (and L a power of two for the
+// padded MSB semantics): then the fold has no tail and the next round's pairs
+// are exactly the quadruples (k, k+Q, k+2Q, k+3Q) (MSB) or (4k..4k+3) (LSB).
+// Every table is folded; outputs are Fp3 when the challenge is.
+template <int POL, int SEM, u32 M, bool ECH>
+__global__ void __launch_bounds__(TPB) k_fused(RoundArgs a) {
+    constexpr int NT = Policy<POL, 0>::NT;
+    constexpr u32 FULL = (1u << NT) - 1;
+    constexpr u32 MO = ECH ? FULL : M;
+    using P = Policy<POL, MO>;
+    P acc;
+    acc.init();
+    F3 rr;
+    Mul3 r = load_challenge_mul(a, rr);
+    if (!ECH) r = mul3_prepare<false>(rr);
+    const u64 Q = a.L >> 2;
+    const u64 tid = (u64)blockIdx.x * TPB + threadIdx.x, stride = (u64)gridDim.x * TPB;
+    F3 lo[3], hi[3];
+    for (u64 k = tid; k < Q; k += stride) {
+#pragma unroll
+        for (int t = 0; t < NT; t++) {
+            const bool EI = ext_of<M>(t);
+            F3 x0, x1, x2, x3;
+            if (SEM == SEM_LSB) {
+                if (EI) { x0 = ld<true>(a.t[t].in, 4 * k); x1 = ld<true>(a.t[t].in, 4 * k + 1); x2 = ld<true>(a.t[t].in, 4 * k + 2); x3 = ld<true>(a.t[t].in, 4 * k + 3); }
+                else { x0 = ld<false>(a.t[t].in, 4 * k); x1 = ld<false>(a.t[t].in, 4 * k + 1); x2 = ld<false>(a.t[t].in, 4 * k + 2); x3 = ld<false>(a.t[t].in, 4 * k + 3); }
+                if (EI) { lo[t] = f3_fold<true, true>(x0, x1, r); hi[t] = f3_fold<true, true>(x2, x3, r); }
+                else if (ECH) { lo[t] = f3_fold<false, true>(x0, x1, r); hi[t] = f3_fold<false, true>(x2, x3, r); }
+                else { lo[t] = f3_fold<false, false>(x0, x1, r); hi[t] = f3_fold<false, false>(x2, x3, r); }
+                if (ext_of<MO>(t)) { st<true>(a.t[t].out, 2 * k, lo[t]); st<true>(a.t[t].out, 2 * k + 1, hi[t]); }
+                else { st<false>(a.t[t].out, 2 * k, lo[t]); st<false>(a.t[t].out, 2 * k + 1, hi[t]); }
+            } else {
+                if (EI) { x0 = ld<true>(a.t[t].in, k); x1 = ld<true>(a.t[t].in, k + Q); x2 = ld<true>(a.t[t].in, k + 2 * Q); x3 = ld<true>(a.t[t].in, k + 3 * Q); }
+                else { x0 = ld<false>(a.t[t].in, k); x1 = ld<false>(a.t[t].in, k + Q); x2 = ld<false>(a.t[t].in, k + 2 * Q); x3 = ld<false>(a.t[t].in, k + 3 * Q); }
+                if (EI) { lo[t] = f3_fold<true, true>(x0, x2, r); hi[t] = f3_fold<true, true>(x1, x3, r); }
+                else if (ECH) { lo[t] = f3_fold<false, true>(x0, x2, r); hi[t] = f3_fold<false, true>(x1, x3, r); }
+                else { lo[t] = f3_fold<false, false>(x0, x2, r); hi[t] = f3_fold<false, false>(x1, x3, r); }
+                if (ext_of<MO>(t)) { st<true>(a.t[t].out, k, lo[t]); st<true>(a.t[t].out, k + Q, hi[t]); }
+                else { st<false>(a.t[t].out, k, lo[t]); st<false>(a.t[t].out, k + Q, hi[t]); }
+            }
+        }
+        acc.pair(lo, hi);
+    }
+    F3 raw[P::NRAW];
+    acc.result(raw);
+    reduce_and_finalize<P::NRAW>(raw, a, POL);
+}
+
+// Fold one table (t) with no evaluation: the unfused path, the last fold of
+// finalize(), and the standalone fold.
+template <int SEM, bool EI, bool ECH>
+__global__ void __launch_bounds__(TPB) k_fold(RoundArgs a, int t) {
+    constexpr bool EO = EI || ECH;
+    F3 rr;
+    Mul3 r = load_challenge_mul(a, rr);
+    if (!ECH) r = mul3_prepare<false>(rr);
+    const u64 L = a.L;
+    const u64 tid = (u64)blockIdx.x * TPB + threadIdx.x, stride = (u64)gridDim.x * TPB;
+    const u64* const* in = a.t[t].in;
+    u64* const* out = a.t[t].out;
+    if (SEM == SEM_MSB_PAD) {
+        const u64 half = next_pow2_dev(L) >> 1, paired = L - half;
+        // (1 - w) prepared for the tail
+        F3 om = f3_sub<ECH>(f3_make(1, 0, 0), rr);
+        Mul3 omm = mul3_prepare<ECH>(om);
+        for (u64 j = tid; j < half; j += stride) {
+            F3 x0 = ld<EI>(in, j);
+            F3 y;
+            if (j < paired) y = f3_fold<EI, ECH>(x0, ld<EI>(in, j + half), r);
+            else y = f3_mul_add<EI, ECH, false, false>(x0, omm, f3_zero());
+            st<EO>(out, j, y);
+        }
+    } else if (SEM == SEM_MSB_FLOOR) {
+        const u64 half = L / 2;
+        for (u64 j = tid; j < half; j += stride)
+            st<EO>(out, j, f3_fold<EI, ECH>(ld<EI>(in, j), ld<EI>(in, j + half), r));
+    } else {
+        const u64 half = L / 2;
+        for (u64 j = tid; j < half; j += stride)
+            st<EO>(out, j, f3_fold<EI, ECH>(ld<EI>(in, 2 * j), ld<EI>(in, 2 * j + 1), r));
+    }
+}
+
+// EqFactored left phase (src/provers/eq_factored.rs:139-172):
+//   q0   = sum_a eq_l_lo[a] * sum_b eq_r[b] p_lo[a m + b]
+//   qinf = sum_a (eq_l_hi[a] - eq_l_lo[a]) * sum_b eq_r[b] (p_hi - p_lo)[a m + b]
+// Tables: t[0] = p, t[1] = eq_l (already folded), t[2] = eq_r.
+// M bit 0: p is Fp3, bit 1: eq tables are Fp3.  FUSED: fold p first (MSB,
+// L a power of two >= 4) and evaluate on the folded table.
+template <bool FUSED, u32 M, bool ECH>
+__global__ void __launch_bounds__(TPB) k_eqf_left(RoundArgs a) {
+    constexpr bool EPI = ext_of<M>(0), EE = ext_of<M>(1);
+    constexpr bool EP = FUSED ? (EPI || ECH) : EPI;     // p after the fold
+    constexpr bool ET = EE || EP;
+    ProdAcc<EE, ET> q0, qi;
+    q0.init();
+    qi.init();
+    F3 rr;
+    Mul3 r = load_challenge_mul(a, rr);
+    if (!ECH) r = mul3_prepare<false>(rr);
+    const u64 L = a.L;
+    const u64 ph = FUSED ? (L >> 2) : (L >> 1);           // half of the (folded) p
+    const u64 eh = a.el_len >> 1;
+    const u64 mmask = (1ULL << a.m_shift) - 1;
+    const u64 tid = (u64)blockIdx.x * TPB + threadIdx.x, stride = (u64)gridDim.x * TPB;
+    for (u64 k = tid; k < ph; k += stride) {
+        F3 pl, phv;
+        if (FUSED) {
+            F3 x0 = ld<EPI>(a.t[0].in, k), x1 = ld<EPI>(a.t[0].in, k + ph);
+            F3 x2 = ld<EPI>(a.t[0].in, k + 2 * ph), x3 = ld<EPI>(a.t[0].in, k + 3 * ph);
+            if (EPI) { pl = f3_fold<true, true>(x0, x2, r); phv = f3_fold<true, true>(x1, x3, r); }
+            else if (ECH) { pl = f3_fold<false, true>(x0, x2, r); phv = f3_fold<false, true>(x1, x3, r); }
+            else { pl = f3_fold<false, false>(x0, x2, r); phv = f3_fold<false, false>(x1, x3, r); }
+            st<EP>(a.t[0].out, k, pl);
+            st<EP>(a.t[0].out, k + ph, phv);
+        } else {
+            pl = ld<EPI>(a.t[0].in, k);
+            phv = ld<EPI>(a.t[0].in, k + ph);
+        }
+        const u64 ai = k >> a.m_shift, bi = k & mmask;
+        F3 er = ld<EE>(a.t[2].in, bi);
+        F3 t0 = f3_mul<EE, EP>(er, pl);
+        F3 td = f3_mul<EE, EP>(er, f3_sub<EP>(phv, pl));
+        F3 el = ld<EE>(a.t[1].in, ai), eh_ = ld<EE>(a.t[1].in, ai + eh);
+        q0.mac(el, t0);
+        qi.mac(f3_sub<EE>(eh_, el), td);
+    }
+    F3 raw[2];
+    raw[0] = q0.result();
+    raw[1] = qi.result();
+    reduce_and_finalize<2>(raw, a, POL_EQFL);
+}
+
+}  // namespace effsc

@@ -1,0 +1,1401 @@
+// runtime.cu -- host runtime behind the C ABI (include/effsc_gpu.h).
+//
+// Owns device tables, dispatches each prover round to the kernels of
+// k_mlip.cu / k_coef.cu / k_misc.cu, runs the whole protocol on the device
+// (optionally as a CUDA graph), and implements the host transcript and the
+// verifier.  Each prover's round logic restates the reference prover it
+// replaces (file:line cited at each branch).
+#include "effsc_gpu.h"
+#include "kernels.h"
+#include "keccak.cuh"
+
+#include <algorithm>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+using namespace effsc;
+
+// ===========================================================================
+// errors
+// ===========================================================================
+namespace {
+thread_local std::string g_err;
+thread_local uint64_t g_launches = 0;
+
+int fail(int code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    g_err = buf;
+    return code;
+}
+}  // namespace
+
+#define CK(call)                                                                                  \
+    do {                                                                                          \
+        cudaError_t e_ = (call);                                                                  \
+        if (e_ != cudaSuccess) return fail(EFFSC_CUDA_ERROR, "%s: %s", #call, cudaGetErrorString(e_)); \
+    } while (0)
+#define TRY(call)                   \
+    do {                            \
+        int r_ = (call);            \
+        if (r_ != EFFSC_OK) return r_; \
+    } while (0)
+
+// ===========================================================================
+// host field arithmetic (boundary conversions, final values, verifier)
+// ===========================================================================
+namespace {
+typedef unsigned __int128 u128;
+const u64 HP = 0xFFFFFFFF00000001ULL;
+const u64 HEPS = 0xFFFFFFFFULL;
+const u64 HW = 0xFFFFFFF800000001ULL;
+const u64 HR_INV = 0xFFFFFFFF00000001ULL - (1ULL << 32);
+
+inline u64 h_reduce128(u128 x) {
+    u64 lo = (u64)x, hi = (u64)(x >> 64);
+    u64 hh = hi >> 32, hl = hi & HEPS;
+    u64 t0 = lo - hh;
+    if (lo < hh) t0 -= HEPS;
+    u64 t1 = hl * HEPS;
+    u64 t2 = t0 + t1;
+    if (t2 < t1) t2 += HEPS;
+    return t2 >= HP ? t2 - HP : t2;
+}
+inline u64 h_add(u64 a, u64 b) { u64 s = a + b; if (s < a) return s + HEPS; return s >= HP ? s - HP : s; }
+inline u64 h_sub(u64 a, u64 b) { u64 d = a - b; return a < b ? d - HEPS : d; }
+inline u64 h_mul(u64 a, u64 b) { return h_reduce128((u128)a * b); }
+u64 h_pow(u64 a, u64 e) { u64 r = 1; while (e) { if (e & 1) r = h_mul(r, a); a = h_mul(a, a); e >>= 1; } return r; }
+inline u64 h_inv(u64 a) { return h_pow(a, HP - 2); }
+
+struct HF { u64 c[3]; };
+inline HF hf(u64 a, u64 b = 0, u64 c = 0) { HF r; r.c[0] = a; r.c[1] = b; r.c[2] = c; return r; }
+inline HF hf_add(HF a, HF b) { return hf(h_add(a.c[0], b.c[0]), h_add(a.c[1], b.c[1]), h_add(a.c[2], b.c[2])); }
+inline HF hf_sub(HF a, HF b) { return hf(h_sub(a.c[0], b.c[0]), h_sub(a.c[1], b.c[1]), h_sub(a.c[2], b.c[2])); }
+inline HF hf_mul(HF a, HF b) {
+    u64 a0 = a.c[0], a1 = a.c[1], a2 = a.c[2], b0 = b.c[0], b1 = b.c[1], b2 = b.c[2];
+    return hf(h_add(h_mul(a0, b0), h_mul(HW, h_add(h_mul(a1, b2), h_mul(a2, b1)))),
+              h_add(h_add(h_mul(a0, b1), h_mul(a1, b0)), h_mul(HW, h_mul(a2, b2))),
+              h_add(h_add(h_mul(a0, b2), h_mul(a1, b1)), h_mul(a2, b0)));
+}
+inline HF hf_from_u64(u64 x) { return hf(x % HP); }
+inline bool hf_is_ext(const HF& a) { return (a.c[1] | a.c[2]) != 0; }
+
+inline u64 to_canon(u64 x, int repr) { x = x >= HP ? x - HP : x; return repr == EFFSC_MONTGOMERY ? h_mul(x, HR_INV) : x; }
+inline u64 from_canon(u64 x, int repr) { return repr == EFFSC_MONTGOMERY ? h_mul(x, HEPS) : x; }
+// Read one element of `field` words in `repr` into canonical Fp3.
+inline HF load_elem(const uint64_t* p, int field, int repr) {
+    HF r = hf(to_canon(p[0], repr));
+    if (field == EFFSC_FP3) { r.c[1] = to_canon(p[1], repr); r.c[2] = to_canon(p[2], repr); }
+    return r;
+}
+inline void store_elem(uint64_t* p, const HF& v, int field, int repr) {
+    p[0] = from_canon(v.c[0], repr);
+    if (field == EFFSC_FP3) { p[1] = from_canon(v.c[1], repr); p[2] = from_canon(v.c[2], repr); }
+}
+
+// ===========================================================================
+// host Keccak-f[1600] and the duplex transcript (same construction as
+// keccak.cuh; FIPS 202 permutation)
+// ===========================================================================
+const u64 K_RC[24] = {
+    0x0000000000000001ULL, 0x0000000000008082ULL, 0x800000000000808AULL, 0x8000000080008000ULL,
+    0x000000000000808BULL, 0x0000000080000001ULL, 0x8000000080008081ULL, 0x8000000000008009ULL,
+    0x000000000000008AULL, 0x0000000000000088ULL, 0x0000000080008009ULL, 0x000000008000000AULL,
+    0x000000008000808BULL, 0x800000000000008BULL, 0x8000000000008089ULL, 0x8000000000008003ULL,
+    0x8000000000008002ULL, 0x8000000000000080ULL, 0x000000000000800AULL, 0x800000008000000AULL,
+    0x8000000080008081ULL, 0x8000000000008080ULL, 0x0000000080000001ULL, 0x8000000080008008ULL};
+const int K_ROT[25] = {0, 1, 62, 28, 27, 36, 44, 6, 55, 20, 3, 10, 43, 25, 39, 41, 45, 15, 21, 8, 18, 2, 61, 56, 14};
+inline u64 rotl(u64 x, int r) { return r ? (x << r) | (x >> (64 - r)) : x; }
+void keccak_f(u64* A) {
+    for (int round = 0; round < 24; round++) {
+        u64 C[5], B[25];
+        for (int x = 0; x < 5; x++) C[x] = A[x] ^ A[x + 5] ^ A[x + 10] ^ A[x + 15] ^ A[x + 20];
+        for (int x = 0; x < 5; x++) {
+            u64 D = C[(x + 4) % 5] ^ rotl(C[(x + 1) % 5], 1);
+            for (int y = 0; y < 5; y++) A[x + 5 * y] ^= D;
+        }
+        for (int x = 0; x < 5; x++)
+            for (int y = 0; y < 5; y++) B[y + 5 * ((2 * x + 3 * y) % 5)] = rotl(A[x + 5 * y], K_ROT[x + 5 * y]);
+        for (int x = 0; x < 5; x++)
+            for (int y = 0; y < 5; y++) A[x + 5 * y] = B[x + 5 * y] ^ (~B[(x + 1) % 5 + 5 * y] & B[(x + 2) % 5 + 5 * y]);
+        A[0] ^= K_RC[round];
+    }
+}
+}  // namespace
+
+struct effsc_transcript {
+    int kind, field, repr;
+    DevTranscript st;
+    u64 sm;
+};
+
+namespace {
+void tx_h_absorb(effsc_transcript* t, const uint8_t* d, size_t n) {
+    if (t->kind != EFFSC_T_KECCAK) return;
+    DevTranscript& s = t->st;
+    if (s.squeezing) { s.pos = 0; s.squeezing = 0; }
+    for (size_t i = 0; i < n; i++) {
+        if (s.pos == TX_RATE) { keccak_f(s.st); s.pos = 0; }
+        s.st[s.pos >> 3] ^= (u64)d[i] << (8 * (s.pos & 7));
+        s.pos++;
+    }
+}
+void tx_h_squeeze(effsc_transcript* t, uint8_t* out, size_t n) {
+    DevTranscript& s = t->st;
+    if (!s.squeezing) {
+        if (s.pos == TX_RATE) { keccak_f(s.st); s.pos = 0; }
+        s.st[s.pos >> 3] ^= (u64)0x06 << (8 * (s.pos & 7));
+        s.st[(TX_RATE - 1) >> 3] ^= (u64)0x80 << (8 * ((TX_RATE - 1) & 7));
+        keccak_f(s.st);
+        s.pos = 0;
+        s.squeezing = 1;
+    }
+    for (size_t i = 0; i < n; i++) {
+        if (s.pos == TX_RATE) { keccak_f(s.st); s.pos = 0; }
+        out[i] = (uint8_t)(s.st[s.pos >> 3] >> (8 * (s.pos & 7)));
+        s.pos++;
+    }
+}
+void tx_h_send(effsc_transcript* t, const HF& v) {
+    if (t->kind != EFFSC_T_KECCAK) return;
+    uint8_t b[24];
+    int n = t->field;
+    for (int c = 0; c < n; c++)
+        for (int i = 0; i < 8; i++) b[8 * c + i] = (uint8_t)(v.c[c] >> (8 * i));
+    tx_h_absorb(t, b, 8 * (size_t)n);
+}
+HF tx_h_challenge(effsc_transcript* t) {
+    if (t->kind == EFFSC_T_TEST) {
+        t->sm += 0x9E3779B97F4A7C15ULL;
+        u64 z = t->sm;
+        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+        z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+        z ^= z >> 31;
+        return hf_from_u64(z);
+    }
+    HF r = hf(0);
+    for (int c = 0; c < t->field; c++) {
+        uint8_t b[16];
+        tx_h_squeeze(t, b, 16);
+        u64 lo = 0, hi = 0;
+        for (int i = 0; i < 8; i++) { lo |= (u64)b[i] << (8 * i); hi |= (u64)b[8 + i] << (8 * i); }
+        r.c[c] = h_reduce128(((u128)hi << 64) | lo);
+    }
+    return r;
+}
+}  // namespace
+
+// ===========================================================================
+// context
+// ===========================================================================
+struct effsc_ctx {
+    int device;
+    cudaStream_t stream;
+    cudaStream_t own;
+};
+
+// ===========================================================================
+// prover state
+// ===========================================================================
+namespace {
+struct Buf {
+    u64* p[3] = {nullptr, nullptr, nullptr};
+    size_t cap = 0;
+    bool ext = false;
+    bool owned = true;
+};
+struct Table {
+    std::vector<Buf> bufs;  // bufs[0]: the input table, never written by a round
+    int cur = 0;
+    size_t len = 0;
+    bool ext = false;
+};
+struct TabState {
+    int cur;
+    size_t len;
+    bool ext;
+};
+}  // namespace
+
+struct effsc_prover {
+    effsc_ctx* ctx = nullptr;
+    int kind = 0, order = 0, field = 1, repr = 0;
+    int ntab = 0;
+    Table t[3];
+    size_t v = 0, v_l = 0, rounds = 0;        // EqFactored: t[0] = p, t[1] = eq_l, t[2] = eq_r
+    size_t len0[3] = {0, 0, 0};
+    bool ext0[3] = {false, false, false};
+    u64* partials = nullptr;
+    u32* counter = nullptr;
+    u32* status = nullptr;
+    u64* h_res = nullptr;                      // mapped pinned: wire (9 words) + aux (6 words)
+    u64* d_res = nullptr;
+    DevTranscript* d_tx = nullptr;
+    uint8_t* d_hook = nullptr;
+    size_t hook_cap = 0;
+    u64* d_wire = nullptr;
+    u64* d_chals = nullptr;
+    size_t rounds_cap = 0;
+    // CUDA graph of a whole proof started from the reset state
+    cudaGraphExec_t gexec = nullptr;
+    size_t g_rounds = 0, g_hook = 0;
+    uint64_t g_kernels = 0;                    // kernel nodes in the graph
+    TabState g_post[3];
+    size_t g_post_rounds = 0;
+};
+
+namespace {
+
+int degree_of(const effsc_prover* p) {
+    switch (p->kind) {
+    case EFFSC_ML: return 1;
+    case EFFSC_COEF: return p->ntab;
+    default: return 2;
+    }
+}
+int pol_of(const effsc_prover* p) {
+    switch (p->kind) {
+    case EFFSC_ML: return POL_ML;
+    case EFFSC_IP: return POL_IP;
+    case EFFSC_COEF: return p->ntab == 1 ? POL_C1 : p->ntab == 2 ? POL_C2 : POL_C3;
+    default: return POL_EQFR;
+    }
+}
+int sem_of(const effsc_prover* p) {
+    if (p->order == EFFSC_LSB) return SEM_LSB;
+    return p->kind == EFFSC_COEF ? SEM_MSB_FLOOR : SEM_MSB_PAD;
+}
+size_t next_pow2(size_t n) { size_t r = 1; while (r < n) r <<= 1; return r; }
+bool is_pow2(size_t n) { return n && !(n & (n - 1)); }
+int grid_for(u64 work) {
+    u64 g = (work + KERNEL_TPB - 1) / KERNEL_TPB;
+    if (g < 1) g = 1;
+    u64 mg = (u64)max_grid();
+    return (int)(g < mg ? g : mg);
+}
+
+int alloc_buf(effsc_prover* P, Buf& b, size_t cap, bool ext) {
+    b.cap = cap;
+    b.ext = ext;
+    b.owned = true;
+    size_t bytes = (cap ? cap : 1) * sizeof(u64);
+    for (int c = 0; c < (ext ? 3 : 1); c++) {
+        cudaError_t e = cudaMallocAsync((void**)&b.p[c], bytes, P->ctx->stream);
+        if (e != cudaSuccess) return fail(EFFSC_OOM, "device allocation of %zu bytes failed: %s", bytes, cudaGetErrorString(e));
+    }
+    return EFFSC_OK;
+}
+void free_buf(effsc_prover* P, Buf& b) {
+    if (!b.owned) return;
+    for (int c = 0; c < 3; c++)
+        if (b.p[c]) { cudaFreeAsync(b.p[c], P->ctx->stream); b.p[c] = nullptr; }
+}
+
+// Pick (or allocate) the output buffer of a fold: never bufs[0] (the input
+// table), in place when allowed and the type matches.
+int out_buffer(effsc_prover* P, Table& T, bool ext, size_t size, bool inplace_ok, int* out_idx) {
+    if (inplace_ok && T.cur != 0 && T.bufs[T.cur].ext == ext && T.bufs[T.cur].cap >= size) { *out_idx = T.cur; return EFFSC_OK; }
+    for (size_t i = 1; i < T.bufs.size(); i++)
+        if ((int)i != T.cur && T.bufs[i].ext == ext && T.bufs[i].cap >= size) { *out_idx = (int)i; return EFFSC_OK; }
+    Buf b;
+    TRY(alloc_buf(P, b, size, ext));
+    T.bufs.push_back(b);
+    *out_idx = (int)T.bufs.size() - 1;
+    return EFFSC_OK;
+}
+
+RoundArgs base_args(effsc_prover* P) {
+    RoundArgs a;
+    memset(&a, 0, sizeof a);
+    a.partials = P->partials;
+    a.counter = P->counter;
+    a.status = P->status;
+    a.result = P->d_res;
+    return a;
+}
+void set_in(RoundArgs& a, int slot, const Table& T) {
+    const Buf& b = T.bufs[T.cur];
+    for (int c = 0; c < 3; c++) a.t[slot].in[c] = b.p[c];
+}
+void set_out(RoundArgs& a, int slot, const Buf& b) {
+    for (int c = 0; c < 3; c++) a.t[slot].out[c] = b.p[c];
+}
+
+// A round's challenge: absent (round 0), a host value, or a device slot.
+struct Chal {
+    bool has = false;
+    bool ext = false;
+    const u64* dev = nullptr;
+    u64 v[3] = {0, 0, 0};
+};
+void put_chal(RoundArgs& a, const Chal& ch) {
+    a.chal_ptr = ch.dev;
+    for (int c = 0; c < 3; c++) a.chal[c] = ch.v[c];
+}
+
+int check_launch(bool ok, const char* what) {
+    if (!ok) return fail(EFFSC_UNSUPPORTED, "no kernel instantiated for %s", what);
+    g_launches++;
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return fail(EFFSC_CUDA_ERROR, "%s launch: %s", what, cudaGetErrorString(e));
+    return EFFSC_OK;
+}
+
+// Per-launch timing for measurement: CUDA events recorded on the launch
+// stream right before and after each kernel, with the kernel's algorithmic
+// bytes (every table element it must read plus every element it writes).
+struct ProfRec {
+    std::string name;
+    cudaEvent_t a, b;
+    uint64_t bytes;
+};
+thread_local bool g_prof = false;
+thread_local bool g_capturing = false;
+thread_local std::vector<ProfRec> g_prof_recs;
+
+template <class F>
+int timed_launch(cudaStream_t s, const char* name, uint64_t bytes, F fn) {
+    bool prof = g_prof && !g_capturing;
+    cudaEvent_t a = nullptr, b = nullptr;
+    if (prof) { cudaEventCreate(&a); cudaEventRecord(a, s); }
+    bool ok = fn();
+    if (prof) {
+        cudaEventCreate(&b);
+        cudaEventRecord(b, s);
+        g_prof_recs.push_back({name, a, b, bytes});
+    }
+    return check_launch(ok, name);
+}
+inline uint64_t wbytes(bool ext) { return ext ? 24 : 8; }
+
+// Fold table `ti` of P (kernel slot `slot`) with semantics `sem`.
+int fold_table(effsc_prover* P, int ti, int sem, const Chal& ch, bool ech, bool dry) {
+    Table& T = P->t[ti];
+    size_t L = T.len;
+    if (L <= 1) return EFFSC_OK;       // fold of a length-0/1 table is a no-op
+    size_t nl = sem == SEM_MSB_PAD ? next_pow2(L) / 2 : L / 2;
+    bool out_ext = T.ext || ech;
+    int bi;
+    TRY(out_buffer(P, T, out_ext, nl, sem != SEM_LSB, &bi));
+    if (!dry) {
+        RoundArgs a = base_args(P);
+        put_chal(a, ch);
+        a.L = L;
+        set_in(a, 0, T);
+        set_out(a, 0, T.bufs[bi]);
+        u64 work = sem == SEM_MSB_PAD ? next_pow2(L) / 2 : L / 2;
+        uint64_t bytes = L * wbytes(T.ext) + nl * wbytes(out_ext);
+        TRY(timed_launch(P->ctx->stream, "fold", bytes, [&] { return launch_fold(sem, T.ext, ech, a, 0, grid_for(work), P->ctx->stream); }));
+    }
+    T.cur = bi;
+    T.len = nl;
+    T.ext = out_ext;
+    return EFFSC_OK;
+}
+
+u32 mask_of(const effsc_prover* P, const int* idx, int n) {
+    u32 m = 0;
+    for (int i = 0; i < n; i++)
+        if (P->t[idx[i]].ext) m |= 1u << i;
+    return m;
+}
+
+// One round of Multilinear / InnerProduct / Coefficient provers
+// (src/provers/multilinear.rs:58-67, multilinear_lsb.rs:180-189,
+// inner_product.rs:61-113, inner_product_lsb.rs:156-164,
+// coefficient.rs:272-294, coefficient_lsb.rs:180-203).
+int round_std(effsc_prover* P, const Chal& ch, const TxIO& tx, bool dry) {
+    const int pol = pol_of(P), sem = sem_of(P), nt = P->ntab;
+    int idx[3] = {0, 1, 2};
+    size_t L = P->t[0].len;
+    RoundArgs a = base_args(P);
+    a.tx = tx;
+    put_chal(a, ch);
+    if (ch.has && L > 1) {
+        bool any_ext = false;
+        for (int i = 0; i < nt; i++) any_ext |= P->t[i].ext;
+        bool ech = ch.ext || any_ext;
+        bool fusable = sem == SEM_MSB_PAD ? (is_pow2(L) && L >= 4) : (L % 4 == 0 && L >= 4);
+        if (fusable) {
+            u32 mask = mask_of(P, idx, nt);
+            int bi[3];
+            for (int i = 0; i < nt; i++) {
+                Table& T = P->t[i];
+                TRY(out_buffer(P, T, T.ext || ech, L / 2, sem != SEM_LSB, &bi[i]));
+                set_in(a, i, T);
+                set_out(a, i, T.bufs[bi[i]]);
+            }
+            a.L = L;
+            uint64_t bytes = 0;
+            for (int i = 0; i < nt; i++) bytes += L * wbytes(P->t[i].ext) + (L / 2) * wbytes(P->t[i].ext || ech);
+            const char* nm = mask ? "fused_round_fp3" : (ech ? "fused_round_fp_to_fp3" : "fused_round_fp");
+            if (!dry) TRY(timed_launch(P->ctx->stream, nm, bytes, [&] { return launch_fused(pol, sem, mask, ech, a, grid_for(L / 4), P->ctx->stream); }));
+            for (int i = 0; i < nt; i++) {
+                Table& T = P->t[i];
+                T.cur = bi[i];
+                T.len = L / 2;
+                T.ext = T.ext || ech;
+            }
+            return EFFSC_OK;
+        }
+        for (int i = 0; i < nt; i++) TRY(fold_table(P, i, sem, ch, ech, dry));
+        L = P->t[0].len;
+    } else if (!ch.has && P->kind == EFFSC_IP && P->order == EFFSC_LSB && L >= 3 && (L & 1)) {
+        // compute_lsb indexes a[i + 1] past the end for odd lengths
+        // (src/provers/inner_product_lsb.rs:66-73): the reference panics.
+        return fail(EFFSC_PANIC, "InnerProductProverLSB round 0 on odd length %zu (the reference panics)", L);
+    }
+    // evaluate on the current tables
+    for (int i = 0; i < nt; i++) set_in(a, i, P->t[i]);
+    a.L = L;
+    u64 work = sem == SEM_MSB_PAD ? (L > 1 ? next_pow2(L) / 2 : 1) : sem == SEM_MSB_FLOOR ? L / 2 : (L + 1) / 2;
+    uint64_t bytes = 0;
+    for (int i = 0; i < nt; i++) bytes += L * wbytes(P->t[i].ext);
+    if (!dry) TRY(timed_launch(P->ctx->stream, "evaluate", bytes, [&] { return launch_eval(pol, sem, mask_of(P, idx, nt), a, grid_for(work), P->ctx->stream); }));
+    return EFFSC_OK;
+}
+
+// One round of EqFactoredProver (src/provers/eq_factored.rs:249-270).
+int round_eqf(effsc_prover* P, const Chal& ch, const TxIO& tx, bool dry) {
+    Table &p = P->t[0], &el = P->t[1], &er = P->t[2];
+    RoundArgs a = base_args(P);
+    a.tx = tx;
+    put_chal(a, ch);
+    const size_t j = P->rounds;
+    const bool left = j < P->v_l;
+    bool done = false;
+    if (ch.has) {
+        size_t prev_var = P->rounds - 1;   // wraps like the reference's release build
+        bool ech = ch.ext || p.ext || el.ext || er.ext;
+        size_t L = p.len;
+        if (left && prev_var < P->v_l && is_pow2(L) && L >= 4) {
+            // fold eq_l, then fold p fused with the left-phase evaluation
+            TRY(fold_table(P, 1, SEM_MSB_PAD, ch, ech, dry));
+            int bi;
+            TRY(out_buffer(P, p, p.ext || ech, L / 2, true, &bi));
+            set_in(a, 0, p);
+            set_out(a, 0, p.bufs[bi]);
+            set_in(a, 1, el);
+            set_in(a, 2, er);
+            a.L = L;
+            a.el_len = el.len;
+            a.m_shift = (u32)__builtin_ctzll(er.len);
+            u32 mask = (p.ext ? 1u : 0u) | (el.ext ? 2u : 0u);
+            uint64_t bytes = L * wbytes(p.ext) + (L / 2) * wbytes(p.ext || ech) + el.len * wbytes(el.ext) + er.len * wbytes(er.ext);
+            if (!dry) TRY(timed_launch(P->ctx->stream, "eqf_left_fused", bytes, [&] { return launch_eqf_left(true, mask, ech, a, grid_for(L / 4), P->ctx->stream); }));
+            p.cur = bi;
+            p.len = L / 2;
+            p.ext = p.ext || ech;
+            done = true;
+        } else if (!left && prev_var >= P->v_l && is_pow2(L) && L >= 4 && er.len == L) {
+            int idx[2] = {2, 0};
+            u32 mask = mask_of(P, idx, 2);
+            int bi_e, bi_p;
+            TRY(out_buffer(P, er, er.ext || ech, L / 2, true, &bi_e));
+            TRY(out_buffer(P, p, p.ext || ech, L / 2, true, &bi_p));
+            set_in(a, 0, er);
+            set_out(a, 0, er.bufs[bi_e]);
+            set_in(a, 1, p);
+            set_out(a, 1, p.bufs[bi_p]);
+            const Buf& sb = el.bufs[el.cur];
+            for (int c = 0; c < 3; c++) a.scalar[c] = sb.p[c];
+            a.L = L;
+            uint64_t bytes = L * (wbytes(er.ext) + wbytes(p.ext)) + (L / 2) * (wbytes(er.ext || ech) + wbytes(p.ext || ech));
+            if (!dry) TRY(timed_launch(P->ctx->stream, "eqf_right_fused", bytes, [&] { return launch_fused(POL_EQFR, SEM_MSB_PAD, mask, ech, a, grid_for(L / 4), P->ctx->stream); }));
+            er.cur = bi_e; er.len = L / 2; er.ext = er.ext || ech;
+            p.cur = bi_p; p.len = L / 2; p.ext = p.ext || ech;
+            done = true;
+        } else {
+            TRY(fold_table(P, 0, SEM_MSB_PAD, ch, ech, dry));
+            TRY(fold_table(P, prev_var < P->v_l ? 1 : 2, SEM_MSB_PAD, ch, ech, dry));
+        }
+    }
+    if (!done) {
+        if (left) {
+            // src/provers/eq_factored.rs:139-172
+            set_in(a, 0, p);
+            set_in(a, 1, el);
+            set_in(a, 2, er);
+            a.L = p.len;
+            a.el_len = el.len;
+            a.m_shift = (u32)__builtin_ctzll(er.len);
+            u32 mask = (p.ext ? 1u : 0u) | (el.ext ? 2u : 0u);
+            uint64_t bytes = p.len * wbytes(p.ext) + el.len * wbytes(el.ext) + er.len * wbytes(er.ext);
+            if (!dry) TRY(timed_launch(P->ctx->stream, "eqf_left_evaluate", bytes, [&] { return launch_eqf_left(false, mask, false, a, grid_for(p.len / 2), P->ctx->stream); }));
+        } else {
+            // src/provers/eq_factored.rs:178-209
+            int idx[2] = {2, 0};
+            set_in(a, 0, er);
+            set_in(a, 1, p);
+            const Buf& sb = el.bufs[el.cur];
+            for (int c = 0; c < 3; c++) a.scalar[c] = sb.p[c];
+            a.L = p.len;
+            u64 work = p.len > 1 ? p.len / 2 : 1;
+            uint64_t bytes = p.len * (wbytes(p.ext) + wbytes(er.ext));
+            if (!dry) TRY(timed_launch(P->ctx->stream, "eqf_right_evaluate", bytes, [&] { return launch_eval(POL_EQFR, SEM_MSB_PAD, mask_of(P, idx, 2), a, grid_for(work), P->ctx->stream); }));
+        }
+    }
+    P->rounds++;
+    return EFFSC_OK;
+}
+
+int do_round(effsc_prover* P, const Chal& ch, const TxIO& tx, bool dry) {
+    return P->kind == EFFSC_EQF ? round_eqf(P, ch, tx, dry) : round_std(P, ch, tx, dry);
+}
+
+// SumcheckProver::finalize of every prover.
+int do_finalize(effsc_prover* P, const Chal& ch, bool dry) {
+    if (P->kind == EFFSC_EQF) {
+        // src/provers/eq_factored.rs:272-280 (last_var = v - 1, wrapping)
+        bool ech = ch.ext || P->t[0].ext || P->t[1].ext || P->t[2].ext;
+        size_t last_var = P->v - 1;
+        TRY(fold_table(P, 0, SEM_MSB_PAD, ch, ech, dry));
+        TRY(fold_table(P, last_var < P->v_l ? 1 : 2, SEM_MSB_PAD, ch, ech, dry));
+        return EFFSC_OK;
+    }
+    bool ech = ch.ext;
+    for (int i = 0; i < P->ntab; i++) ech |= P->t[i].ext;
+    for (int i = 0; i < P->ntab; i++) TRY(fold_table(P, i, sem_of(P), ch, ech, dry));
+    return EFFSC_OK;
+}
+
+int read_first(effsc_prover* P, int ti, HF* out) {
+    Table& T = P->t[ti];
+    const Buf& b = T.bufs[T.cur];
+    u64 w[3] = {0, 0, 0};
+    for (int c = 0; c < (T.ext ? 3 : 1); c++)
+        CK(cudaMemcpyAsync(&w[c], b.p[c], sizeof(u64), cudaMemcpyDeviceToHost, P->ctx->stream));
+    CK(cudaStreamSynchronize(P->ctx->stream));
+    *out = hf(w[0], w[1], w[2]);
+    return EFFSC_OK;
+}
+
+// SumcheckProver::final_value of every prover.
+int final_value(effsc_prover* P, HF* out) {
+    *out = hf(0);
+    switch (P->kind) {
+    case EFFSC_ML:   // src/provers/multilinear.rs:74-79
+        if (P->t[0].len == 1) TRY(read_first(P, 0, out));
+        return EFFSC_OK;
+    case EFFSC_IP: { // src/provers/inner_product.rs:120-126
+        if (P->t[0].len != 1) return EFFSC_OK;
+        HF a, b;
+        TRY(read_first(P, 0, &a));
+        TRY(read_first(P, 1, &b));
+        *out = hf_mul(a, b);
+        return EFFSC_OK;
+    }
+    case EFFSC_COEF: { // src/provers/coefficient.rs:300-329: h(0) + h(1) of the
+        // product evaluator on (singleton, 0) pairs = product of the singletons
+        if (P->ntab == 1 && P->t[0].len == 1) return read_first(P, 0, out);
+        HF acc = hf(1);
+        for (int i = 0; i < P->ntab; i++) {
+            HF x = hf(0);
+            if (P->t[i].len == 1) TRY(read_first(P, i, &x));
+            acc = hf_mul(acc, x);
+        }
+        // coefficients c(x) = prod (x_i - x x_i): h(0) = prod x_i, h(1) = 0
+        *out = acc;
+        return EFFSC_OK;
+    }
+    default: {       // src/provers/eq_factored.rs:282-288
+        if (P->t[0].len != 1) return EFFSC_OK;
+        HF pv, a, b;
+        TRY(read_first(P, 0, &pv));
+        TRY(read_first(P, 1, &a));
+        TRY(read_first(P, 2, &b));
+        *out = hf_mul(hf_mul(pv, a), b);
+        return EFFSC_OK;
+    }
+    }
+}
+
+int prover_common_init(effsc_prover* P) {
+    cudaStream_t s = P->ctx->stream;
+    CK(cudaMallocAsync((void**)&P->partials, (size_t)max_grid() * 12 * sizeof(u64), s));
+    CK(cudaMallocAsync((void**)&P->counter, 2 * sizeof(u32), s));
+    P->status = P->counter + 1;
+    CK(cudaMemsetAsync(P->counter, 0, 2 * sizeof(u32), s));
+    CK(cudaHostAlloc((void**)&P->h_res, 16 * sizeof(u64), cudaHostAllocMapped));
+    CK(cudaHostGetDevicePointer((void**)&P->d_res, P->h_res, 0));
+    memset(P->h_res, 0, 16 * sizeof(u64));
+    return EFFSC_OK;
+}
+
+// Upload one host table (AoS, ncomp words per element) into bufs[0].
+int upload_table(effsc_prover* P, Table& T, const uint64_t* host, size_t len, int ncomp, int repr) {
+    cudaStream_t s = P->ctx->stream;
+    Buf b;
+    if (ncomp == 1) {
+        TRY(alloc_buf(P, b, len, false));
+        if (len) CK(cudaMemcpyAsync(b.p[0], host, len * sizeof(u64), cudaMemcpyHostToDevice, s));
+        if (repr == EFFSC_MONTGOMERY && len) {
+            launch_split_aos(b.p[0], len, 1, b.p[0], nullptr, nullptr, 1, nullptr, s);
+            g_launches++;
+        }
+    } else {
+        TRY(alloc_buf(P, b, len, true));
+        u64* stage = nullptr;
+        u32* flag = nullptr;
+        CK(cudaMallocAsync((void**)&stage, (len ? len : 1) * 3 * sizeof(u64), s));
+        CK(cudaMallocAsync((void**)&flag, sizeof(u32), s));
+        CK(cudaMemsetAsync(flag, 0, sizeof(u32), s));
+        if (len) {
+            CK(cudaMemcpyAsync(stage, host, len * 3 * sizeof(u64), cudaMemcpyHostToDevice, s));
+            launch_split_aos(stage, len, 3, b.p[0], b.p[1], b.p[2], repr == EFFSC_MONTGOMERY, flag, s);
+            g_launches++;
+        }
+        u32 hflag = 0;
+        CK(cudaMemcpyAsync(&hflag, flag, sizeof(u32), cudaMemcpyDeviceToHost, s));
+        CK(cudaFreeAsync(stage, s));
+        CK(cudaFreeAsync(flag, s));
+        CK(cudaStreamSynchronize(s));
+        if (!hflag) {
+            // every element is embedded (c1 = c2 = 0): keep the base component
+            cudaFreeAsync(b.p[1], s);
+            cudaFreeAsync(b.p[2], s);
+            b.p[1] = b.p[2] = nullptr;
+            b.ext = false;
+        }
+    }
+    T.bufs.clear();
+    T.bufs.push_back(b);
+    T.cur = 0;
+    T.len = len;
+    T.ext = b.ext;
+    return EFFSC_OK;
+}
+
+// Make table T an Fp3 table (input buffer replaced by its embedded copy).
+int promote(effsc_prover* P, Table& T) {
+    if (T.ext) return EFFSC_OK;
+    cudaStream_t s = P->ctx->stream;
+    Buf nb;
+    TRY(alloc_buf(P, nb, T.len, true));
+    Buf& ob = T.bufs[T.cur];
+    if (T.len) {
+        CK(cudaMemcpyAsync(nb.p[0], ob.p[0], T.len * sizeof(u64), cudaMemcpyDeviceToDevice, s));
+        CK(cudaMemsetAsync(nb.p[1], 0, T.len * sizeof(u64), s));
+        CK(cudaMemsetAsync(nb.p[2], 0, T.len * sizeof(u64), s));
+    }
+    for (auto& b : T.bufs) free_buf(P, b);
+    T.bufs.clear();
+    T.bufs.push_back(nb);
+    T.cur = 0;
+    T.ext = true;
+    return EFFSC_OK;
+}
+
+// Keep every table combination on an instantiated kernel: mixed base/Fp3
+// tables are promoted except the (Fp3, base, base) CoefficientProver shape
+// (eq(r, x) * f * g with base f, g).
+int normalize_masks(effsc_prover* P) {
+    if (P->kind == EFFSC_EQF) {
+        if (P->field == EFFSC_FP3 || P->t[0].ext) { TRY(promote(P, P->t[1])); TRY(promote(P, P->t[2])); }
+        return EFFSC_OK;
+    }
+    int nt = P->ntab;
+    bool any = false, all = true;
+    for (int i = 0; i < nt; i++) { any |= P->t[i].ext; all &= P->t[i].ext; }
+    if (!any || all) return EFFSC_OK;
+    if (P->kind == EFFSC_COEF && nt == 3 && P->t[0].ext && !P->t[1].ext && !P->t[2].ext) return EFFSC_OK;
+    for (int i = 0; i < nt; i++) TRY(promote(P, P->t[i]));
+    return EFFSC_OK;
+}
+
+void snapshot_initial(effsc_prover* P) {
+    for (int i = 0; i < 3; i++) { P->len0[i] = P->t[i].len; P->ext0[i] = P->t[i].ext; }
+}
+
+int check_field(int field) {
+    if (field != EFFSC_FP && field != EFFSC_FP3) return fail(EFFSC_INVALID_ARG, "field must be EFFSC_FP (1) or EFFSC_FP3 (3)");
+    return EFFSC_OK;
+}
+
+void release_prover(effsc_prover* P) {
+    if (!P) return;
+    if (P->ctx) {
+        cudaSetDevice(P->ctx->device);
+        cudaStreamSynchronize(P->ctx->stream);
+        for (int i = 0; i < 3; i++)
+            for (auto& b : P->t[i].bufs) free_buf(P, b);
+        cudaStream_t s = P->ctx->stream;
+        if (P->partials) cudaFreeAsync(P->partials, s);
+        if (P->counter) cudaFreeAsync(P->counter, s);
+        if (P->d_tx) cudaFreeAsync(P->d_tx, s);
+        if (P->d_hook) cudaFreeAsync(P->d_hook, s);
+        if (P->d_wire) cudaFreeAsync(P->d_wire, s);
+        if (P->d_chals) cudaFreeAsync(P->d_chals, s);
+        if (P->gexec) cudaGraphExecDestroy(P->gexec);
+        cudaStreamSynchronize(s);
+    }
+    if (P->h_res) cudaFreeHost(P->h_res);
+    delete P;
+}
+
+Chal host_chal(const effsc_prover* P, const uint64_t* c) {
+    Chal ch;
+    ch.has = c != nullptr;
+    if (c) {
+        HF v = load_elem(c, P->field, P->repr);
+        for (int i = 0; i < 3; i++) ch.v[i] = v.c[i];
+        ch.ext = hf_is_ext(v);
+    }
+    return ch;
+}
+
+}  // namespace
+
+// ===========================================================================
+// C ABI
+// ===========================================================================
+extern "C" {
+
+const char* effsc_last_error(void) { return g_err.c_str(); }
+const char* effsc_status_str(int s) {
+    switch (s) {
+    case EFFSC_OK: return "ok";
+    case EFFSC_INVALID_ARG: return "invalid argument";
+    case EFFSC_OOM: return "out of device memory";
+    case EFFSC_CUDA_ERROR: return "CUDA error";
+    case EFFSC_TIMEOUT: return "timeout";
+    case EFFSC_UNSUPPORTED: return "unsupported";
+    case EFFSC_PANIC: return "the reference panics on this input";
+    default: return "unknown status";
+    }
+}
+uint64_t effsc_launch_count(void) { return g_launches; }
+void effsc_launch_count_reset(void) { g_launches = 0; }
+
+int effsc_profile_enable(int on) {
+    g_prof = on != 0;
+    return EFFSC_OK;
+}
+size_t effsc_profile_count(void) { return g_prof_recs.size(); }
+int effsc_profile_get(size_t i, char* name, size_t name_cap, double* ms, uint64_t* bytes) {
+    if (i >= g_prof_recs.size()) return fail(EFFSC_INVALID_ARG, "profile record %zu out of range", i);
+    ProfRec& r = g_prof_recs[i];
+    if (name && name_cap) {
+        strncpy(name, r.name.c_str(), name_cap - 1);
+        name[name_cap - 1] = 0;
+    }
+    if (ms) {
+        CK(cudaEventSynchronize(r.b));
+        float f = 0;
+        CK(cudaEventElapsedTime(&f, r.a, r.b));
+        *ms = f;
+    }
+    if (bytes) *bytes = r.bytes;
+    return EFFSC_OK;
+}
+void effsc_profile_clear(void) {
+    for (auto& r : g_prof_recs) { cudaEventDestroy(r.a); cudaEventDestroy(r.b); }
+    g_prof_recs.clear();
+}
+
+int effsc_diag_mulmod_rate(effsc_ctx* ctx, double* mulmod_per_s, double* fp3_mul_per_s) {
+    if (!ctx) return fail(EFFSC_INVALID_ARG, "ctx is NULL");
+    CK(cudaSetDevice(ctx->device));
+    double a = 0, b = 0;
+    if (!diag_mulmod_rate(ctx->stream, &a, &b)) return fail(EFFSC_CUDA_ERROR, "mulmod microbenchmark failed");
+    if (mulmod_per_s) *mulmod_per_s = a;
+    if (fp3_mul_per_s) *fp3_mul_per_s = b;
+    return EFFSC_OK;
+}
+
+int effsc_ctx_create(int device, effsc_ctx** out) {
+    if (!out) return fail(EFFSC_INVALID_ARG, "out is NULL");
+    int n = 0;
+    CK(cudaGetDeviceCount(&n));
+    if (device < 0 || device >= n) return fail(EFFSC_INVALID_ARG, "device %d out of range (%d devices)", device, n);
+    CK(cudaSetDevice(device));
+    effsc_ctx* c = new effsc_ctx();
+    c->device = device;
+    cudaError_t e = cudaStreamCreateWithFlags(&c->own, cudaStreamNonBlocking);
+    if (e != cudaSuccess) { delete c; return fail(EFFSC_CUDA_ERROR, "cudaStreamCreate: %s", cudaGetErrorString(e)); }
+    c->stream = c->own;
+    kernels_init(device);
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+        uint64_t thr = UINT64_MAX;
+        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+    }
+    *out = c;
+    return EFFSC_OK;
+}
+int effsc_ctx_destroy(effsc_ctx* c) {
+    if (!c) return EFFSC_OK;
+    cudaSetDevice(c->device);
+    cudaStreamSynchronize(c->stream);
+    cudaStreamDestroy(c->own);
+    delete c;
+    return EFFSC_OK;
+}
+int effsc_ctx_set_stream(effsc_ctx* c, void* s) {
+    if (!c) return fail(EFFSC_INVALID_ARG, "ctx is NULL");
+    c->stream = s ? (cudaStream_t)s : c->own;
+    return EFFSC_OK;
+}
+int effsc_ctx_synchronize(effsc_ctx* c) {
+    if (!c) return fail(EFFSC_INVALID_ARG, "ctx is NULL");
+    CK(cudaSetDevice(c->device));
+    CK(cudaStreamSynchronize(c->stream));
+    return EFFSC_OK;
+}
+
+int effsc_prover_create(effsc_ctx* ctx, int kind, int order, int field, int repr, int n_tables,
+                        const uint64_t* const* tables, const size_t* lens, const int* ncomp, effsc_prover** out) {
+    if (!ctx || !out || !tables || !lens || !ncomp) return fail(EFFSC_INVALID_ARG, "NULL argument");
+    TRY(check_field(field));
+    if (kind != EFFSC_ML && kind != EFFSC_IP && kind != EFFSC_COEF) return fail(EFFSC_INVALID_ARG, "kind must be ML, IP or COEF (use effsc_eqf_create)");
+    if (order != EFFSC_MSB && order != EFFSC_LSB) return fail(EFFSC_INVALID_ARG, "order must be MSB or LSB");
+    int want = kind == EFFSC_ML ? 1 : kind == EFFSC_IP ? 2 : -1;
+    if ((want > 0 && n_tables != want) || n_tables < 1 || n_tables > 3)
+        return fail(EFFSC_INVALID_ARG, "wrong number of tables (%d)", n_tables);
+    for (int i = 0; i < n_tables; i++) {
+        if (ncomp[i] != 1 && ncomp[i] != 3) return fail(EFFSC_INVALID_ARG, "ncomp must be 1 or 3");
+        if (ncomp[i] == 3 && field != EFFSC_FP3) return fail(EFFSC_INVALID_ARG, "Fp3 table for an Fp prover");
+        if (lens[i] && !tables[i]) return fail(EFFSC_INVALID_ARG, "table %d is NULL", i);
+    }
+    if (kind == EFFSC_IP && lens[0] != lens[1])
+        return fail(EFFSC_PANIC, "a and b must have equal length (%zu != %zu)", lens[0], lens[1]);
+    if (kind == EFFSC_COEF)
+        for (int i = 1; i < n_tables; i++)
+            if (lens[i] != lens[0]) return fail(EFFSC_PANIC, "pairwise tables must have equal length");
+    CK(cudaSetDevice(ctx->device));
+    effsc_prover* P = new effsc_prover();
+    P->ctx = ctx; P->kind = kind; P->order = order; P->field = field; P->repr = repr; P->ntab = n_tables;
+    int rc = prover_common_init(P);
+    for (int i = 0; i < n_tables && rc == EFFSC_OK; i++) rc = upload_table(P, P->t[i], tables[i], lens[i], ncomp[i], repr);
+    if (rc == EFFSC_OK) rc = normalize_masks(P);
+    if (rc == EFFSC_OK) { cudaError_t e = cudaStreamSynchronize(ctx->stream); if (e != cudaSuccess) rc = fail(EFFSC_CUDA_ERROR, "upload: %s", cudaGetErrorString(e)); }
+    if (rc != EFFSC_OK) { release_prover(P); return rc; }
+    snapshot_initial(P);
+    *out = P;
+    return EFFSC_OK;
+}
+
+int effsc_prover_create_device(effsc_ctx* ctx, int kind, int order, int field, int n_tables,
+                               const uint64_t* const* dev_tables, const size_t* lens, const int* ncomp,
+                               effsc_prover** out) {
+    if (!ctx || !out || !dev_tables || !lens || !ncomp) return fail(EFFSC_INVALID_ARG, "NULL argument");
+    TRY(check_field(field));
+    if (kind != EFFSC_ML && kind != EFFSC_IP && kind != EFFSC_COEF) return fail(EFFSC_INVALID_ARG, "kind must be ML, IP or COEF");
+    int want = kind == EFFSC_ML ? 1 : kind == EFFSC_IP ? 2 : -1;
+    if ((want > 0 && n_tables != want) || n_tables < 1 || n_tables > 3) return fail(EFFSC_INVALID_ARG, "wrong number of tables");
+    if (kind == EFFSC_IP && lens[0] != lens[1]) return fail(EFFSC_PANIC, "a and b must have equal length");
+    if (kind == EFFSC_COEF)
+        for (int i = 1; i < n_tables; i++)
+            if (lens[i] != lens[0]) return fail(EFFSC_PANIC, "pairwise tables must have equal length");
+    CK(cudaSetDevice(ctx->device));
+    effsc_prover* P = new effsc_prover();
+    P->ctx = ctx; P->kind = kind; P->order = order; P->field = field; P->repr = EFFSC_CANONICAL; P->ntab = n_tables;
+    int rc = prover_common_init(P);
+    for (int i = 0; i < n_tables && rc == EFFSC_OK; i++) {
+        if (ncomp[i] != 1 && ncomp[i] != 3) { rc = fail(EFFSC_INVALID_ARG, "ncomp must be 1 or 3"); break; }
+        Buf b;
+        b.owned = false;
+        b.cap = lens[i];
+        b.ext = ncomp[i] == 3;
+        b.p[0] = (u64*)dev_tables[i];
+        if (b.ext) { b.p[1] = b.p[0] + lens[i]; b.p[2] = b.p[0] + 2 * lens[i]; }
+        Table& T = P->t[i];
+        T.bufs.assign(1, b);
+        T.cur = 0;
+        T.len = lens[i];
+        T.ext = b.ext;
+    }
+    if (rc == EFFSC_OK) {
+        bool any = false, all = true;
+        for (int i = 0; i < n_tables; i++) { any |= P->t[i].ext; all &= P->t[i].ext; }
+        bool coef_eq_shape = kind == EFFSC_COEF && n_tables == 3 && P->t[0].ext && !P->t[1].ext && !P->t[2].ext;
+        if (any && !all && !coef_eq_shape) rc = fail(EFFSC_UNSUPPORTED, "mixed base/Fp3 device tables: pass all tables in one field");
+    }
+    if (rc != EFFSC_OK) { release_prover(P); return rc; }
+    snapshot_initial(P);
+    *out = P;
+    return EFFSC_OK;
+}
+
+int effsc_eqf_create(effsc_ctx* ctx, int field, int repr, const uint64_t* w, size_t num_vars, const uint64_t* pv,
+                     size_t p_len, int p_ncomp, effsc_prover** out) {
+    if (!ctx || !out || (num_vars && !w) || (p_len && !pv)) return fail(EFFSC_INVALID_ARG, "NULL argument");
+    TRY(check_field(field));
+    if (num_vars > 40) return fail(EFFSC_INVALID_ARG, "num_vars too large");
+    if (p_ncomp != 1 && p_ncomp != 3) return fail(EFFSC_INVALID_ARG, "p_ncomp must be 1 or 3");
+    size_t n = (size_t)1 << num_vars;
+    if (p_len > n) return fail(EFFSC_PANIC, "p_evals length %zu exceeds 2^%zu = %zu", p_len, num_vars, n);
+    CK(cudaSetDevice(ctx->device));
+    effsc_prover* P = new effsc_prover();
+    P->ctx = ctx; P->kind = EFFSC_EQF; P->order = EFFSC_MSB; P->field = field; P->repr = repr; P->ntab = 3;
+    P->v = num_vars; P->v_l = num_vars / 2;
+    int rc = prover_common_init(P);
+    cudaStream_t s = ctx->stream;
+    // p, zero-padded to 2^v
+    if (rc == EFFSC_OK) {
+        std::vector<uint64_t> padded;
+        const uint64_t* src = pv;
+        if (p_len < n) {
+            padded.assign(n * (size_t)p_ncomp, 0);
+            if (p_len) memcpy(padded.data(), pv, p_len * (size_t)p_ncomp * sizeof(uint64_t));
+            if (repr == EFFSC_MONTGOMERY) { /* zero is zero in both encodings */ }
+            src = padded.data();
+        }
+        rc = upload_table(P, P->t[0], src, n, p_ncomp, repr);
+    }
+    // eq_l, eq_r built on the device from w (src/provers/eq_factored.rs:100-103)
+    std::vector<u64> wc(3 * (num_vars ? num_vars : 1), 0);
+    bool wext = false;
+    for (size_t j = 0; j < num_vars; j++) {
+        HF x = load_elem(w + j * (size_t)field, field, repr);
+        wc[3 * j] = x.c[0]; wc[3 * j + 1] = x.c[1]; wc[3 * j + 2] = x.c[2];
+        wext |= hf_is_ext(x);
+    }
+    u64* dw = nullptr;
+    if (rc == EFFSC_OK) {
+        cudaError_t e = cudaMallocAsync((void**)&dw, wc.size() * sizeof(u64), s);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(dw, wc.data(), wc.size() * sizeof(u64), cudaMemcpyHostToDevice, s);
+        if (e != cudaSuccess) rc = fail(EFFSC_CUDA_ERROR, "w upload: %s", cudaGetErrorString(e));
+    }
+    for (int h = 0; h < 2 && rc == EFFSC_OK; h++) {
+        size_t vv = h == 0 ? P->v_l : num_vars - P->v_l;
+        size_t off = h == 0 ? 0 : P->v_l;
+        Buf b;
+        rc = alloc_buf(P, b, (size_t)1 << vv, wext);
+        if (rc != EFFSC_OK) break;
+        launch_build_eq(dw + 3 * off, (u32)vv, wext, b.p[0], b.p[1], b.p[2], s);
+        g_launches++;
+        Table& T = P->t[1 + h];
+        T.bufs.assign(1, b);
+        T.cur = 0;
+        T.len = (size_t)1 << vv;
+        T.ext = wext;
+    }
+    if (dw) cudaFreeAsync(dw, s);
+    if (rc == EFFSC_OK) rc = normalize_masks(P);
+    if (rc == EFFSC_OK) { cudaError_t e = cudaStreamSynchronize(s); if (e != cudaSuccess) rc = fail(EFFSC_CUDA_ERROR, "%s", cudaGetErrorString(e)); }
+    if (rc != EFFSC_OK) { release_prover(P); return rc; }
+    snapshot_initial(P);
+    *out = P;
+    return EFFSC_OK;
+}
+
+int effsc_prover_destroy(effsc_prover* p) {
+    release_prover(p);
+    return EFFSC_OK;
+}
+
+int effsc_prover_degree(const effsc_prover* p) { return p ? degree_of(p) : -1; }
+
+int effsc_prover_round(effsc_prover* P, const uint64_t* challenge, uint64_t* out_evals, uint64_t* out_aux) {
+    if (!P) return fail(EFFSC_INVALID_ARG, "prover is NULL");
+    CK(cudaSetDevice(P->ctx->device));
+    Chal ch = host_chal(P, challenge);
+    TxIO tx;
+    memset(&tx, 0, sizeof tx);
+    TRY(do_round(P, ch, tx, false));
+    CK(cudaStreamSynchronize(P->ctx->stream));
+    int d = degree_of(P);
+    const u64* r = P->h_res;
+    if (out_evals)
+        for (int i = 0; i < d; i++) store_elem(out_evals + (size_t)i * P->field, hf(r[3 * i], r[3 * i + 1], r[3 * i + 2]), P->field, P->repr);
+    if (out_aux)
+        for (int i = 0; i < 2; i++) {
+            const u64* q = r + 3 * d + 3 * i;
+            store_elem(out_aux + (size_t)i * P->field, hf(q[0], q[1], q[2]), P->field, P->repr);
+        }
+    return EFFSC_OK;
+}
+
+int effsc_prover_finalize(effsc_prover* P, const uint64_t* challenge) {
+    if (!P || !challenge) return fail(EFFSC_INVALID_ARG, "NULL argument");
+    CK(cudaSetDevice(P->ctx->device));
+    TRY(do_finalize(P, host_chal(P, challenge), false));
+    CK(cudaStreamSynchronize(P->ctx->stream));
+    return EFFSC_OK;
+}
+
+int effsc_prover_final_value(effsc_prover* P, uint64_t* out) {
+    if (!P || !out) return fail(EFFSC_INVALID_ARG, "NULL argument");
+    CK(cudaSetDevice(P->ctx->device));
+    HF v;
+    TRY(final_value(P, &v));
+    store_elem(out, v, P->field, P->repr);
+    return EFFSC_OK;
+}
+
+int effsc_prover_table_len(const effsc_prover* P, int table, size_t* out) {
+    if (!P || !out) return fail(EFFSC_INVALID_ARG, "NULL argument");
+    int nt = P->kind == EFFSC_EQF ? 3 : P->ntab;
+    if (table < 0 || table >= nt) return fail(EFFSC_INVALID_ARG, "table index out of range");
+    *out = P->t[table].len;
+    return EFFSC_OK;
+}
+
+int effsc_prover_read_table(effsc_prover* P, int table, uint64_t* out) {
+    size_t n;
+    TRY(effsc_prover_table_len(P, table, &n));
+    if (!n) return EFFSC_OK;
+    if (!out) return fail(EFFSC_INVALID_ARG, "out is NULL");
+    CK(cudaSetDevice(P->ctx->device));
+    cudaStream_t s = P->ctx->stream;
+    Table& T = P->t[table];
+    const Buf& b = T.bufs[T.cur];
+    u64* stage = nullptr;
+    CK(cudaMallocAsync((void**)&stage, n * (size_t)P->field * sizeof(u64), s));
+    launch_join_aos(b.p[0], T.ext ? b.p[1] : nullptr, T.ext ? b.p[2] : nullptr, n, P->field, stage,
+                    P->repr == EFFSC_MONTGOMERY, s);
+    g_launches++;
+    CK(cudaMemcpyAsync(out, stage, n * (size_t)P->field * sizeof(u64), cudaMemcpyDeviceToHost, s));
+    CK(cudaFreeAsync(stage, s));
+    CK(cudaStreamSynchronize(s));
+    return EFFSC_OK;
+}
+
+int effsc_prover_reset(effsc_prover* P) {
+    if (!P) return fail(EFFSC_INVALID_ARG, "prover is NULL");
+    for (int i = 0; i < 3; i++) {
+        if (P->t[i].bufs.empty()) continue;
+        P->t[i].cur = 0;
+        P->t[i].len = P->len0[i];
+        P->t[i].ext = P->ext0[i];
+    }
+    P->rounds = 0;
+    return EFFSC_OK;
+}
+
+int effsc_prove(effsc_prover* P, size_t num_rounds, effsc_transcript* T, const uint8_t* hook, size_t hook_len,
+                int use_graph, uint64_t* round_polys, uint64_t* challenges, uint64_t* final_value_out) {
+    if (!P || !T) return fail(EFFSC_INVALID_ARG, "NULL argument");
+    if (T->kind != EFFSC_T_KECCAK) return fail(EFFSC_UNSUPPORTED, "the device path needs a Keccak transcript");
+    if (T->field != P->field) return fail(EFFSC_INVALID_ARG, "transcript field differs from the prover field");
+    if (hook_len && !hook) return fail(EFFSC_INVALID_ARG, "hook is NULL");
+    CK(cudaSetDevice(P->ctx->device));
+    cudaStream_t s = P->ctx->stream;
+    const int d = degree_of(P);
+    // device buffers for the proof and the transcript
+    if (!P->d_tx) CK(cudaMallocAsync((void**)&P->d_tx, sizeof(DevTranscript), s));
+    if (hook_len > P->hook_cap) {
+        if (P->d_hook) CK(cudaFreeAsync(P->d_hook, s));
+        CK(cudaMallocAsync((void**)&P->d_hook, hook_len, s));
+        P->hook_cap = hook_len;
+        if (P->gexec) { cudaGraphExecDestroy(P->gexec); P->gexec = nullptr; }
+    }
+    if (num_rounds > P->rounds_cap || !P->d_wire) {
+        if (P->d_wire) CK(cudaFreeAsync(P->d_wire, s));
+        if (P->d_chals) CK(cudaFreeAsync(P->d_chals, s));
+        size_t cap = std::max<size_t>(num_rounds, 1);
+        CK(cudaMallocAsync((void**)&P->d_wire, cap * 9 * sizeof(u64), s));
+        CK(cudaMallocAsync((void**)&P->d_chals, cap * 3 * sizeof(u64), s));
+        P->rounds_cap = cap;
+        if (P->gexec) { cudaGraphExecDestroy(P->gexec); P->gexec = nullptr; }
+    }
+    CK(cudaMemcpyAsync(P->d_tx, &T->st, sizeof(DevTranscript), cudaMemcpyHostToDevice, s));
+    if (hook_len) CK(cudaMemcpyAsync(P->d_hook, hook, hook_len, cudaMemcpyHostToDevice, s));
+
+    bool at_reset = P->rounds == 0;
+    for (int i = 0; i < 3; i++)
+        if (!P->t[i].bufs.empty() && (P->t[i].cur != 0 || P->t[i].len != P->len0[i])) at_reset = false;
+
+    auto launch_all = [&](bool dry) -> int {
+        for (size_t r = 0; r < num_rounds; r++) {
+            Chal ch;
+            if (r > 0) { ch.has = true; ch.ext = P->field == EFFSC_FP3; ch.dev = P->d_chals + 3 * (r - 1); }
+            TxIO tx;
+            tx.tx = P->d_tx;
+            tx.hook = P->d_hook;
+            tx.hook_len = (u32)hook_len;
+            tx.proof_wire = P->d_wire + (size_t)r * 3 * d;
+            tx.proof_chal = P->d_chals + 3 * r;
+            tx.chal_next = nullptr;
+            TRY(do_round(P, ch, tx, dry));
+        }
+        if (num_rounds) {
+            Chal ch;
+            ch.has = true; ch.ext = P->field == EFFSC_FP3; ch.dev = P->d_chals + 3 * (num_rounds - 1);
+            TRY(do_finalize(P, ch, dry));
+        }
+        return EFFSC_OK;
+    };
+
+    if (use_graph && at_reset && P->gexec && P->g_rounds == num_rounds && P->g_hook == hook_len) {
+        CK(cudaGraphLaunch(P->gexec, s));
+        g_launches += P->g_kernels;
+        for (int i = 0; i < 3; i++) { P->t[i].cur = P->g_post[i].cur; P->t[i].len = P->g_post[i].len; P->t[i].ext = P->g_post[i].ext; }
+        P->rounds = P->g_post_rounds;
+    } else if (use_graph) {
+        // plan once without launching so that every buffer exists before capture
+        TabState pre[3];
+        for (int i = 0; i < 3; i++) pre[i] = {P->t[i].cur, P->t[i].len, P->t[i].ext};
+        size_t pre_rounds = P->rounds;
+        TRY(launch_all(true));
+        for (int i = 0; i < 3; i++) { P->t[i].cur = pre[i].cur; P->t[i].len = pre[i].len; P->t[i].ext = pre[i].ext; }
+        P->rounds = pre_rounds;
+        CK(cudaStreamSynchronize(s));
+        cudaGraph_t graph;
+        CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+        uint64_t before = g_launches;
+        g_capturing = true;
+        int rc = launch_all(false);
+        g_capturing = false;
+        cudaError_t ec = cudaStreamEndCapture(s, &graph);
+        if (rc != EFFSC_OK) return rc;
+        if (ec != cudaSuccess) return fail(EFFSC_CUDA_ERROR, "graph capture: %s", cudaGetErrorString(ec));
+        cudaGraphExec_t ge;
+        ec = cudaGraphInstantiate(&ge, graph, 0);
+        cudaGraphDestroy(graph);
+        if (ec != cudaSuccess) return fail(EFFSC_CUDA_ERROR, "graph instantiate: %s", cudaGetErrorString(ec));
+        CK(cudaGraphLaunch(ge, s));
+        if (at_reset) {
+            P->g_kernels = g_launches - before;
+            if (P->gexec) cudaGraphExecDestroy(P->gexec);
+            P->gexec = ge;
+            P->g_rounds = num_rounds;
+            P->g_hook = hook_len;
+            for (int i = 0; i < 3; i++) P->g_post[i] = {P->t[i].cur, P->t[i].len, P->t[i].ext};
+            P->g_post_rounds = P->rounds;
+        } else {
+            CK(cudaStreamSynchronize(s));
+            cudaGraphExecDestroy(ge);
+        }
+    } else {
+        TRY(launch_all(false));
+    }
+    // results
+    std::vector<u64> wire(num_rounds * 3 * d), chal(num_rounds * 3);
+    if (num_rounds) {
+        CK(cudaMemcpyAsync(wire.data(), P->d_wire, wire.size() * sizeof(u64), cudaMemcpyDeviceToHost, s));
+        CK(cudaMemcpyAsync(chal.data(), P->d_chals, chal.size() * sizeof(u64), cudaMemcpyDeviceToHost, s));
+    }
+    CK(cudaMemcpyAsync(&T->st, P->d_tx, sizeof(DevTranscript), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    for (size_t r = 0; r < num_rounds; r++) {
+        if (round_polys)
+            for (int i = 0; i < d; i++) {
+                const u64* q = &wire[(r * d + i) * 3];
+                store_elem(round_polys + (r * d + i) * P->field, hf(q[0], q[1], q[2]), P->field, P->repr);
+            }
+        if (challenges) store_elem(challenges + r * P->field, hf(chal[3 * r], chal[3 * r + 1], chal[3 * r + 2]), P->field, P->repr);
+    }
+    if (final_value_out) {
+        HF v;
+        TRY(final_value(P, &v));
+        store_elem(final_value_out, v, P->field, P->repr);
+    }
+    return EFFSC_OK;
+}
+
+// ---- transcripts -----------------------------------------------------------
+int effsc_transcript_create(int kind, int field, int repr, const uint8_t* label, size_t label_len, uint64_t seed,
+                            effsc_transcript** out) {
+    if (!out) return fail(EFFSC_INVALID_ARG, "out is NULL");
+    TRY(check_field(field));
+    if (kind != EFFSC_T_KECCAK && kind != EFFSC_T_TEST) return fail(EFFSC_INVALID_ARG, "unknown transcript kind");
+    if (label_len && !label) return fail(EFFSC_INVALID_ARG, "label is NULL");
+    effsc_transcript* t = new effsc_transcript();
+    memset(&t->st, 0, sizeof t->st);
+    t->kind = kind;
+    t->field = field;
+    t->repr = repr;
+    t->st.deg = (u32)field;
+    t->sm = seed;
+    if (kind == EFFSC_T_KECCAK) {
+        uint8_t l8[8];
+        for (int i = 0; i < 8; i++) l8[i] = (uint8_t)((uint64_t)label_len >> (8 * i));
+        tx_h_absorb(t, l8, 8);
+        tx_h_absorb(t, label, label_len);
+    }
+    *out = t;
+    return EFFSC_OK;
+}
+int effsc_transcript_destroy(effsc_transcript* t) { delete t; return EFFSC_OK; }
+int effsc_transcript_clone(const effsc_transcript* t, effsc_transcript** out) {
+    if (!t || !out) return fail(EFFSC_INVALID_ARG, "NULL argument");
+    *out = new effsc_transcript(*t);
+    return EFFSC_OK;
+}
+int effsc_transcript_absorb(effsc_transcript* t, const uint8_t* b, size_t n) {
+    if (!t || (n && !b)) return fail(EFFSC_INVALID_ARG, "NULL argument");
+    tx_h_absorb(t, b, n);
+    return EFFSC_OK;
+}
+int effsc_transcript_squeeze(effsc_transcript* t, uint8_t* out, size_t n) {
+    if (!t || (n && !out)) return fail(EFFSC_INVALID_ARG, "NULL argument");
+    if (t->kind != EFFSC_T_KECCAK) return fail(EFFSC_UNSUPPORTED, "squeeze needs a Keccak transcript");
+    tx_h_squeeze(t, out, n);
+    return EFFSC_OK;
+}
+int effsc_transcript_send(effsc_transcript* t, const uint64_t* v) {
+    if (!t || !v) return fail(EFFSC_INVALID_ARG, "NULL argument");
+    tx_h_send(t, load_elem(v, t->field, t->repr));
+    return EFFSC_OK;
+}
+int effsc_transcript_challenge(effsc_transcript* t, uint64_t* out) {
+    if (!t || !out) return fail(EFFSC_INVALID_ARG, "NULL argument");
+    store_elem(out, tx_h_challenge(t), t->field, t->repr);
+    return EFFSC_OK;
+}
+
+// ---- verifier (src/verifier.rs:61-184) -------------------------------------
+int effsc_verify(int field, int repr, const uint64_t* claimed_sum, size_t degree, size_t num_rounds,
+                 effsc_transcript* t, const uint8_t* hook, size_t hook_len, const uint64_t* round_polys,
+                 uint64_t* challenges, uint64_t* final_claim) {
+    if (!t || !claimed_sum || (num_rounds && !round_polys) || !final_claim) return fail(EFFSC_INVALID_ARG, "NULL argument");
+    TRY(check_field(field));
+    if (degree > 8) return fail(EFFSC_INVALID_ARG, "degree too large");
+    HF claim = load_elem(claimed_sum, field, repr);
+    const size_t dd = degree, n_wire = dd > 1 ? dd : 1;
+    for (size_t round = 0; round < num_rounds; round++) {
+        HF recv[8];
+        for (size_t i = 0; i < n_wire; i++) {
+            recv[i] = load_elem(round_polys + (round * n_wire + i) * (size_t)field, field, repr);
+            tx_h_send(t, recv[i]);
+        }
+        HF h0 = recv[0], h1 = hf_sub(claim, h0);
+        if (hook_len) tx_h_absorb(t, hook, hook_len);
+        HF r = tx_h_challenge(t);
+        if (challenges) store_elem(challenges + round * (size_t)field, r, field, repr);
+        if (dd == 0) { claim = h0; continue; }
+        HF hinf = dd >= 2 ? recv[1] : hf_sub(h1, h0);
+        HF q[8];
+        q[0] = h0;
+        q[1] = hf_sub(h1, hinf);
+        for (size_t i = 2; i < dd; i++) {
+            HF id = hf(1), fi = hf_from_u64(i);
+            for (size_t k = 0; k < dd; k++) id = hf_mul(id, fi);
+            q[i] = hf_sub(recv[i], hf_mul(hinf, id));
+        }
+        HF qr;
+        if (dd == 1) qr = q[0];
+        else if (dd == 2) qr = hf_add(q[0], hf_mul(r, hf_sub(q[1], q[0])));
+        else {
+            // Lagrange at {0..dd-1} with barycentric weights prod_{j != i} (i - j)
+            HF pre[9], suf[9], rm[8];
+            for (size_t j = 0; j < dd; j++) rm[j] = hf_sub(r, hf_from_u64(j));
+            pre[0] = hf(1);
+            for (size_t i = 0; i < dd; i++) pre[i + 1] = hf_mul(pre[i], rm[i]);
+            suf[dd] = hf(1);
+            for (size_t i = dd; i-- > 0;) suf[i] = hf_mul(suf[i + 1], rm[i]);
+            qr = hf(0);
+            for (size_t i = 0; i < dd; i++) {
+                u64 w = 1;
+                for (size_t j = 0; j < dd; j++) {
+                    if (j == i) continue;
+                    long long diff = (long long)i - (long long)j;
+                    w = h_mul(w, diff > 0 ? (u64)diff : h_sub(0, (u64)(-diff)));
+                }
+                qr = hf_add(qr, hf_mul(hf_mul(q[i], hf_mul(pre[i], suf[i + 1])), hf(h_inv(w))));
+            }
+        }
+        HF rd = hf(1);
+        for (size_t k = 0; k < dd; k++) rd = hf_mul(rd, r);
+        claim = hf_add(qr, hf_mul(hinf, rd));
+    }
+    store_elem(final_claim, claim, field, repr);
+    return EFFSC_OK;
+}
+
+// ---- standalone fold, eq table, generator ------------------------------------
+int effsc_fold(effsc_ctx* ctx, int field, int repr, const uint64_t* values, size_t len, int ncomp,
+               const uint64_t* weight, uint64_t* out, size_t* out_len) {
+    if (!ctx || !weight || !out_len || (len && (!values || !out))) return fail(EFFSC_INVALID_ARG, "NULL argument");
+    const uint64_t* tabs[1] = {values};
+    size_t lens[1] = {len};
+    int nc[1] = {ncomp};
+    effsc_prover* P = nullptr;
+    TRY(effsc_prover_create(ctx, EFFSC_ML, EFFSC_MSB, field, repr, 1, tabs, lens, nc, &P));
+    int rc = do_finalize(P, host_chal(P, weight), false);
+    if (rc == EFFSC_OK) {
+        *out_len = P->t[0].len;
+        rc = effsc_prover_read_table(P, 0, out);
+    }
+    release_prover(P);
+    return rc;
+}
+
+int effsc_build_eq_table(effsc_ctx* ctx, int field, int repr, const uint64_t* w, size_t num_vars, uint64_t* out) {
+    if (!ctx || !out || (num_vars && !w)) return fail(EFFSC_INVALID_ARG, "NULL argument");
+    TRY(check_field(field));
+    if (num_vars > 34) return fail(EFFSC_INVALID_ARG, "num_vars too large");
+    CK(cudaSetDevice(ctx->device));
+    cudaStream_t s = ctx->stream;
+    std::vector<u64> wc(3 * (num_vars ? num_vars : 1), 0);
+    bool ext = false;
+    for (size_t j = 0; j < num_vars; j++) {
+        HF x = load_elem(w + j * (size_t)field, field, repr);
+        for (int c = 0; c < 3; c++) wc[3 * j + c] = x.c[c];
+        ext |= hf_is_ext(x);
+    }
+    size_t n = (size_t)1 << num_vars;
+    u64 *dw = nullptr, *c0 = nullptr, *c1 = nullptr, *c2 = nullptr, *stage = nullptr;
+    CK(cudaMallocAsync((void**)&dw, wc.size() * sizeof(u64), s));
+    CK(cudaMemcpyAsync(dw, wc.data(), wc.size() * sizeof(u64), cudaMemcpyHostToDevice, s));
+    CK(cudaMallocAsync((void**)&c0, n * sizeof(u64), s));
+    if (ext) { CK(cudaMallocAsync((void**)&c1, n * sizeof(u64), s)); CK(cudaMallocAsync((void**)&c2, n * sizeof(u64), s)); }
+    launch_build_eq(dw, (u32)num_vars, ext, c0, c1, c2, s);
+    g_launches++;
+    CK(cudaMallocAsync((void**)&stage, n * (size_t)field * sizeof(u64), s));
+    launch_join_aos(c0, c1, c2, n, field, stage, repr == EFFSC_MONTGOMERY, s);
+    g_launches++;
+    CK(cudaMemcpyAsync(out, stage, n * (size_t)field * sizeof(u64), cudaMemcpyDeviceToHost, s));
+    cudaFreeAsync(dw, s); cudaFreeAsync(c0, s); if (c1) cudaFreeAsync(c1, s); if (c2) cudaFreeAsync(c2, s); cudaFreeAsync(stage, s);
+    CK(cudaStreamSynchronize(s));
+    return EFFSC_OK;
+}
+
+uint64_t effsc_table_seed(uint64_t seed, uint64_t table) {
+    u64 z = seed + (table + 1) * 0x632BE59BD9B4E019ULL;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+    return z ^ (z >> 31);
+}
+
+int effsc_gen_uniform(effsc_ctx* ctx, uint64_t seed, uint64_t n, uint64_t* dev_out, uint64_t* host_out) {
+    if (!ctx || (!dev_out && !host_out)) return fail(EFFSC_INVALID_ARG, "NULL argument");
+    CK(cudaSetDevice(ctx->device));
+    cudaStream_t s = ctx->stream;
+    u64* d = (u64*)dev_out;
+    if (!d) CK(cudaMallocAsync((void**)&d, (n ? n : 1) * sizeof(u64), s));
+    launch_gen_uniform(seed, n, d, s);
+    g_launches++;
+    if (host_out && n) CK(cudaMemcpyAsync(host_out, d, n * sizeof(u64), cudaMemcpyDeviceToHost, s));
+    if (!dev_out) CK(cudaFreeAsync(d, s));
+    CK(cudaStreamSynchronize(s));
+    return EFFSC_OK;
+}
+
+int effsc_device_alloc(effsc_ctx* ctx, size_t bytes, void** out) {
+    if (!ctx || !out) return fail(EFFSC_INVALID_ARG, "NULL argument");
+    CK(cudaSetDevice(ctx->device));
+    cudaError_t e = cudaMalloc(out, bytes ? bytes : 1);
+    if (e != cudaSuccess) return fail(EFFSC_OOM, "cudaMalloc(%zu): %s", bytes, cudaGetErrorString(e));
+    return EFFSC_OK;
+}
+int effsc_device_free(effsc_ctx* ctx, void* p) {
+    if (!ctx) return fail(EFFSC_INVALID_ARG, "NULL argument");
+    CK(cudaSetDevice(ctx->device));
+    CK(cudaFree(p));
+    return EFFSC_OK;
+}
+int effsc_memcpy_h2d(effsc_ctx* ctx, void* dst, const void* src, size_t bytes) {
+    if (!ctx) return fail(EFFSC_INVALID_ARG, "NULL argument");
+    CK(cudaSetDevice(ctx->device));
+    CK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return EFFSC_OK;
+}
+int effsc_memcpy_d2h(effsc_ctx* ctx, void* dst, const void* src, size_t bytes) {
+    if (!ctx) return fail(EFFSC_INVALID_ARG, "NULL argument");
+    CK(cudaSetDevice(ctx->device));
+    CK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return EFFSC_OK;
+}
+
+}  // extern "C"

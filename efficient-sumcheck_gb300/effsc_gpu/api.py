@@ -1,0 +1,504 @@
+"""Python mirror of the effsc crate API over the GPU C ABI.
+
+Names, argument meaning and error behaviour follow the Rust crate
+(compsec-epfl/efficient-sumcheck):
+
+  * provers: MultilinearProver[LSB] (src/provers/multilinear*.rs),
+    InnerProductProver[LSB] (src/provers/inner_product*.rs),
+    CoefficientProver[LSB] with the device product evaluator
+    (src/provers/coefficient*.rs), EqFactoredProver (src/provers/eq_factored.rs);
+    each exposes degree() / round(challenge) / finalize(r) / final_value()
+    (the SumcheckProver trait, src/sumcheck_prover.rs:36-71) and the
+    reference's post-state accessors;
+  * sumcheck(prover, num_rounds, transcript, hook) -- src/runner.rs:29-69;
+  * SumcheckProof -- src/proof.rs:18-34;
+  * sumcheck_verify -- src/verifier.rs:61-139;
+  * fold -- src/fold.rs:14;
+  * the legacy runners inner_product_sumcheck[_partial] and
+    multilinear_sumcheck[_partial] (src/lib.rs:51-57).
+
+Field elements are numpy uint64 arrays: an element of F = Fp is one word, an
+element of F = Fp3 is three words [c0, c1, c2].  Tables are 1-D (base field,
+the embedded elements) or (n, 3) arrays (Fp3).
+"""
+import ctypes
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _lib
+from ._lib import check, load, u64p, u8p, vp
+
+ML, IP, COEF, EQF = 0, 1, 2, 3
+MSB, LSB = 0, 1
+FP, FP3 = 1, 3
+CANONICAL, MONTGOMERY = 0, 1
+T_KECCAK, T_TEST = 0, 1
+
+P = 0xFFFFFFFF00000001
+
+
+def _p(a):
+    return a.ctypes.data_as(u64p)
+
+
+def _bytes(b):
+    b = bytes(b)
+    buf = (ctypes.c_uint8 * max(1, len(b))).from_buffer_copy(b if b else b"\0")
+    return buf, len(b)
+
+
+class Context:
+    """One GPU and one CUDA stream (effsc_ctx)."""
+    _default = None
+
+    def __init__(self, device=0):
+        L = load()
+        h = vp()
+        check(L.effsc_ctx_create(device, ctypes.byref(h)))
+        self.h = h
+        self.device = device
+
+    @classmethod
+    def default(cls):
+        if cls._default is None:
+            cls._default = Context(0)
+        return cls._default
+
+    def synchronize(self):
+        check(load().effsc_ctx_synchronize(self.h))
+
+    def set_stream(self, stream_handle):
+        check(load().effsc_ctx_set_stream(self.h, stream_handle))
+
+
+def launch_count():
+    return int(load().effsc_launch_count())
+
+
+def launch_count_reset():
+    load().effsc_launch_count_reset()
+
+
+def _elem(v, field):
+    """Coerce one field element to a uint64 array of `field` words."""
+    a = np.ascontiguousarray(np.asarray(v, dtype=np.uint64).reshape(-1))
+    if a.size == field:
+        return a
+    if a.size == 1 and field == 3:
+        return np.array([a[0], 0, 0], dtype=np.uint64)
+    if a.size == 3 and field == 1:
+        if a[1] or a[2]:
+            raise ValueError("Fp3 value for an Fp prover")
+        return a[:1].copy()
+    raise ValueError("bad field element shape %s" % (a.shape,))
+
+
+# ---------------------------------------------------------------------------
+# transcripts
+# ---------------------------------------------------------------------------
+class Transcript:
+    """ProverTranscript / VerifierTranscript (src/transcript/transcript.rs)."""
+
+    def __init__(self, field=FP3, label=b"", kind=T_KECCAK, seed=0, repr=CANONICAL, _h=None):
+        self.field, self.repr, self.kind = field, repr, kind
+        if _h is not None:
+            self.h = _h
+            return
+        b, n = _bytes(label)
+        h = vp()
+        check(load().effsc_transcript_create(kind, field, repr, b, n, seed, ctypes.byref(h)))
+        self.h = h
+
+    @classmethod
+    def keccak(cls, field, label, repr=CANONICAL):
+        return cls(field, label, T_KECCAK, 0, repr)
+
+    @classmethod
+    def test(cls, field, seed, repr=CANONICAL):
+        """SanityTranscript semantics (src/transcript/sanity.rs): no-op sends."""
+        return cls(field, b"", T_TEST, seed, repr)
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib._lib is not None:
+            _lib._lib.effsc_transcript_destroy(self.h)
+            self.h = None
+
+    def clone(self):
+        h = vp()
+        check(load().effsc_transcript_clone(self.h, ctypes.byref(h)))
+        return Transcript(self.field, repr=self.repr, kind=self.kind, _h=h)
+
+    def absorb(self, data):
+        b, n = _bytes(data)
+        check(load().effsc_transcript_absorb(self.h, b, n))
+
+    def squeeze(self, n):
+        out = (ctypes.c_uint8 * n)()
+        check(load().effsc_transcript_squeeze(self.h, out, n))
+        return bytes(out)
+
+    def send(self, value):
+        v = _elem(value, self.field)
+        check(load().effsc_transcript_send(self.h, _p(v)))
+
+    def challenge(self):
+        out = np.zeros(self.field, dtype=np.uint64)
+        check(load().effsc_transcript_challenge(self.h, _p(out)))
+        return out
+
+
+@dataclass
+class SumcheckProof:
+    """src/proof.rs:18-34 (EvalsInfty round polynomials)."""
+    round_polys: np.ndarray   # (num_rounds, degree, field)
+    challenges: np.ndarray    # (num_rounds, field)
+    final_value: np.ndarray   # (field,)
+
+
+# ---------------------------------------------------------------------------
+# provers
+# ---------------------------------------------------------------------------
+def _as_table(t, field):
+    a = np.ascontiguousarray(np.asarray(t, dtype=np.uint64))
+    if a.ndim == 1:
+        return a, 1
+    if a.ndim == 2 and a.shape[1] == 3:
+        if field != FP3:
+            raise ValueError("Fp3 table for an Fp prover")
+        return a, 3
+    raise ValueError("table must be (n,) base words or (n, 3) Fp3 words")
+
+
+class _Prover:
+    kind = None
+    order = MSB
+
+    def __init__(self, tables, field=FP3, repr=CANONICAL, ctx=None, _h=None):
+        self.ctx = ctx or Context.default()
+        self.field, self.repr = field, repr
+        if _h is not None:
+            self.h = _h
+            return
+        arrs = [_as_table(t, field) for t in tables]
+        n = len(arrs)
+        ptrs = (u64p * n)(*[_p(a) for a, _ in arrs])
+        lens = (ctypes.c_size_t * n)(*[a.shape[0] for a, _ in arrs])
+        nc = (ctypes.c_int * n)(*[c for _, c in arrs])
+        h = vp()
+        check(load().effsc_prover_create(self.ctx.h, self.kind, self.order, field, repr, n, ptrs, lens, nc,
+                                         ctypes.byref(h)))
+        self.h = h
+
+    @classmethod
+    def from_device(cls, dev_tables, lens, ncomp, field=FP3, ctx=None):
+        """Construct on device-resident canonical SoA tables (not copied)."""
+        ctx = ctx or Context.default()
+        n = len(dev_tables)
+        ptrs = (u64p * n)(*[ctypes.cast(ctypes.c_void_p(int(p)), u64p) for p in dev_tables])
+        ls = (ctypes.c_size_t * n)(*lens)
+        nc = (ctypes.c_int * n)(*ncomp)
+        h = vp()
+        check(load().effsc_prover_create_device(ctx.h, cls.kind, cls.order, field, n, ptrs, ls, nc, ctypes.byref(h)))
+        obj = cls.__new__(cls)
+        _Prover.__init__(obj, None, field, CANONICAL, ctx, _h=h)
+        return obj
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib._lib is not None:
+            _lib._lib.effsc_prover_destroy(self.h)
+            self.h = None
+
+    def degree(self):
+        return int(load().effsc_prover_degree(self.h))
+
+    def round(self, challenge=None, aux=False):
+        d = self.degree()
+        out = np.zeros((d, self.field), dtype=np.uint64)
+        ax = np.zeros((2, self.field), dtype=np.uint64)
+        c = _elem(challenge, self.field) if challenge is not None else None
+        check(load().effsc_prover_round(self.h, _p(c) if c is not None else None, _p(out), _p(ax)))
+        return (out, ax) if aux else out
+
+    def finalize(self, challenge):
+        c = _elem(challenge, self.field)
+        check(load().effsc_prover_finalize(self.h, _p(c)))
+
+    def final_value(self):
+        out = np.zeros(self.field, dtype=np.uint64)
+        check(load().effsc_prover_final_value(self.h, _p(out)))
+        return out
+
+    def table_len(self, i):
+        n = ctypes.c_size_t()
+        check(load().effsc_prover_table_len(self.h, i, ctypes.byref(n)))
+        return n.value
+
+    def table(self, i):
+        n = self.table_len(i)
+        out = np.zeros((n, self.field), dtype=np.uint64)
+        if n:
+            check(load().effsc_prover_read_table(self.h, i, _p(out)))
+        return out if self.field == FP3 else out.reshape(-1)
+
+    def reset(self):
+        check(load().effsc_prover_reset(self.h))
+
+    def prove(self, num_rounds, transcript, hook=b"", use_graph=True):
+        """Whole protocol on the device (effsc_prove) with the device transcript."""
+        d = self.degree()
+        rp = np.zeros((num_rounds, d, self.field), dtype=np.uint64)
+        ch = np.zeros((num_rounds, self.field), dtype=np.uint64)
+        fv = np.zeros(self.field, dtype=np.uint64)
+        hb, hn = _bytes(hook)
+        check(load().effsc_prove(self.h, num_rounds, transcript.h, hb, hn, 1 if use_graph else 0,
+                                 _p(rp), _p(ch), _p(fv)))
+        return SumcheckProof(rp, ch, fv)
+
+
+class MultilinearProver(_Prover):
+    """src/provers/multilinear.rs:25-80."""
+    kind, order = ML, MSB
+
+    def __init__(self, evals, field=FP3, repr=CANONICAL, ctx=None):
+        super().__init__([evals], field, repr, ctx)
+
+    def evals(self):
+        return self.table(0)
+
+    def num_variables(self):
+        n = self.table_len(0)
+        return 0 if n == 0 else (n - 1).bit_length()
+
+
+class MultilinearProverLSB(MultilinearProver):
+    """src/provers/multilinear_lsb.rs:29-194."""
+    kind, order = ML, LSB
+
+
+class InnerProductProver(_Prover):
+    """src/provers/inner_product.rs:26-127."""
+    kind, order = IP, MSB
+
+    def __init__(self, a, b, field=FP3, repr=CANONICAL, ctx=None):
+        super().__init__([a, b], field, repr, ctx)
+
+    def evaluations(self):
+        return self.table(0), self.table(1)
+
+    def final_evaluations(self):
+        if self.table_len(0) == 1:
+            return self.table(0)[0], self.table(1)[0]
+        z = np.zeros(self.field, dtype=np.uint64)
+        return z, z.copy()
+
+
+class InnerProductProverLSB(InnerProductProver):
+    """src/provers/inner_product_lsb.rs:25-178."""
+    kind, order = IP, LSB
+
+
+class CoefficientProver(_Prover):
+    """src/provers/coefficient.rs:18-330 with the device product evaluator:
+    accumulate_pair adds the coefficients of prod_i (lo_i + x (hi_i - lo_i))
+    over the pairwise tables (1 to 3 of them; degree = number of tables)."""
+    kind, order = COEF, MSB
+
+    def __init__(self, pairwise, field=FP3, repr=CANONICAL, ctx=None):
+        super().__init__(list(pairwise), field, repr, ctx)
+
+    def pairwise(self):
+        return [self.table(i) for i in range(self.degree())]
+
+
+class CoefficientProverLSB(CoefficientProver):
+    """src/provers/coefficient_lsb.rs:37-237."""
+    kind, order = COEF, LSB
+
+
+class EqFactoredProver(_Prover):
+    """src/provers/eq_factored.rs:67-289.  Tables: 0 = p, 1 = eq_l, 2 = eq_r."""
+    kind, order = EQF, MSB
+
+    def __init__(self, w, p, field=FP3, repr=CANONICAL, ctx=None):
+        self.ctx = ctx or Context.default()
+        self.field, self.repr = field, repr
+        w = np.ascontiguousarray(np.asarray(w, dtype=np.uint64))
+        if field == FP3 and w.ndim == 1:
+            w3 = np.zeros((w.shape[0], 3), dtype=np.uint64)
+            w3[:, 0] = w
+            w = w3
+        v = w.shape[0]
+        pa, nc = _as_table(p, field)
+        h = vp()
+        check(load().effsc_eqf_create(self.ctx.h, field, repr, _p(np.ascontiguousarray(w.reshape(-1))), v,
+                                      _p(pa), pa.shape[0], nc, ctypes.byref(h)))
+        self.h = h
+
+    def final_factors(self):
+        if self.table_len(0) != 1:
+            z = np.zeros(self.field, dtype=np.uint64)
+            return z, z.copy()
+        from .field import f_mul
+        p0 = self.table(0)[0]
+        e = f_mul(self.table(1)[0], self.table(2)[0], self.field)
+        return p0, e
+
+
+# ---------------------------------------------------------------------------
+# runner, verifier, free functions
+# ---------------------------------------------------------------------------
+def sumcheck(prover, num_rounds, transcript, hook=None):
+    """runner::sumcheck (src/runner.rs:29-69) on the host, one prover round per
+    C-ABI call.  hook(round, transcript) runs after the round's messages."""
+    d = prover.degree()
+    f = prover.field
+    rps = np.zeros((num_rounds, d, f), dtype=np.uint64)
+    chs = np.zeros((num_rounds, f), dtype=np.uint64)
+    prev = None
+    for r in range(num_rounds):
+        evals = prover.round(prev)
+        for v in evals:
+            transcript.send(v)
+        rps[r] = evals
+        if hook is not None:
+            hook(r, transcript)
+        prev = transcript.challenge()
+        chs[r] = prev
+    if prev is not None:
+        prover.finalize(prev)
+    return SumcheckProof(rps, chs, prover.final_value())
+
+
+def noop_hook(_round, _transcript):
+    """src/lib.rs:28-33."""
+
+
+def sumcheck_verify(claimed_sum, degree, num_rounds, transcript, round_polys, hook=b""):
+    """src/verifier.rs:61-139.  Returns (challenges, final_claim)."""
+    f = transcript.field
+    cs = _elem(claimed_sum, f)
+    rp = np.ascontiguousarray(np.asarray(round_polys, dtype=np.uint64))
+    ch = np.zeros((num_rounds, f), dtype=np.uint64)
+    fc = np.zeros(f, dtype=np.uint64)
+    hb, hn = _bytes(hook)
+    check(load().effsc_verify(f, transcript.repr, _p(cs), degree, num_rounds, transcript.h, hb, hn,
+                              _p(rp) if rp.size else None, _p(ch), _p(fc)))
+    return ch, fc
+
+
+def fold(values, weight, field=FP3, repr=CANONICAL, ctx=None):
+    """effsc::fold (src/fold.rs:14): half-split fold with implicit zero padding."""
+    ctx = ctx or Context.default()
+    a, nc = _as_table(values, field)
+    w = _elem(weight, field)
+    n = a.shape[0]
+    out = np.zeros((max(n, 1), field), dtype=np.uint64)
+    ol = ctypes.c_size_t()
+    check(load().effsc_fold(ctx.h, field, repr, _p(a), n, nc, _p(w), _p(out), ctypes.byref(ol)))
+    out = out[: ol.value]
+    return out if field == FP3 else out.reshape(-1)
+
+
+def build_eq_table(w, field=FP3, repr=CANONICAL, ctx=None):
+    """eq(w, .) over {0,1}^v, MSB layout (src/provers/eq_factored.rs:217-239)."""
+    ctx = ctx or Context.default()
+    w = np.ascontiguousarray(np.asarray(w, dtype=np.uint64).reshape(-1))
+    v = w.size // field
+    out = np.zeros(((1 << v), field), dtype=np.uint64)
+    check(load().effsc_build_eq_table(ctx.h, field, repr, _p(w), v, _p(out)))
+    return out if field == FP3 else out.reshape(-1)
+
+
+def gen_uniform(seed, n, ctx=None):
+    """Seeded uniform canonical table (host array)."""
+    ctx = ctx or Context.default()
+    out = np.empty(n, dtype=np.uint64)
+    check(load().effsc_gen_uniform(ctx.h, seed, n, None, _p(out)))
+    return out
+
+
+def table_seed(seed, t):
+    return int(load().effsc_table_seed(seed, t))
+
+
+@dataclass
+class ProductSumcheck:
+    """Legacy return type, src/inner_product_sumcheck.rs:33-37."""
+    prover_messages: list
+    verifier_messages: list
+    final_evaluations: tuple
+    a: np.ndarray = None
+    b: np.ndarray = None
+
+
+@dataclass
+class Sumcheck:
+    """Legacy return type, src/multilinear_sumcheck.rs:31-35."""
+    prover_messages: list
+    verifier_messages: list
+    final_evaluation: np.ndarray
+    values: np.ndarray = None
+
+
+def _rounds_for(n):
+    return 0 if n == 0 else (n - 1).bit_length()
+
+
+def inner_product_sumcheck_partial(a, b, transcript, num_rounds, hook=None, field=FP3):
+    """src/inner_product_sumcheck.rs:507-565: sends (c0, c2) per round."""
+    na = np.asarray(a).shape[0]
+    if np.asarray(b).shape[0] != na:
+        raise _lib.ReferencePanic(6, "a and b must have equal length")
+    if num_rounds and (1 << _rounds_for(na)) < (1 << num_rounds):
+        raise _lib.ReferencePanic(6, "num_rounds (%d) exceeds log2 of next-pow2 of len (%d)" % (num_rounds, na))
+    pr = InnerProductProver(a, b, field=field)
+    msgs, chals, prev = [], [], None
+    for r in range(num_rounds):
+        _, aux = pr.round(prev, aux=True)
+        c0, c2 = aux[0], aux[1]
+        msgs.append((c0, c2))
+        transcript.send(c0)
+        transcript.send(c2)
+        if hook is not None:
+            hook(r, transcript)
+        prev = transcript.challenge()
+        chals.append(prev)
+    if prev is not None:
+        pr.finalize(prev)
+    ta, tb = pr.evaluations()
+    fe = (ta[0], tb[0]) if len(ta) == 1 else (np.zeros(field, np.uint64), np.zeros(field, np.uint64))
+    return ProductSumcheck(msgs, chals, fe, ta, tb)
+
+
+def inner_product_sumcheck(a, b, transcript, hook=None, field=FP3):
+    """src/inner_product_sumcheck.rs:568-585."""
+    return inner_product_sumcheck_partial(a, b, transcript, _rounds_for(np.asarray(a).shape[0]), hook, field)
+
+
+def multilinear_sumcheck_partial(values, transcript, num_rounds, hook=None, field=FP3):
+    """src/multilinear_sumcheck.rs:265-319: sends (s0, s1) per round."""
+    n = np.asarray(values).shape[0]
+    if num_rounds and (1 << _rounds_for(n)) < (1 << num_rounds):
+        raise _lib.ReferencePanic(6, "num_rounds (%d) exceeds log2 of next-pow2 of len (%d)" % (num_rounds, n))
+    pr = MultilinearProver(values, field=field)
+    msgs, chals, prev = [], [], None
+    for r in range(num_rounds):
+        _, aux = pr.round(prev, aux=True)
+        msgs.append((aux[0], aux[1]))
+        transcript.send(aux[0])
+        transcript.send(aux[1])
+        if hook is not None:
+            hook(r, transcript)
+        prev = transcript.challenge()
+        chals.append(prev)
+    if prev is not None:
+        pr.finalize(prev)
+    t = pr.evals()
+    fe = t[0] if len(t) == 1 else np.zeros(field, np.uint64)
+    return Sumcheck(msgs, chals, fe, t)
+
+
+def multilinear_sumcheck(values, transcript, hook=None, field=FP3):
+    """src/multilinear_sumcheck.rs:322-338."""
+    return multilinear_sumcheck_partial(values, transcript, _rounds_for(np.asarray(values).shape[0]), hook, field)

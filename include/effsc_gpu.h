@@ -1,0 +1,218 @@
+/*
+ * effsc_gpu.h -- C ABI of the GB300 sumcheck prover.
+ *
+ * The entry points are what a Rust binding of the crate `effsc`
+ * (compsec-epfl/efficient-sumcheck) needs to keep its prover API as a drop-in
+ * while the fold+evaluate rounds run on one sm_103a GPU.  Each function names
+ * the reference item it stands in for (paths relative to that crate's root).
+ *
+ * Conventions
+ *  - Every function returns an effsc_status; on failure
+ *    effsc_last_error() returns a thread-local message.  EFFSC_PANIC marks the
+ *    cases where the reference panics (e.g. unequal table lengths).
+ *  - Field elements are uint64_t words.  A prover's field F is Fp
+ *    (EFFSC_FP, 1 word per element) or the cubic extension F64Ext3
+ *    (EFFSC_FP3, 3 words [c0, c1, c2] per element, the layout of arkworks'
+ *    CubicExtField).  Tables may also be passed as base-field words
+ *    (ncomp = 1) for an Fp3 prover: they are the embedded elements (x, 0, 0),
+ *    exactly what the reference receives as "lifted" tables.
+ *  - repr selects the word encoding at the boundary: EFFSC_CANONICAL
+ *    (0 <= x < p) or EFFSC_MONTGOMERY (arkworks' x * 2^64 mod p, so that
+ *    `&[F]` reinterpreted as `&[u64]` can be passed without a copy,
+ *    reference src/field.rs:314-375).  The device computes in canonical form.
+ *  - Handles are not re-entrant: one thread at a time per handle.
+ *  - Host pointers are plain host memory (pageable or pinned).
+ */
+#ifndef EFFSC_GPU_H
+#define EFFSC_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    EFFSC_OK = 0,
+    EFFSC_INVALID_ARG = 1,
+    EFFSC_OOM = 2,
+    EFFSC_CUDA_ERROR = 3,
+    EFFSC_TIMEOUT = 4,
+    EFFSC_UNSUPPORTED = 5,
+    EFFSC_PANIC = 6
+} effsc_status;
+
+typedef enum { EFFSC_ML = 0, EFFSC_IP = 1, EFFSC_COEF = 2, EFFSC_EQF = 3 } effsc_kind;
+typedef enum { EFFSC_MSB = 0, EFFSC_LSB = 1 } effsc_order;
+typedef enum { EFFSC_FP = 1, EFFSC_FP3 = 3 } effsc_field;
+typedef enum { EFFSC_CANONICAL = 0, EFFSC_MONTGOMERY = 1 } effsc_repr;
+typedef enum { EFFSC_T_KECCAK = 0, EFFSC_T_TEST = 1 } effsc_transcript_kind;
+
+typedef struct effsc_ctx effsc_ctx;
+typedef struct effsc_prover effsc_prover;
+typedef struct effsc_transcript effsc_transcript;
+
+/* ---- errors / library -------------------------------------------------- */
+const char* effsc_last_error(void);
+const char* effsc_status_str(int status);
+/* Number of kernel launches issued by this thread since the last reset. */
+uint64_t effsc_launch_count(void);
+void effsc_launch_count_reset(void);
+
+/* Measurement (no reference counterpart).  While enabled on a thread, every
+ * kernel that thread launches outside a CUDA graph is bracketed by CUDA events
+ * on its stream and recorded with its algorithmic bytes (table words it must
+ * read plus words it writes).  effsc_profile_get waits for record i. */
+int effsc_profile_enable(int on);
+size_t effsc_profile_count(void);
+int effsc_profile_get(size_t i, char* name, size_t name_cap, double* ms, uint64_t* bytes);
+void effsc_profile_clear(void);
+
+/* ---- context: one GPU and one CUDA stream -------------------------------- */
+/* No reference counterpart (the crate is CPU-only); every prover, transcript
+ * upload and batch runs on the context's stream. */
+int effsc_ctx_create(int device, effsc_ctx** out);
+int effsc_ctx_destroy(effsc_ctx* ctx);
+/* Use an external cudaStream_t (NULL restores the context's own stream). */
+int effsc_ctx_set_stream(effsc_ctx* ctx, void* cuda_stream);
+int effsc_ctx_synchronize(effsc_ctx* ctx);
+
+/* ---- provers --------------------------------------------------------------
+ * kind/order select the reference prover:
+ *   EFFSC_ML  MSB: MultilinearProver::new(evals)      src/provers/multilinear.rs:30-33
+ *   EFFSC_ML  LSB: MultilinearProverLSB::new(evals)   src/provers/multilinear_lsb.rs:31-35
+ *   EFFSC_IP  MSB: InnerProductProver::new(a, b)      src/provers/inner_product.rs:33-36
+ *   EFFSC_IP  LSB: InnerProductProverLSB::new(a, b)   src/provers/inner_product_lsb.rs:31-34
+ *   EFFSC_COEF MSB/LSB: CoefficientProver[LSB]::new(&E, vec![], pairwise)
+ *                   src/provers/coefficient.rs:28-40, coefficient_lsb.rs:51-66,
+ *                   with E the device product evaluator of degree n_tables
+ *                   (1..3): accumulate_pair adds the coefficients of
+ *                   prod_i (lo_i + x (hi_i - lo_i)) -- TripleProductEval
+ *                   (tests/adversarial_verifier.rs:444-466) for n_tables = 3.
+ * tables[i] has lens[i] elements of ncomp[i] words (1: base field, 3: Fp3).
+ * IP with lens[0] != lens[1] returns EFFSC_PANIC like the reference's assert.
+ * The input tables are copied to the device; the prover owns the copies. */
+int effsc_prover_create(effsc_ctx* ctx, int kind, int order, int field, int repr,
+                        int n_tables, const uint64_t* const* tables, const size_t* lens,
+                        const int* ncomp, effsc_prover** out);
+/* EqFactoredProver::new(w, p_evals), src/provers/eq_factored.rs:90-114.
+ * w: num_vars elements of `field`; p: p_len <= 2^num_vars elements of
+ * p_ncomp words (zero-padded to 2^num_vars; longer is EFFSC_PANIC). */
+int effsc_eqf_create(effsc_ctx* ctx, int field, int repr, const uint64_t* w, size_t num_vars,
+                     const uint64_t* p, size_t p_len, int p_ncomp, effsc_prover** out);
+/* Same constructors with the tables already in device memory (canonical,
+ * structure-of-arrays: c0 of every element, then c1, then c2 when ncomp = 3);
+ * the prover copies nothing and does not take ownership: the caller keeps the
+ * buffers alive and unchanged until the prover is destroyed.  Rounds never
+ * write to these buffers, so effsc_prover_reset() can rerun the proof. */
+int effsc_prover_create_device(effsc_ctx* ctx, int kind, int order, int field,
+                               int n_tables, const uint64_t* const* dev_tables, const size_t* lens,
+                               const int* ncomp, effsc_prover** out);
+int effsc_prover_destroy(effsc_prover* p);
+
+/* SumcheckProver::degree, src/sumcheck_prover.rs:36-71. */
+int effsc_prover_degree(const effsc_prover* p);
+/* SumcheckProver::round, src/sumcheck_prover.rs:40-59: challenge == NULL is
+ * round(None) (round 0); otherwise fold with *challenge and compute the next
+ * round polynomial.  out_evals receives degree() elements in the EvalsInfty
+ * wire format [h(0)] (d = 1) or [h(0), h(inf), h(2), ..., h(d-1)].  out_aux
+ * (optional, 2 elements) receives the raw per-round pair the legacy runners
+ * send: (s0, s1) for ML (src/multilinear_sumcheck.rs:9-14), (c0, c2) for IP
+ * (src/inner_product_sumcheck.rs:11-16), (c0, c1) for COEF. */
+int effsc_prover_round(effsc_prover* p, const uint64_t* challenge, uint64_t* out_evals, uint64_t* out_aux);
+/* SumcheckProver::finalize, src/sumcheck_prover.rs:61-66. */
+int effsc_prover_finalize(effsc_prover* p, const uint64_t* challenge);
+/* SumcheckProver::final_value, src/sumcheck_prover.rs:68-70. */
+int effsc_prover_final_value(effsc_prover* p, uint64_t* out);
+/* Post-state accessors: InnerProductProver::evaluations / MultilinearProver::evals
+ * / CoefficientProver::pairwise / EqFactoredProver tables (p, eq_l, eq_r).
+ * Writes table_len() elements of `field` words each (AoS). */
+int effsc_prover_table_len(const effsc_prover* p, int table, size_t* out_len);
+int effsc_prover_read_table(effsc_prover* p, int table, uint64_t* out);
+/* Restore the state right after construction (the input tables are never
+ * written by the rounds), so a proof can be recomputed without re-upload. */
+int effsc_prover_reset(effsc_prover* p);
+
+/* The whole protocol on the device: runner::sumcheck (src/runner.rs:29-69)
+ * with the device transcript -- per round the wire values and `hook` bytes
+ * (hook_len may be 0) are absorbed into `t` and the next challenge squeezed on
+ * the GPU.  `t` must be an EFFSC_T_KECCAK transcript of the prover's field;
+ * its state is uploaded first and written back at the end, so host-side
+ * sends/challenges can be interleaved with device proofs (partial runs).
+ * Outputs (host, may be NULL): round_polys (num_rounds * degree elements),
+ * challenges (num_rounds elements), final_value (1 element).
+ * use_graph != 0 captures the launches in a CUDA graph and replays it; the
+ * graph is cached per (prover, num_rounds, hook_len) and reused by later
+ * calls after effsc_prover_reset(). */
+int effsc_prove(effsc_prover* p, size_t num_rounds, effsc_transcript* t,
+                const uint8_t* hook, size_t hook_len, int use_graph,
+                uint64_t* round_polys, uint64_t* challenges, uint64_t* final_value);
+
+/* ---- transcripts ---------------------------------------------------------
+ * ProverTranscript / VerifierTranscript (src/transcript/transcript.rs:11-43).
+ * EFFSC_T_KECCAK: the project's Fiat-Shamir transcript (Keccak-f[1600]
+ *   duplex, 136-byte rate; label absorbed as 8-byte LE length + bytes;
+ *   elements absorbed as 8 LE bytes per component; a challenge component is
+ *   16 squeezed LE bytes mod p).  The crate's default spongefish transcript
+ *   (src/transcript/spongefish.rs:17-44) is not reproduced.
+ * EFFSC_T_TEST: SanityTranscript semantics (src/transcript/sanity.rs:12-55):
+ *   sends are no-ops, challenge = F::from_u64(next_u64()) from a SplitMix64
+ *   stream seeded with `seed`. */
+int effsc_transcript_create(int kind, int field, int repr, const uint8_t* label, size_t label_len,
+                            uint64_t seed, effsc_transcript** out);
+int effsc_transcript_destroy(effsc_transcript* t);
+int effsc_transcript_clone(const effsc_transcript* t, effsc_transcript** out);
+int effsc_transcript_absorb(effsc_transcript* t, const uint8_t* bytes, size_t len);
+int effsc_transcript_squeeze(effsc_transcript* t, uint8_t* out, size_t len);
+int effsc_transcript_send(effsc_transcript* t, const uint64_t* value);
+int effsc_transcript_challenge(effsc_transcript* t, uint64_t* out);
+
+/* ---- verifier --------------------------------------------------------------
+ * sumcheck_verify, src/verifier.rs:61-139, on the host: receives degree
+ * values per round from round_polys (absorbing them into t), applies the hook
+ * bytes, squeezes the challenge and reduces the claim.  The oracle check
+ * final_claim == final_value stays with the caller, as in the reference. */
+int effsc_verify(int field, int repr, const uint64_t* claimed_sum, size_t degree, size_t num_rounds,
+                 effsc_transcript* t, const uint8_t* hook, size_t hook_len,
+                 const uint64_t* round_polys, uint64_t* challenges, uint64_t* final_claim);
+
+/* ---- standalone fold -------------------------------------------------------
+ * effsc::fold (src/fold.rs:14 -> src/multilinear_sumcheck.rs:132-178):
+ * values[k] + weight * (values[k + L/2] - values[k]) with implicit zero
+ * padding to the next power of two; *out_len = next_pow2(len)/2 (len <= 1:
+ * unchanged).  values: len elements of ncomp words; out: *out_len elements of
+ * `field` words. */
+int effsc_fold(effsc_ctx* ctx, int field, int repr, const uint64_t* values, size_t len, int ncomp,
+               const uint64_t* weight, uint64_t* out, size_t* out_len);
+
+/* ---- eq table ----------------------------------------------------------------
+ * eq(w, .) over {0,1}^num_vars in MSB layout (EqFactored's build_eq_table,
+ * src/provers/eq_factored.rs:217-239), written to host `out`
+ * (2^num_vars elements of `field` words). */
+int effsc_build_eq_table(effsc_ctx* ctx, int field, int repr, const uint64_t* w, size_t num_vars,
+                         uint64_t* out);
+
+/* ---- seeded inputs ---------------------------------------------------------
+ * The seeded uniform generator shared with the tests: element i of a table
+ * with seed s is SplitMix64 output i (re-mixed while >= p), canonical.
+ * Fills a device buffer (dev_out) or a host buffer (host_out). */
+int effsc_gen_uniform(effsc_ctx* ctx, uint64_t seed, uint64_t n, uint64_t* dev_out, uint64_t* host_out);
+uint64_t effsc_table_seed(uint64_t seed, uint64_t table);
+
+/* Integer-pipe microbenchmark (no reference counterpart): the device's rate
+ * of Goldilocks products (64x64 -> 128-bit product plus reduction) and of
+ * Fp3 x Fp3 products, each from independent dependency chains in every
+ * thread of a full grid; the denominator of the integer-multiply roofline. */
+int effsc_diag_mulmod_rate(effsc_ctx* ctx, double* mulmod_per_s, double* fp3_mul_per_s);
+
+/* ---- device memory helpers (for the device-resident constructors) ------- */
+int effsc_device_alloc(effsc_ctx* ctx, size_t bytes, void** out);
+int effsc_device_free(effsc_ctx* ctx, void* ptr);
+int effsc_memcpy_h2d(effsc_ctx* ctx, void* dst, const void* src, size_t bytes);
+int effsc_memcpy_d2h(effsc_ctx* ctx, void* dst, const void* src, size_t bytes);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

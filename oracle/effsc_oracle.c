@@ -172,7 +172,9 @@ size_t or_transcript_size(void) { return sizeof(or_transcript); }
 
 void or_transcript_absorb(or_transcript* t, const uint8_t* data, size_t len) {
     if (t->kind != OR_T_KECCAK) return;
-    if (t->squeezing) { or_keccak_f1600(t->st); t->pos = 0; t->squeezing = 0; }
+    /* Duplex: the next call's input is XORed into the state that produced the
+     * last output; the permutation runs once per absorb->squeeze switch. */
+    if (t->squeezing) { t->pos = 0; t->squeezing = 0; }
     for (size_t i = 0; i < len; i++) {
         if (t->pos == T_RATE) { or_keccak_f1600(t->st); t->pos = 0; }
         st_xor_byte(t->st, t->pos++, data[i]);

@@ -99,12 +99,21 @@ def _bytes(b):
 
 
 def as_f(x):
-    """Coerce to a (..., 3) uint64 array of canonical Fp3 triples."""
-    a = np.ascontiguousarray(np.asarray(x, dtype=np.uint64))
-    if a.ndim == 0 or a.shape[-1] != 3:
-        z = np.zeros(a.shape + (3,), dtype=np.uint64)
-        z[..., 0] = a
-        a = z
+    """One field element (scalar, 1 word or 3 words) as a (3,) uint64 triple."""
+    a = np.asarray(x, dtype=np.uint64).reshape(-1)
+    z = np.zeros(3, dtype=np.uint64)
+    z[: a.size] = a
+    return z
+
+
+def as_table(x):
+    """A table: 1-D arrays are base-field values, (n, 3) arrays Fp3 triples."""
+    a = np.asarray(x, dtype=np.uint64)
+    if a.ndim == 1:
+        z = np.zeros((a.shape[0], 3), dtype=np.uint64)
+        z[:, 0] = a
+        return z
+    assert a.ndim == 2 and a.shape[1] == 3, a.shape
     return np.ascontiguousarray(a)
 
 
@@ -180,8 +189,14 @@ class Prover:
         if _handle is not None:
             self.h = _handle
             return
-        arrs = [np.ascontiguousarray(np.asarray(t, dtype=np.uint64)) for t in tables]
-        ncomp = 3 if arrs[0].ndim == 2 else 1
+        raw = [np.asarray(t, dtype=np.uint64) for t in tables]
+        if all(r.ndim == 1 for r in raw):
+            arrs = [np.ascontiguousarray(r) for r in raw]
+            ncomp = 1
+        else:
+            # every table as (n, 3) triples, so base and Fp3 tables can be mixed
+            arrs = [as_table(t) for t in raw]
+            ncomp = 3
         ptrs = (_u64p * len(arrs))(*[_p(a) for a in arrs])
         lens = (ctypes.c_size_t * len(arrs))(*[a.shape[0] for a in arrs])
         self._keep = arrs
@@ -189,7 +204,7 @@ class Prover:
 
     @classmethod
     def eq_factored(cls, deg, w, p):
-        w = as_f(w)
+        w = as_table(w) if np.asarray(w).size else np.zeros((0, 3), dtype=np.uint64)
         p = np.ascontiguousarray(np.asarray(p, dtype=np.uint64))
         ncomp = 3 if p.ndim == 2 else 1
         h = lib().or_eqf_new(deg, _p(w), w.shape[0], _p(p), p.shape[0], ncomp)
@@ -258,7 +273,7 @@ def verify(claimed_sum, degree, num_rounds, transcript, round_polys, hook=b""):
 
 
 def build_eq_table(w):
-    w = as_f(w)
+    w = as_table(w)
     v = w.shape[0]
     out = np.zeros((1 << v, 3), dtype=np.uint64)
     lib().or_build_eq_table(_p(w), v, _p(out))
@@ -266,8 +281,8 @@ def build_eq_table(w):
 
 
 def mle_eval_msb(table, point):
-    t = as_f(table)
-    pt = as_f(point)
+    t = as_table(table)
+    pt = as_table(point)
     out = np.zeros(3, dtype=np.uint64)
     lib().or_mle_eval_msb(_p(t), t.shape[0], _p(pt), pt.shape[0], _p(out))
     return out
