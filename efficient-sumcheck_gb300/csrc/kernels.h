@@ -79,3 +79,10 @@ int max_grid(void);
 void kernels_init(int device);
 
 }  // namespace effsc
+
+// Sets the thread-local message returned by effsc_last_error(); returns code.
+int effsc_set_error(int code, const char* fmt, ...);
+
+namespace effsc {
+
+}  // namespace effsc

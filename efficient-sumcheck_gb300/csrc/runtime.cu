@@ -36,6 +36,16 @@ int fail(int code, const char* fmt, ...) {
 }
 }  // namespace
 
+int effsc_set_error(int code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    g_err = buf;
+    return code;
+}
+
 #define CK(call)                                                                                  \
     do {                                                                                          \
         cudaError_t e_ = (call);                                                                  \

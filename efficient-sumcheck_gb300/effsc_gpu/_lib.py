@@ -58,6 +58,7 @@ SIGNATURES = {
     "effsc_build_eq_table": (ci, [vp, ci, ci, u64p, sz, u64p]),
     "effsc_gen_uniform": (ci, [vp, ctypes.c_uint64, ctypes.c_uint64, u64p, u64p]),
     "effsc_table_seed": (ctypes.c_uint64, [ctypes.c_uint64, ctypes.c_uint64]),
+    "effsc_ip_round_noalloc": (ci, [vp, vp, vp, vp, sz, u64p, vp, ci, vp]),
     "effsc_device_alloc": (ci, [vp, sz, ctypes.POINTER(vp)]),
     "effsc_device_free": (ci, [vp, vp]),
     "effsc_memcpy_h2d": (ci, [vp, vp, vp, sz]),

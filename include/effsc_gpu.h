@@ -206,6 +206,28 @@ uint64_t effsc_table_seed(uint64_t seed, uint64_t table);
  * thread of a full grid; the denominator of the integer-multiply roofline. */
 int effsc_diag_mulmod_rate(effsc_ctx* ctx, double* mulmod_per_s, double* fp3_mul_per_s);
 
+/* ---- one round without allocation -----------------------------------------
+ * No counterpart in the reference.  For callers that must not allocate device
+ * memory (a host application whose own pool has reserved the HBM, or work
+ * sharing a stream with latency-critical kernels that a synchronising
+ * cudaMalloc/cudaFree would stall): one InnerProductProver (MSB) round on the
+ * caller's device buffers -- challenge == NULL evaluates round 0 on a, b
+ * (len >= 1); otherwise folds a, b with *challenge (3 canonical words, Fp3) and
+ * evaluates the next round (len a power of two >= 4).  a, b: Fp3 tables of len
+ * elements in structure-of-arrays form (c0[len], c1[len], c2[len], canonical);
+ * the folded tables go to the first len/2 entries of each component array of
+ * a_out, b_out (same component stride len; a_out == a works in place).
+ * out_evals: 6 device words [q(0), q(inf)], valid once the stream has run the
+ * call.  The grid reduction uses a static device array sized for at most 4096
+ * blocks (about 384 KiB, held by every GPU that loads the library); blocks = 0
+ * picks the grid, blocks > 4096 is rejected.  The first call on a device
+ * resolves that array's address, so make it before any stream capture.  All
+ * calls share the array: calls that overlap on the GPU (other streams,
+ * threads) race and must be serialised by the caller.  Issues no cudaMalloc
+ * or cudaFree and does not synchronise. */
+int effsc_ip_round_noalloc(const uint64_t* a, const uint64_t* b, uint64_t* a_out, uint64_t* b_out,
+                           size_t len, const uint64_t* challenge, uint64_t* out_evals, int blocks, void* stream);
+
 /* ---- device memory helpers (for the device-resident constructors) ------- */
 int effsc_device_alloc(effsc_ctx* ctx, size_t bytes, void** out);
 int effsc_device_free(effsc_ctx* ctx, void* ptr);
