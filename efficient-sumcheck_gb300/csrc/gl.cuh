@@ -6,9 +6,10 @@
 // W is the canonical value of the crate's F64Ext3 non-residue F64::from_raw(7)
 // (src/tests/fields.rs:73-100), i.e. 7 * 2^-64 mod p = -7 * 2^32 mod p.
 //
-// Products are formed as 128-bit integers and reduced with 2^64 = 2^32 - 1 and
-// 2^96 = -1 (mod p).  Sums of many products are accumulated lazily in 160-bit
-// accumulators (lo, hi, top) and reduced once, using 2^128 = -2^32 (mod p).
+// Sums of products are accumulated lazily in 160-bit accumulators of five
+// 32-bit limbs (32x32-bit multiply-add chains with carry) and reduced once
+// with 2^64 = 2^32 - 1 and 2^96 = -1 (mod p).  Single products outside the hot
+// loops use a 128-bit product and the same reduction.
 #pragma once
 #include <cstdint>
 
@@ -24,9 +25,18 @@ __device__ __forceinline__ u64 gl_add(u64 a, u64 b) {
     if (s < a) return s + GL_EPS;            // carry: 2^64 = eps; result already < p
     return s >= GL_P ? s - GL_P : s;
 }
+// a - b for canonical a, b; on a borrow subtract 2^32 - 1 (i.e. add p mod 2^64).
 __device__ __forceinline__ u64 gl_sub(u64 a, u64 b) {
-    u64 d = a - b;
-    return a < b ? d - GL_EPS : d;           // borrow: add p (mod 2^64)
+    u32 d0, d1;
+    asm("{\n\t.reg .u32 m;\n\t"
+        "sub.cc.u32 %0, %2, %4;\n\t"
+        "subc.cc.u32 %1, %3, %5;\n\t"
+        "subc.u32 m, 0, 0;\n\t"
+        "sub.cc.u32 %0, %0, m;\n\t"
+        "subc.u32 %1, %1, 0;\n\t}"
+        : "=r"(d0), "=r"(d1)
+        : "r"((u32)a), "r"((u32)(a >> 32)), "r"((u32)b), "r"((u32)(b >> 32)));
+    return ((u64)d1 << 32) | d0;
 }
 __device__ __forceinline__ u64 gl_neg(u64 a) { return a ? GL_P - a : 0; }
 
@@ -51,33 +61,84 @@ __device__ __forceinline__ u64 gl_mul(u64 a, u64 b) {
 }
 
 // ---- lazy 160-bit accumulator -------------------------------------------------
+// Five 32-bit limbs c0..c4 (value c0 + c1 2^32 + ... + c4 2^128).  A product is
+// added with a chain of eight 32-bit multiply-adds with carry (mad.lo.cc /
+// madc.hi.cc), so no 128-bit intermediate and no separate carry handling.
+__device__ __forceinline__ u32 lo32(u64 x) { return (u32)x; }
+__device__ __forceinline__ u32 hi32(u64 x) { return (u32)(x >> 32); }
+__device__ __forceinline__ u64 mk64(u32 lo, u32 hi) { return ((u64)hi << 32) | lo; }
+
 struct Acc {
-    u64 lo, hi;
-    u32 top;
+    u32 c0, c1, c2, c3, c4;
 };
-__device__ __forceinline__ Acc acc_zero() { Acc a; a.lo = 0; a.hi = 0; a.top = 0; return a; }
-__device__ __forceinline__ void acc_add128(Acc& a, u64 lo, u64 hi) {
-    asm("add.cc.u64 %0, %0, %3;\n\t"
-        "addc.cc.u64 %1, %1, %4;\n\t"
-        "addc.u32 %2, %2, 0;"
-        : "+l"(a.lo), "+l"(a.hi), "+r"(a.top)
-        : "l"(lo), "l"(hi));
+__device__ __forceinline__ Acc acc_zero() { Acc a; a.c0 = a.c1 = a.c2 = a.c3 = a.c4 = 0; return a; }
+__device__ __forceinline__ Acc acc_from(u64 v) { Acc a; a.c0 = lo32(v); a.c1 = hi32(v); a.c2 = a.c3 = a.c4 = 0; return a; }
+__device__ __forceinline__ void acc_mac(Acc& s, u64 x, u64 y) {
+    const u32 x0 = lo32(x), x1 = hi32(x), y0 = lo32(y), y1 = hi32(y);
+    asm("mad.lo.cc.u32 %0, %5, %7, %0;\n\t"
+        "madc.hi.cc.u32 %1, %5, %7, %1;\n\t"
+        "madc.lo.cc.u32 %2, %6, %8, %2;\n\t"
+        "madc.hi.cc.u32 %3, %6, %8, %3;\n\t"
+        "addc.u32 %4, %4, 0;\n\t"
+        "mad.lo.cc.u32 %1, %5, %8, %1;\n\t"
+        "madc.hi.cc.u32 %2, %5, %8, %2;\n\t"
+        "addc.cc.u32 %3, %3, 0;\n\t"
+        "addc.u32 %4, %4, 0;\n\t"
+        "mad.lo.cc.u32 %1, %6, %7, %1;\n\t"
+        "madc.hi.cc.u32 %2, %6, %7, %2;\n\t"
+        "addc.cc.u32 %3, %3, 0;\n\t"
+        "addc.u32 %4, %4, 0;"
+        : "+r"(s.c0), "+r"(s.c1), "+r"(s.c2), "+r"(s.c3), "+r"(s.c4)
+        : "r"(x0), "r"(x1), "r"(y0), "r"(y1));
 }
-__device__ __forceinline__ void acc_add64(Acc& a, u64 v) {
-    asm("add.cc.u64 %0, %0, %3;\n\t"
-        "addc.cc.u64 %1, %1, 0;\n\t"
-        "addc.u32 %2, %2, 0;"
-        : "+l"(a.lo), "+l"(a.hi), "+r"(a.top)
-        : "l"(v));
+__device__ __forceinline__ void acc_add64(Acc& s, u64 v) {
+    asm("add.cc.u32 %0, %0, %5;\n\t"
+        "addc.cc.u32 %1, %1, %6;\n\t"
+        "addc.cc.u32 %2, %2, 0;\n\t"
+        "addc.cc.u32 %3, %3, 0;\n\t"
+        "addc.u32 %4, %4, 0;"
+        : "+r"(s.c0), "+r"(s.c1), "+r"(s.c2), "+r"(s.c3), "+r"(s.c4)
+        : "r"(lo32(v)), "r"(hi32(v)));
 }
-__device__ __forceinline__ void acc_mac(Acc& a, u64 x, u64 y) {
-    u64 lo, hi;
-    gl_mul128(x, y, lo, hi);
-    acc_add128(a, lo, hi);
-}
-__device__ __forceinline__ u64 acc_reduce(const Acc& a) {
-    u64 r = gl_reduce128(a.lo, a.hi);
-    return gl_sub(r, ((u64)a.top) << 32);     // top * 2^128 = -top * 2^32
+// Canonical value mod p.  With B = 2^32: B^2 = B - 1 and B^3 = -1 (mod p), so
+//   x = (c1:c0) - (c4:c3) + c2 (B - 1).
+// The 64-bit subtraction and addition leave a net carry cm in {-1, 0, 1}
+// worth cm * 2^64 = cm (B - 1); adding that back can underflow only when
+// cm = -1, and then once more by B - 1.  A final conditional subtraction of p
+// gives the canonical residue.
+__device__ __forceinline__ u64 acc_reduce(const Acc& s) {
+    u32 r0, r1;
+    asm("{\n\t"
+        ".reg .u32 t0, t1, bm, e0, e1, cm, sx, f0, f1, cc2, nf, d, v0, v1, ge;\n\t"
+        ".reg .pred pge;\n\t"
+        "sub.cc.u32 t0, %2, %5;\n\t"
+        "subc.cc.u32 t1, %3, %6;\n\t"
+        "subc.u32 bm, 0, 0;\n\t"
+        "sub.cc.u32 e0, 0, %4;\n\t"
+        "subc.u32 e1, %4, 0;\n\t"
+        "add.cc.u32 t0, t0, e0;\n\t"
+        "addc.cc.u32 t1, t1, e1;\n\t"
+        "addc.u32 cm, bm, 0;\n\t"
+        "shr.s32 sx, cm, 31;\n\t"
+        "sub.cc.u32 f0, 0, cm;\n\t"
+        "subc.u32 f1, cm, sx;\n\t"
+        "add.cc.u32 t0, t0, f0;\n\t"
+        "addc.cc.u32 t1, t1, f1;\n\t"
+        "addc.u32 cc2, 0, 0;\n\t"
+        "shr.u32 nf, cm, 31;\n\t"
+        "sub.u32 d, cc2, nf;\n\t"
+        "sub.cc.u32 t0, t0, d;\n\t"
+        "subc.u32 t1, t1, 0;\n\t"
+        "add.cc.u32 v0, t0, 0xFFFFFFFF;\n\t"
+        "addc.cc.u32 v1, t1, 0;\n\t"
+        "addc.u32 ge, 0, 0;\n\t"
+        "setp.ne.u32 pge, ge, 0;\n\t"
+        "selp.b32 %0, v0, t0, pge;\n\t"
+        "selp.b32 %1, v1, t1, pge;\n\t"
+        "}"
+        : "=r"(r0), "=r"(r1)
+        : "r"(s.c0), "r"(s.c1), "r"(s.c2), "r"(s.c3), "r"(s.c4));
+    return mk64(r0, r1);
 }
 
 // ---- Fp3 ---------------------------------------------------------------------
@@ -134,34 +195,28 @@ __device__ __forceinline__ Mul3 mul3_prepare(const F3& m) {
 template <bool EX, bool EM, bool EADD, bool HAS_ADD>
 __device__ __forceinline__ F3 f3_mul_add(const F3& x, const Mul3& m, const F3& add) {
     F3 r;
+    Acc a0 = acc_from(HAS_ADD ? add.c0 : 0);
     if (!EX && !EM) {
-        u64 p = gl_mul(x.c0, m.m0);
-        r.c0 = HAS_ADD ? gl_add(p, add.c0) : p;
+        acc_mac(a0, x.c0, m.m0);
+        r.c0 = acc_reduce(a0);
         if (HAS_ADD && EADD) { r.c1 = add.c1; r.c2 = add.c2; } else { r.c1 = r.c2 = 0; }
         return r;
     }
+    Acc a1 = acc_from(HAS_ADD && EADD ? add.c1 : 0), a2 = acc_from(HAS_ADD && EADD ? add.c2 : 0);
     if (EX != EM) {
         // one side base: three independent products
         u64 b = EX ? m.m0 : x.c0;
-        u64 e0 = EX ? x.c0 : m.m0, e1 = EX ? x.c1 : m.m1, e2 = EX ? x.c2 : m.m2;
-        r.c0 = gl_mul(e0, b);
-        r.c1 = gl_mul(e1, b);
-        r.c2 = gl_mul(e2, b);
-        if (HAS_ADD) {
-            r.c0 = gl_add(r.c0, add.c0);
-            if (EADD) { r.c1 = gl_add(r.c1, add.c1); r.c2 = gl_add(r.c2, add.c2); }
-        }
-        return r;
+        acc_mac(a0, EX ? x.c0 : m.m0, b);
+        acc_mac(a1, EX ? x.c1 : m.m1, b);
+        acc_mac(a2, EX ? x.c2 : m.m2, b);
+    } else {
+        acc_mac(a0, x.c0, m.m0); acc_mac(a0, x.c1, m.w2); acc_mac(a0, x.c2, m.w1);
+        acc_mac(a1, x.c0, m.m1); acc_mac(a1, x.c1, m.m0); acc_mac(a1, x.c2, m.w2);
+        acc_mac(a2, x.c0, m.m2); acc_mac(a2, x.c1, m.m1); acc_mac(a2, x.c2, m.m0);
     }
-    Acc a0 = acc_zero(), a1 = acc_zero(), a2 = acc_zero();
-    acc_mac(a0, x.c0, m.m0); acc_mac(a0, x.c1, m.w2); acc_mac(a0, x.c2, m.w1);
-    acc_mac(a1, x.c0, m.m1); acc_mac(a1, x.c1, m.m0); acc_mac(a1, x.c2, m.w2);
-    acc_mac(a2, x.c0, m.m2); acc_mac(a2, x.c1, m.m1); acc_mac(a2, x.c2, m.m0);
-    if (HAS_ADD) {
-        acc_add64(a0, add.c0);
-        if (EADD) { acc_add64(a1, add.c1); acc_add64(a2, add.c2); }
-    }
-    r.c0 = acc_reduce(a0); r.c1 = acc_reduce(a1); r.c2 = acc_reduce(a2);
+    r.c0 = acc_reduce(a0);
+    r.c1 = acc_reduce(a1);
+    r.c2 = acc_reduce(a2);
     return r;
 }
 template <bool EA, bool EB>

@@ -33,6 +33,31 @@ bool launch_fused_mlip(int pol, int sem, u32 mask, bool ech, const RoundArgs& a,
     }
 }
 
+template <int POL, u32 M, bool ECH>
+static bool launch_tma_inst(const RoundArgs& a, u32 ntiles, int grid, cudaStream_t s) {
+    constexpr int NT = Policy<POL, 0>::NT;
+    constexpr int SM_BYTES = TmaLayout<M, NT>::smem_bytes();
+    static bool configured = false;
+    if (!configured) {
+        if (cudaFuncSetAttribute(k_fused_tma<POL, M, ECH>, cudaFuncAttributeMaxDynamicSharedMemorySize, SM_BYTES) != cudaSuccess)
+            return false;
+        configured = true;
+    }
+    k_fused_tma<POL, M, ECH><<<grid, TPB, SM_BYTES, s>>>(a, ntiles);
+    return true;
+}
+
+bool launch_fused_tma(int pol, u32 mask, bool ech, const RoundArgs& a, u32 ntiles, int grid, cudaStream_t s) {
+    int key = pol * 64 + (int)mask * 2 + (ech ? 1 : 0);
+    switch (key) {
+        case POL_IP * 64 + 0 * 2 + 0: return launch_tma_inst<POL_IP, 0, false>(a, ntiles, grid, s);
+        case POL_IP * 64 + 0 * 2 + 1: return launch_tma_inst<POL_IP, 0, true>(a, ntiles, grid, s);
+        case POL_IP * 64 + 3 * 2 + 1: return launch_tma_inst<POL_IP, 3, true>(a, ntiles, grid, s);
+        default: return false;
+    }
+}
+int fused_tma_blocks_per_sm(void) { return 2; }
+
 bool launch_eqf_left(bool fused, u32 mask, bool ech, const RoundArgs& a, int grid, cudaStream_t s) {
     int key = (fused ? 16 : 0) + (int)mask * 2 + (ech ? 1 : 0);
     switch (key) {

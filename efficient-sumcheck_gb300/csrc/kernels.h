@@ -11,6 +11,8 @@ namespace effsc {
 
 // Threads per block of every round kernel.
 constexpr int KERNEL_TPB = 256;
+// Value a kernel writes to RoundArgs::status when a bounded wait times out.
+constexpr unsigned EFFSC_STATUS_TIMEOUT = 4;
 
 // Fold / evaluate semantics.
 //  SEM_MSB_PAD  : half = next_pow2(L)/2, unpaired tail folds as v*(1-w)
@@ -66,6 +68,10 @@ bool launch_fold(int sem, bool ein, bool ech, const RoundArgs& a, int t, int gri
 bool launch_eval(int pol, int sem, u32 mask, const RoundArgs& a, int grid, cudaStream_t s);
 bool launch_fused(int pol, int sem, u32 mask, bool ech, const RoundArgs& a, int grid, cudaStream_t s);
 bool launch_eqf_left(bool fused, u32 mask, bool ech, const RoundArgs& a, int grid, cudaStream_t s);
+// TMA-staged fused MSB round: tiles of KERNEL_TPB quadruples; returns false
+// if no kernel is instantiated for the combination.
+bool launch_fused_tma(int pol, u32 mask, bool ech, const RoundArgs& a, u32 ntiles, int grid, cudaStream_t s);
+int fused_tma_blocks_per_sm(void);
 
 // Utility kernels.
 void launch_split_aos(const u64* aos, u64 n, int ncomp, u64* c0, u64* c1, u64* c2, int from_mont, u32* ext_flag, cudaStream_t s);

@@ -385,7 +385,7 @@ __global__ void __launch_bounds__(TPB) k_eval(RoundArgs a) {
 // are exactly the quadruples (k, k+Q, k+2Q, k+3Q) (MSB) or (4k..4k+3) (LSB).
 // Every table is folded; outputs are Fp3 when the challenge is.
 template <int POL, int SEM, u32 M, bool ECH>
-__global__ void __launch_bounds__(TPB) k_fused(RoundArgs a) {
+__global__ void __launch_bounds__(TPB, 2) k_fused(RoundArgs a) {
     constexpr int NT = Policy<POL, 0>::NT;
     constexpr u32 FULL = (1u << NT) - 1;
     constexpr u32 MO = ECH ? FULL : M;
@@ -422,6 +422,164 @@ __global__ void __launch_bounds__(TPB) k_fused(RoundArgs a) {
             }
         }
         acc.pair(lo, hi);
+    }
+    F3 raw[P::NRAW];
+    acc.result(raw);
+    reduce_and_finalize<P::NRAW>(raw, a, POL);
+}
+
+// ---------------------------------------------------------------------------
+// TMA-staged fused round (MSB, L a power of two, Q = L/4 a multiple of TQ).
+// Each block owns tiles tile = blockIdx.x + i * gridDim.x of TQ quadruples.
+// Thread 0 streams a tile's 4 quarters x components x tables into one shared
+// memory stage with cp.async.bulk (one bulk copy per contiguous chunk), the
+// stage's mbarrier counting the bytes; TMA_S stages are kept in flight while
+// every thread folds and evaluates the quadruple it owns from shared memory
+// and stores the folded pair straight to global memory.  Waits are bounded
+// by the global timer: after 1 s the block records a timeout in a.status,
+// waits (bounded) for its copies in flight and stops.
+// ---------------------------------------------------------------------------
+constexpr int TQ = TPB;
+
+__device__ __forceinline__ u32 smem_u32(const void* p) { return (u32)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(u64* bar, u32 count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(u64* bar, u32 bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void tma_load_1d(void* dst, const void* src, u32 bytes, u64* bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                 ::"r"(smem_u32(dst)), "l"(src), "r"(bytes), "r"(smem_u32(bar)) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(u64* bar, u32 phase) {
+    u32 ok;
+    asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+                 : "=r"(ok) : "r"(smem_u32(bar)), "r"(phase) : "memory");
+    return ok != 0;
+}
+__device__ __forceinline__ u64 global_ns() {
+    u64 t;
+    asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+    return t;
+}
+// Wait for phase `phase` of `bar`; false after ~1 s.
+__device__ __forceinline__ bool mbar_wait_bounded(u64* bar, u32 phase) {
+    if (mbar_try_wait(bar, phase)) return true;
+    const u64 t0 = global_ns();
+    while (!mbar_try_wait(bar, phase))
+        if (global_ns() - t0 > 1000000000ULL) return false;
+    return true;
+}
+
+template <u32 M, int NT>
+struct TmaLayout {
+    __host__ __device__ static constexpr int nc(int t) { return ((M >> t) & 1u) ? 3 : 1; }
+    // word offset of (table t, quarter q, component c) inside a stage
+    __host__ __device__ static constexpr int off(int t, int q, int c) {
+        int o = 0;
+        for (int u = 0; u < t; u++) o += 4 * nc(u);
+        return (o + q * nc(t) + c) * TQ;
+    }
+    __host__ __device__ static constexpr int words() {
+        int o = 0;
+        for (int u = 0; u < NT; u++) o += 4 * nc(u);
+        return o * TQ;
+    }
+    __host__ __device__ static constexpr int stages() { return words() * 8 <= 24 * 1024 ? 4 : 2; }
+    __host__ __device__ static constexpr int smem_bytes() { return words() * 8 * stages(); }
+};
+
+template <int POL, u32 M, bool ECH>
+__global__ void __launch_bounds__(TPB, 2) k_fused_tma(RoundArgs a, u32 ntiles) {
+    constexpr int NT = Policy<POL, 0>::NT;
+    constexpr u32 FULL = (1u << NT) - 1;
+    constexpr u32 MO = ECH ? FULL : M;
+    using P = Policy<POL, MO>;
+    using LAY = TmaLayout<M, NT>;
+    constexpr int S = LAY::stages();
+    constexpr int SW = LAY::words();
+    extern __shared__ __align__(128) u64 tma_smem[];
+    __shared__ __align__(8) u64 bars[4];
+    __shared__ int s_abort;
+
+    const u64 Q = a.L >> 2;
+    const u32 G = gridDim.x;
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < S; s++) mbar_init(&bars[s], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        s_abort = 0;
+    }
+    __syncthreads();
+    auto issue = [&](u32 tile, int s) {
+        mbar_expect_tx(&bars[s], (u32)(SW * 8));
+        u64* dst = tma_smem + (size_t)s * SW;
+#pragma unroll
+        for (int t = 0; t < NT; t++)
+#pragma unroll
+            for (int q = 0; q < 4; q++)
+#pragma unroll
+                for (int c = 0; c < LAY::nc(t); c++)
+                    tma_load_1d(dst + LAY::off(t, q, c), a.t[t].in[c] + q * Q + (u64)tile * TQ, TQ * 8, &bars[s]);
+    };
+    if (threadIdx.x == 0)
+        for (int s = 0; s < S; s++) {
+            u32 tile = blockIdx.x + s * G;
+            if (tile < ntiles) issue(tile, s);
+        }
+    P acc;
+    acc.init();
+    F3 rr;
+    Mul3 r = load_challenge_mul(a, rr);
+    if (!ECH) r = mul3_prepare<false>(rr);
+    F3 lo[3], hi[3];
+    u32 i = 0;
+    for (u32 tile = blockIdx.x; tile < ntiles; tile += G, i++) {
+        const int s = i % S;
+        const u32 phase = (i / S) & 1u;
+        if (!mbar_wait_bounded(&bars[s], phase)) s_abort = 1;
+        __syncthreads();
+        if (s_abort) break;
+        const u64* st_ = tma_smem + (size_t)s * SW;
+        const u64 k = (u64)tile * TQ + threadIdx.x;
+#pragma unroll
+        for (int t = 0; t < NT; t++) {
+            F3 x[4];
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                x[q].c0 = st_[LAY::off(t, q, 0) + threadIdx.x];
+                if (LAY::nc(t) == 3) {
+                    x[q].c1 = st_[LAY::off(t, q, 1) + threadIdx.x];
+                    x[q].c2 = st_[LAY::off(t, q, 2) + threadIdx.x];
+                } else {
+                    x[q].c1 = x[q].c2 = 0;
+                }
+            }
+            if (ext_of<M>(t)) { lo[t] = f3_fold<true, true>(x[0], x[2], r); hi[t] = f3_fold<true, true>(x[1], x[3], r); }
+            else if (ECH) { lo[t] = f3_fold<false, true>(x[0], x[2], r); hi[t] = f3_fold<false, true>(x[1], x[3], r); }
+            else { lo[t] = f3_fold<false, false>(x[0], x[2], r); hi[t] = f3_fold<false, false>(x[1], x[3], r); }
+            if (ext_of<MO>(t)) { st<true>(a.t[t].out, k, lo[t]); st<true>(a.t[t].out, k + Q, hi[t]); }
+            else { st<false>(a.t[t].out, k, lo[t]); st<false>(a.t[t].out, k + Q, hi[t]); }
+        }
+        acc.pair(lo, hi);
+        __syncthreads();   // every thread is done with stage s
+        if (threadIdx.x == 0) {
+            u32 nt = tile + S * G;
+            if (nt < ntiles) {
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                issue(nt, s);
+            }
+        }
+    }
+    if (s_abort) {
+        // drain this block's copies in flight (bounded), then report and stop
+        if (threadIdx.x == 0) {
+            u32 j = i;
+            for (u32 tile = blockIdx.x + i * G; tile < ntiles && j < i + S; tile += G, j++)
+                mbar_wait_bounded(&bars[j % S], (j / S) & 1u);
+            if (a.status) *(volatile u32*)a.status = EFFSC_STATUS_TIMEOUT;
+        }
+        return;
     }
     F3 raw[P::NRAW];
     acc.result(raw);

@@ -383,6 +383,8 @@ int timed_launch(cudaStream_t s, const char* name, uint64_t bytes, F fn) {
     return check_launch(ok, name);
 }
 inline uint64_t wbytes(bool ext) { return ext ? 24 : 8; }
+// Rounds with at least this many quadruples use the TMA-staged kernel.
+const u64 TMA_MIN_QUADS = 1ULL << 15;
 
 // Fold table `ti` of P (kernel slot `slot`) with semantics `sem`.
 int fold_table(effsc_prover* P, int ti, int sem, const Chal& ch, bool ech, bool dry) {
@@ -445,7 +447,19 @@ int round_std(effsc_prover* P, const Chal& ch, const TxIO& tx, bool dry) {
             uint64_t bytes = 0;
             for (int i = 0; i < nt; i++) bytes += L * wbytes(P->t[i].ext) + (L / 2) * wbytes(P->t[i].ext || ech);
             const char* nm = mask ? "fused_round_fp3" : (ech ? "fused_round_fp_to_fp3" : "fused_round_fp");
-            if (!dry) TRY(timed_launch(P->ctx->stream, nm, bytes, [&] { return launch_fused(pol, sem, mask, ech, a, grid_for(L / 4), P->ctx->stream); }));
+            // large power-of-two MSB rounds: the TMA-staged kernel
+            const u64 Q = L / 4;
+            bool tma = pol == POL_IP && sem == SEM_MSB_PAD && is_pow2(L) && Q >= TMA_MIN_QUADS && Q % KERNEL_TPB == 0;
+            for (int i = 0; i < nt && tma; i++)
+                for (int c = 0; c < (P->t[i].ext ? 3 : 1); c++)
+                    tma &= ((uintptr_t)a.t[i].in[c] % 16) == 0;
+            if (tma) {
+                u32 ntiles = (u32)(Q / KERNEL_TPB);
+                int g = std::min<int>((int)ntiles, (max_grid() / 8) * fused_tma_blocks_per_sm());
+                if (!dry) TRY(timed_launch(P->ctx->stream, nm, bytes, [&] { return launch_fused_tma(pol, mask, ech, a, ntiles, g, P->ctx->stream); }));
+            } else {
+                if (!dry) TRY(timed_launch(P->ctx->stream, nm, bytes, [&] { return launch_fused(pol, sem, mask, ech, a, grid_for(L / 4), P->ctx->stream); }));
+            }
             for (int i = 0; i < nt; i++) {
                 Table& T = P->t[i];
                 T.cur = bi[i];
@@ -555,6 +569,16 @@ int round_eqf(effsc_prover* P, const Chal& ch, const TxIO& tx, bool dry) {
     return EFFSC_OK;
 }
 
+// A kernel that gave up a bounded wait leaves a code in the status word.
+int check_status(effsc_prover* P) {
+    volatile u32* st = (volatile u32*)(P->h_res + 15);
+    u32 v = *st;
+    if (!v) return EFFSC_OK;
+    *st = 0;
+    cudaMemsetAsync(P->counter, 0, sizeof(u32), P->ctx->stream);
+    return fail(EFFSC_TIMEOUT, "a round kernel timed out waiting for its staged loads (status %u)", v);
+}
+
 int do_round(effsc_prover* P, const Chal& ch, const TxIO& tx, bool dry) {
     return P->kind == EFFSC_EQF ? round_eqf(P, ch, tx, dry) : round_std(P, ch, tx, dry);
 }
@@ -630,11 +654,12 @@ int prover_common_init(effsc_prover* P) {
     cudaStream_t s = P->ctx->stream;
     CK(cudaMallocAsync((void**)&P->partials, (size_t)max_grid() * 12 * sizeof(u64), s));
     CK(cudaMallocAsync((void**)&P->counter, 2 * sizeof(u32), s));
-    P->status = P->counter + 1;
     CK(cudaMemsetAsync(P->counter, 0, 2 * sizeof(u32), s));
     CK(cudaHostAlloc((void**)&P->h_res, 16 * sizeof(u64), cudaHostAllocMapped));
     CK(cudaHostGetDevicePointer((void**)&P->d_res, P->h_res, 0));
     memset(P->h_res, 0, 16 * sizeof(u64));
+    // word 15 of the mapped result block: kernel status (0 = ok)
+    P->status = (u32*)(P->d_res + 15);
     return EFFSC_OK;
 }
 
@@ -1011,6 +1036,7 @@ int effsc_prover_round(effsc_prover* P, const uint64_t* challenge, uint64_t* out
     memset(&tx, 0, sizeof tx);
     TRY(do_round(P, ch, tx, false));
     CK(cudaStreamSynchronize(P->ctx->stream));
+    TRY(check_status(P));
     int d = degree_of(P);
     const u64* r = P->h_res;
     if (out_evals)
@@ -1185,6 +1211,7 @@ int effsc_prove(effsc_prover* P, size_t num_rounds, effsc_transcript* T, const u
     }
     CK(cudaMemcpyAsync(&T->st, P->d_tx, sizeof(DevTranscript), cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
+    TRY(check_status(P));
     for (size_t r = 0; r < num_rounds; r++) {
         if (round_polys)
             for (int i = 0; i < d; i++) {
