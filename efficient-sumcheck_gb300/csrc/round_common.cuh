@@ -500,19 +500,15 @@ __global__ void __launch_bounds__(TPB, 2) k_fused_tma(RoundArgs a, u32 ntiles) {
     constexpr int S = LAY::stages();
     constexpr int SW = LAY::words();
     extern __shared__ __align__(128) u64 tma_smem[];
-    __shared__ __align__(8) u64 bars[4];
-    __shared__ int s_abort;
+    __shared__ __align__(8) u64 full_bar[4];
+    __shared__ u32 reads_done[4];     // warps done reading the stage's current tile
+    __shared__ u32 issued_cnt[4];     // tiles issued into each stage
 
     const u64 Q = a.L >> 2;
     const u32 G = gridDim.x;
-    if (threadIdx.x == 0) {
-        for (int s = 0; s < S; s++) mbar_init(&bars[s], 1);
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-        s_abort = 0;
-    }
-    __syncthreads();
+    const int lane = threadIdx.x & 31;
     auto issue = [&](u32 tile, int s) {
-        mbar_expect_tx(&bars[s], (u32)(SW * 8));
+        mbar_expect_tx(&full_bar[s], (u32)(SW * 8));
         u64* dst = tma_smem + (size_t)s * SW;
 #pragma unroll
         for (int t = 0; t < NT; t++)
@@ -520,26 +516,33 @@ __global__ void __launch_bounds__(TPB, 2) k_fused_tma(RoundArgs a, u32 ntiles) {
             for (int q = 0; q < 4; q++)
 #pragma unroll
                 for (int c = 0; c < LAY::nc(t); c++)
-                    tma_load_1d(dst + LAY::off(t, q, c), a.t[t].in[c] + q * Q + (u64)tile * TQ, TQ * 8, &bars[s]);
+                    tma_load_1d(dst + LAY::off(t, q, c), a.t[t].in[c] + q * Q + (u64)tile * TQ, TQ * 8, &full_bar[s]);
     };
-    if (threadIdx.x == 0)
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < S; s++) {
+            mbar_init(&full_bar[s], 1);
+            reads_done[s] = 0;
+            issued_cnt[s] = 0;
+        }
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        // the tile of iteration j goes to stage j % S; keep S tiles in flight
         for (int s = 0; s < S; s++) {
             u32 tile = blockIdx.x + s * G;
-            if (tile < ntiles) issue(tile, s);
+            if (tile < ntiles) { issue(tile, s); issued_cnt[s]++; }
         }
+    }
+    __syncthreads();
     P acc;
     acc.init();
     F3 rr;
     Mul3 r = load_challenge_mul(a, rr);
     if (!ECH) r = mul3_prepare<false>(rr);
     F3 lo[3], hi[3];
+    bool abort = false;
     u32 i = 0;
     for (u32 tile = blockIdx.x; tile < ntiles; tile += G, i++) {
         const int s = i % S;
-        const u32 phase = (i / S) & 1u;
-        if (!mbar_wait_bounded(&bars[s], phase)) s_abort = 1;
-        __syncthreads();
-        if (s_abort) break;
+        if (!mbar_wait_bounded(&full_bar[s], (i / S) & 1u)) { abort = true; break; }
         const u64* st_ = tma_smem + (size_t)s * SW;
         const u64 k = (u64)tile * TQ + threadIdx.x;
 #pragma unroll
@@ -555,6 +558,23 @@ __global__ void __launch_bounds__(TPB, 2) k_fused_tma(RoundArgs a, u32 ntiles) {
                     x[q].c1 = x[q].c2 = 0;
                 }
             }
+            if (t == NT - 1) {
+                // this warp is done with the stage; the last warp to finish
+                // reading refills it with the tile of iteration i + S
+                __syncwarp();
+                if (lane == 0) {
+                    __threadfence_block();
+                    if (atomicAdd(&reads_done[s], 1u) == NWARP - 1) {
+                        atomicExch(&reads_done[s], 0u);
+                        const u32 nt = blockIdx.x + (i + S) * G;
+                        if (nt < ntiles) {
+                            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                            issue(nt, s);
+                            issued_cnt[s]++;
+                        }
+                    }
+                }
+            }
             if (ext_of<M>(t)) { lo[t] = f3_fold<true, true>(x[0], x[2], r); hi[t] = f3_fold<true, true>(x[1], x[3], r); }
             else if (ECH) { lo[t] = f3_fold<false, true>(x[0], x[2], r); hi[t] = f3_fold<false, true>(x[1], x[3], r); }
             else { lo[t] = f3_fold<false, false>(x[0], x[2], r); hi[t] = f3_fold<false, false>(x[1], x[3], r); }
@@ -562,21 +582,14 @@ __global__ void __launch_bounds__(TPB, 2) k_fused_tma(RoundArgs a, u32 ntiles) {
             else { st<false>(a.t[t].out, k, lo[t]); st<false>(a.t[t].out, k + Q, hi[t]); }
         }
         acc.pair(lo, hi);
-        __syncthreads();   // every thread is done with stage s
-        if (threadIdx.x == 0) {
-            u32 nt = tile + S * G;
-            if (nt < ntiles) {
-                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-                issue(nt, s);
-            }
-        }
     }
-    if (s_abort) {
-        // drain this block's copies in flight (bounded), then report and stop
+    if (__syncthreads_or(abort)) {
+        // drain the copies in flight (bounded): stage s has completed
+        // consumed(s) phases and holds issued_cnt[s] - consumed(s) more
         if (threadIdx.x == 0) {
-            u32 j = i;
-            for (u32 tile = blockIdx.x + i * G; tile < ntiles && j < i + S; tile += G, j++)
-                mbar_wait_bounded(&bars[j % S], (j / S) & 1u);
+            for (int s = 0; s < S; s++)
+                for (u32 ph = i / S + (s < (int)(i % S) ? 1u : 0u); ph < issued_cnt[s]; ph++)
+                    mbar_wait_bounded(&full_bar[s], ph & 1u);
             if (a.status) *(volatile u32*)a.status = EFFSC_STATUS_TIMEOUT;
         }
         return;
