@@ -59,6 +59,14 @@ struct RoundArgs {
     TxIO tx;
 };
 
+// Batched rounds: one entry per active instance, sorted by first_block.
+struct BatchSeg {
+    u32 first_block;
+    u32 nblocks;
+    u32 inst;
+    u32 reserved;
+};
+
 int pol_ntables(int pol);
 int pol_nraw(int pol);
 int pol_nwire(int pol);
@@ -72,6 +80,9 @@ bool launch_eqf_left(bool fused, u32 mask, bool ech, const RoundArgs& a, int gri
 // if no kernel is instantiated for the combination.
 bool launch_fused_tma(int pol, u32 mask, bool ech, const RoundArgs& a, u32 ntiles, int grid, cudaStream_t s);
 int fused_tma_blocks_per_sm(void);
+bool launch_batch_round(int pol, bool fused, u32 mask, bool ech, const BatchSeg* segs, u32 nsegs,
+                        const RoundArgs* args, u32 grid, cudaStream_t s);
+void launch_batch_finalize(const RoundArgs* args, const unsigned char* ext, u32 n, int ntab, u64* finals, cudaStream_t s);
 
 // Utility kernels.
 void launch_split_aos(const u64* aos, u64 n, int ncomp, u64* c0, u64* c1, u64* c2, int from_mont, u32* ext_flag, cudaStream_t s);

@@ -248,9 +248,10 @@ static __device__ __noinline__ void finalize_warp(int pol, const u64* raw, const
     }
 }
 
-// Block + grid reduction of NRAW Fp3 values; the last block finalises.
+// Block + grid reduction of NRAW Fp3 values over the nb blocks of one round
+// (this block is number bid); the last block to finish finalises.
 template <int NRAW>
-__device__ __forceinline__ void reduce_and_finalize(F3 (&v)[NRAW], const RoundArgs& a, int pol) {
+__device__ __forceinline__ void reduce_and_finalize_seg(F3 (&v)[NRAW], const RoundArgs& a, int pol, u32 nb, u32 bid) {
     __shared__ u64 s_red[NWARP][RAW_WORDS];
     __shared__ u64 s_tot[RAW_WORDS];
     __shared__ int s_last;
@@ -273,15 +274,15 @@ __device__ __forceinline__ void reduce_and_finalize(F3 (&v)[NRAW], const RoundAr
         u64 s = 0;
 #pragma unroll
         for (int w = 0; w < NWARP; w++) s = gl_add(s, s_red[w][threadIdx.x]);
-        if (gridDim.x == 1) s_tot[threadIdx.x] = s;
-        else a.partials[(u64)blockIdx.x * RAW_WORDS + threadIdx.x] = s;
+        if (nb == 1) s_tot[threadIdx.x] = s;
+        else a.partials[(u64)bid * RAW_WORDS + threadIdx.x] = s;
     }
-    if (gridDim.x > 1) {
+    if (nb > 1) {
         __threadfence();
         __syncthreads();
         if (threadIdx.x == 0) {
             u32 t = atomicAdd(a.counter, 1u);
-            s_last = (t == gridDim.x - 1);
+            s_last = (t == nb - 1);
         }
         __syncthreads();
         if (!s_last) return;
@@ -289,7 +290,7 @@ __device__ __forceinline__ void reduce_and_finalize(F3 (&v)[NRAW], const RoundAr
         // every thread owns one of the 3*NRAW words and walks the partials
         u64 acc[RAW_WORDS];
         for (int i = 0; i < 3 * NRAW; i++) acc[i] = 0;
-        for (u32 b = threadIdx.x; b < gridDim.x; b += TPB)
+        for (u32 b = threadIdx.x; b < nb; b += TPB)
             for (int i = 0; i < 3 * NRAW; i++) acc[i] = gl_add(acc[i], __ldcg(&a.partials[(u64)b * RAW_WORDS + i]));
 #pragma unroll
         for (int off = 16; off; off >>= 1)
@@ -311,6 +312,11 @@ __device__ __forceinline__ void reduce_and_finalize(F3 (&v)[NRAW], const RoundAr
     if (warp == 0) finalize_warp(pol, s_tot, a);
 }
 
+template <int NRAW>
+__device__ __forceinline__ void reduce_and_finalize(F3 (&v)[NRAW], const RoundArgs& a, int pol) {
+    reduce_and_finalize_seg<NRAW>(v, a, pol, gridDim.x, blockIdx.x);
+}
+
 __device__ __forceinline__ Mul3 load_challenge_mul(const RoundArgs& a, F3& r) {
     if (a.chal_ptr) r = f3_make(a.chal_ptr[0], a.chal_ptr[1], a.chal_ptr[2]);
     else r = f3_make(a.chal[0], a.chal[1], a.chal[2]);
@@ -323,12 +329,12 @@ __device__ __forceinline__ Mul3 load_challenge_mul(const RoundArgs& a, F3& r) {
 
 // Unfused evaluation of the round polynomial on the current tables.
 template <int POL, int SEM, u32 M>
-__global__ void __launch_bounds__(TPB) k_eval(RoundArgs a) {
+__device__ __forceinline__ void eval_body(const RoundArgs& a, u32 bid, u32 nb) {
     using P = Policy<POL, M>;
     P acc;
     acc.init();
     const u64 L = a.L;
-    const u64 tid = (u64)blockIdx.x * TPB + threadIdx.x, stride = (u64)gridDim.x * TPB;
+    const u64 tid = (u64)bid * TPB + threadIdx.x, stride = (u64)nb * TPB;
     F3 lo[3], hi[3];
     if (SEM == SEM_MSB_PAD) {
         if (L == 1) {
@@ -377,7 +383,11 @@ __global__ void __launch_bounds__(TPB) k_eval(RoundArgs a) {
     }
     F3 raw[P::NRAW];
     acc.result(raw);
-    reduce_and_finalize<P::NRAW>(raw, a, POL);
+    reduce_and_finalize_seg<P::NRAW>(raw, a, POL, nb, bid);
+}
+template <int POL, int SEM, u32 M>
+__global__ void __launch_bounds__(TPB) k_eval(RoundArgs a) {
+    eval_body<POL, SEM, M>(a, blockIdx.x, gridDim.x);
 }
 
 // Fused fold + evaluate.  Requires L % 4 == 0 (and L a power of two for the
@@ -385,7 +395,7 @@ __global__ void __launch_bounds__(TPB) k_eval(RoundArgs a) {
 // are exactly the quadruples (k, k+Q, k+2Q, k+3Q) (MSB) or (4k..4k+3) (LSB).
 // Every table is folded; outputs are Fp3 when the challenge is.
 template <int POL, int SEM, u32 M, bool ECH>
-__global__ void __launch_bounds__(TPB, 2) k_fused(RoundArgs a) {
+__device__ __forceinline__ void fused_body(const RoundArgs& a, u32 bid, u32 nb) {
     constexpr int NT = Policy<POL, 0>::NT;
     constexpr u32 FULL = (1u << NT) - 1;
     constexpr u32 MO = ECH ? FULL : M;
@@ -396,7 +406,7 @@ __global__ void __launch_bounds__(TPB, 2) k_fused(RoundArgs a) {
     Mul3 r = load_challenge_mul(a, rr);
     if (!ECH) r = mul3_prepare<false>(rr);
     const u64 Q = a.L >> 2;
-    const u64 tid = (u64)blockIdx.x * TPB + threadIdx.x, stride = (u64)gridDim.x * TPB;
+    const u64 tid = (u64)bid * TPB + threadIdx.x, stride = (u64)nb * TPB;
     F3 lo[3], hi[3];
     for (u64 k = tid; k < Q; k += stride) {
 #pragma unroll
@@ -425,7 +435,11 @@ __global__ void __launch_bounds__(TPB, 2) k_fused(RoundArgs a) {
     }
     F3 raw[P::NRAW];
     acc.result(raw);
-    reduce_and_finalize<P::NRAW>(raw, a, POL);
+    reduce_and_finalize_seg<P::NRAW>(raw, a, POL, nb, bid);
+}
+template <int POL, int SEM, u32 M, bool ECH>
+__global__ void __launch_bounds__(TPB, 2) k_fused(RoundArgs a) {
+    fused_body<POL, SEM, M, ECH>(a, blockIdx.x, gridDim.x);
 }
 
 // ---------------------------------------------------------------------------

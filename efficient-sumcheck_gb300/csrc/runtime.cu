@@ -787,6 +787,16 @@ Chal host_chal(const effsc_prover* P, const uint64_t* c) {
 
 }  // namespace
 
+// Internal accessors used by batch.cu / serve.cu.
+void effsc_internal_tx_state(const effsc_transcript* t, void* out) {
+    DevTranscript st = t->st;
+    if (t->kind != EFFSC_T_KECCAK) st.deg = 0;   // marks a transcript the device cannot run
+    memcpy(out, &st, sizeof st);
+}
+int effsc_internal_ctx_device(const effsc_ctx* c) { return c->device; }
+cudaStream_t effsc_internal_ctx_stream(const effsc_ctx* c) { return c->stream; }
+uint64_t effsc_internal_add_launches(uint64_t k) { g_launches += k; return g_launches; }
+
 // ===========================================================================
 // C ABI
 // ===========================================================================

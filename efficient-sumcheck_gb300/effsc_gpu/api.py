@@ -410,6 +410,104 @@ def build_eq_table(w, field=FP3, repr=CANONICAL, ctx=None):
     return out if field == FP3 else out.reshape(-1)
 
 
+class Batch:
+    """Many independent MSB InnerProduct (kind=IP) or Multilinear (kind=ML)
+    provers proved together (effsc_batch_*): one kernel per round for every
+    instance still active, the whole protocol replayed as one CUDA graph.
+
+    ``tables`` is a list per instance of base-field tables (IP: [a, b],
+    ML: [v]), each of 2^num_vars canonical words; or pass ``seeds`` (a list per
+    instance of per-table seeds) to generate gen_uniform tables on the device.
+    Instance i's proof is the one runner::sumcheck (src/runner.rs:29-69)
+    produces with num_vars[i] rounds, transcript i and no hook.
+    """
+
+    def __init__(self, kind, num_vars, tables=None, seeds=None, field=FP3, ctx=None):
+        self.ctx = ctx or Context.default()
+        self.kind, self.field = kind, field
+        self.num_vars = [int(v) for v in num_vars]
+        n = len(self.num_vars)
+        ntab = 2 if kind == IP else 1
+        self.ntab = ntab
+        nv = (ctypes.c_uint32 * n)(*self.num_vars)
+        tp = None
+        sp = None
+        keep = []
+        if tables is not None:
+            flat = []
+            for i, ts in enumerate(tables):
+                if len(ts) != ntab:
+                    raise ValueError("instance %d: expected %d tables" % (i, ntab))
+                for t in ts:
+                    a = np.ascontiguousarray(np.asarray(t, dtype=np.uint64).reshape(-1))
+                    if a.size != 1 << self.num_vars[i]:
+                        raise ValueError("instance %d: table length %d != 2^%d" % (i, a.size, self.num_vars[i]))
+                    keep.append(a)
+                    flat.append(_p(a))
+            tp = (u64p * len(flat))(*flat)
+        else:
+            sd = np.ascontiguousarray(np.asarray(seeds, dtype=np.uint64).reshape(-1))
+            if sd.size != n * ntab:
+                raise ValueError("need %d seeds" % (n * ntab))
+            keep.append(sd)
+            sp = _p(sd)
+        h = vp()
+        check(load().effsc_batch_create(self.ctx.h, kind, field, n, nv, tp, sp, ctypes.byref(h)))
+        self.h = h
+        self.rows = np.concatenate([[0], np.cumsum(self.num_vars)]).astype(np.int64)
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib._lib is not None:
+            _lib._lib.effsc_batch_destroy(self.h)
+            self.h = None
+
+    def __len__(self):
+        return len(self.num_vars)
+
+    def degree(self):
+        return 2 if self.kind == IP else 1
+
+    def _tx_array(self, transcripts):
+        if len(transcripts) != len(self):
+            raise ValueError("one transcript per instance")
+        return (vp * len(transcripts))(*[t.h for t in transcripts])
+
+    def prove_raw(self, transcripts, use_graph=True, outputs=True):
+        """Run the protocol; returns (round_polys, challenges, final_values) as
+        flat arrays (rows concatenated in instance order) or None."""
+        d, f, rows = self.degree(), self.field, int(self.rows[-1])
+        if not outputs:
+            check(load().effsc_batch_prove(self.h, self._tx_array(transcripts), 1 if use_graph else 0, None, None, None))
+            return None
+        rp = np.zeros((rows, d, f), dtype=np.uint64)
+        ch = np.zeros((rows, f), dtype=np.uint64)
+        fv = np.zeros((len(self), f), dtype=np.uint64)
+        check(load().effsc_batch_prove(self.h, self._tx_array(transcripts), 1 if use_graph else 0,
+                                       _p(rp), _p(ch), _p(fv)))
+        return rp, ch, fv
+
+    def prove(self, transcripts, use_graph=True):
+        """One SumcheckProof per instance."""
+        rp, ch, fv = self.prove_raw(transcripts, use_graph)
+        return [SumcheckProof(rp[self.rows[i]:self.rows[i + 1]], ch[self.rows[i]:self.rows[i + 1]], fv[i])
+                for i in range(len(self))]
+
+    def set_quads_per_thread(self, q):
+        check(load().effsc_batch_set_quads_per_thread(self.h, int(q)))
+
+    def tune(self, transcripts, cache_path=None):
+        """Autotune quadruples per thread; returns the chosen value."""
+        c = ctypes.c_int()
+        path = cache_path.encode() if cache_path else None
+        check(load().effsc_batch_tune(self.h, self._tx_array(transcripts), path, ctypes.byref(c)))
+        return c.value
+
+    def device_table(self, inst, t):
+        out = u64p()
+        check(load().effsc_batch_device_table(self.h, inst, t, ctypes.byref(out)))
+        return ctypes.cast(out, ctypes.c_void_p).value
+
+
 def gen_uniform(seed, n, ctx=None):
     """Seeded uniform canonical table (host array)."""
     ctx = ctx or Context.default()

@@ -206,6 +206,36 @@ uint64_t effsc_table_seed(uint64_t seed, uint64_t table);
  * thread of a full grid; the denominator of the integer-multiply roofline. */
 int effsc_diag_mulmod_rate(effsc_ctx* ctx, double* mulmod_per_s, double* fp3_mul_per_s);
 
+/* ---- batches: many independent provers, one launch per round -------------
+ * No reference counterpart (the crate proves one instance per call).  A batch
+ * holds n_inst InnerProductProver (kind EFFSC_IP, tables a and b) or
+ * MultilinearProver (EFFSC_ML) instances in MSB order; instance i has
+ * num_vars[i] (1..34) variables and power-of-two tables of 2^num_vars[i]
+ * base-field elements: host_tables[i * ntab + t] (canonical words) or, when
+ * host_tables is NULL, the seeded uniform tables of effsc_gen_uniform with
+ * seed seeds[i * ntab + t].  effsc_batch_prove proves every instance with all
+ * num_vars[i] rounds -- runner::sumcheck (src/runner.rs:29-69) with the
+ * Keccak transcript transcripts[i], no hook -- running one kernel per round
+ * for all instances still active (replayed as one CUDA graph when use_graph).
+ * Each proof is bit-identical to proving that instance alone.  Outputs are
+ * concatenated: instance i's rounds start at row R_i = num_vars[0] + ... +
+ * num_vars[i-1] (round_polys: deg elements per row, challenges: 1 element per
+ * row), final_values[i]; all canonical, `field` words per element.  The
+ * input tables are never written, so the batch can be proved again. */
+typedef struct effsc_batch effsc_batch;
+int effsc_batch_create(effsc_ctx* ctx, int kind, int field, size_t n_inst, const uint32_t* num_vars,
+                       const uint64_t* const* host_tables, const uint64_t* seeds, effsc_batch** out);
+int effsc_batch_destroy(effsc_batch* b);
+int effsc_batch_prove(effsc_batch* b, const effsc_transcript* const* transcripts, int use_graph,
+                      uint64_t* round_polys, uint64_t* challenges, uint64_t* final_values);
+/* Work granularity: quadruples per thread of a round's blocks (1..64). */
+int effsc_batch_set_quads_per_thread(effsc_batch* b, int quads_per_thread);
+/* Autotuner: times quads-per-thread 1, 2, 4, 8 on this batch, keeps the
+ * fastest and appends the measurement to cache_path (JSON lines) if given. */
+int effsc_batch_tune(effsc_batch* b, const effsc_transcript* const* transcripts, const char* cache_path, int* chosen);
+/* Device address of instance inst's input table (2^num_vars canonical words). */
+int effsc_batch_device_table(effsc_batch* b, size_t inst, int table, const uint64_t** out);
+
 /* ---- one round without allocation -----------------------------------------
  * No counterpart in the reference.  For callers that must not allocate device
  * memory (a host application whose own pool has reserved the HBM, or work
