@@ -432,7 +432,7 @@ def run_batch(args, E, L, ctx, stream, rank):
     b = E.Batch(E.IP, nv, seeds=seeds, field=E.FP3, ctx=ctx)
     txs = lambda: [E.Transcript.keccak(E.FP3, batch_label(i)) for i in range(count)]  # noqa: E731
     cache = os.path.join(PKG, "_build", "autotune.jsonl")
-    q = b.tune(txs(), cache_path=cache)
+    q, tail = b.tune(txs(), cache_path=cache)
     tune_rec = None
     try:
         tune_rec = json.loads(open(cache).read().strip().splitlines()[-1])
@@ -505,7 +505,7 @@ def run_batch(args, E, L, ctx, stream, rank):
         "instances": count, "total_evals": evals, "algorithmic_bytes": alg,
         "batched": {"ms_per_cohort": ms_batch, "proofs_per_s": count / (ms_batch * 1e-3),
                     "evals_per_s": evals / (ms_batch * 1e-3), "hbm_gbs": alg / (ms_batch * 1e-3) / 1e9,
-                    "launches_per_cohort": max(nv) + 1, "quads_per_thread": q,
+                    "quads_per_thread": q, "tail_len": tail,
                     "path": "effsc_batch_prove: one kernel per round for all active instances, one CUDA graph, "
                             "proofs copied back every step"},
         "one_at_a_time": {"ms_per_cohort": ms_solo, "proofs_per_s": count / (ms_solo * 1e-3),

@@ -46,7 +46,13 @@ struct effsc_batch {
     std::vector<u64*> work;                // n * ntab work tables (3 component arrays for Fp3)
     // schedule
     int quads_per_thread = 2;
+    u64 tail_len = ~0ULL;                  // tables of at most this length finish in the tail kernel
     bool planned = false;
+    std::vector<u32> tail_r0;              // first tail round per instance (nv[i]: no tail)
+    TailArgs* d_tail = nullptr;
+    u32 n_tail = 0;
+    u64 tail_smem_len = 0;
+    u32 rounds_planned = 0;                // batched round kernels before the tail
     std::vector<size_t> seg_off, seg_cnt;  // per round into d_segs
     std::vector<u32> grid;                 // blocks per round
     BatchSeg* d_segs = nullptr;
@@ -76,6 +82,9 @@ void free_schedule(effsc_batch* b) {
     if (b->d_fin_args) cudaFreeAsync(b->d_fin_args, s);
     if (b->d_ext) cudaFreeAsync(b->d_ext, s);
     if (b->d_partials) cudaFreeAsync(b->d_partials, s);
+    if (b->d_tail) cudaFreeAsync(b->d_tail, s);
+    b->d_tail = nullptr;
+    b->n_tail = 0;
     b->d_segs = nullptr; b->d_args = nullptr; b->d_fin_args = nullptr; b->d_ext = nullptr; b->d_partials = nullptr;
     if (b->gexec) { cudaGraphExecDestroy(b->gexec); b->gexec = nullptr; }
     b->planned = false;
@@ -85,10 +94,23 @@ void free_schedule(effsc_batch* b) {
 int plan(effsc_batch* b) {
     free_schedule(b);
     const int F3W = b->field == EFFSC_FP3 ? 3 : 1;
-    const u32 R = b->max_nv;
+    // tail switch: instance i runs rounds tail_r0[i] .. n_i - 1 in the one-block
+    // tail kernel, starting from a table of at most `tl` entries
+    const u64 tl = std::min<u64>(b->tail_len, tail_max_len(b->pol, F3W, TAIL_SMEM_CAP));
+    u32 tail_log = 0;
+    while ((2ULL << tail_log) <= tl) tail_log++;
+    b->tail_r0.assign(b->n, 0);
+    u32 R = 0;
+    for (size_t i = 0; i < b->n; i++) {
+        const u32 n_i = b->nv[i];
+        if (tail_log < 2) b->tail_r0[i] = n_i;
+        else b->tail_r0[i] = n_i <= tail_log ? 0 : n_i - tail_log + 1;
+        R = std::max<u32>(R, b->tail_r0[i]);
+    }
     const int maxb = max_grid();
     std::vector<BatchSeg> segs;
     std::vector<RoundArgs> args((size_t)R * b->n);
+    b->rounds_planned = R;
     b->seg_off.assign(R, 0);
     b->seg_cnt.assign(R, 0);
     b->grid.assign(R, 0);
@@ -100,7 +122,7 @@ int plan(effsc_batch* b) {
         u32 first = 0;
         for (size_t i = 0; i < b->n; i++) {
             const u32 n_i = b->nv[i];
-            if (n_i <= r) continue;
+            if (b->tail_r0[i] <= r) continue;
             const u64 L = r == 0 ? (1ULL << n_i) : (1ULL << (n_i - r + 1));
             const u64 work = r == 0 ? L / 2 : L / 4;
             u64 nb = (work + (u64)KERNEL_TPB * b->quads_per_thread - 1) / ((u64)KERNEL_TPB * b->quads_per_thread);
@@ -159,8 +181,44 @@ int plan(effsc_batch* b) {
         fin[i] = a;
         ext[i] = e ? 1 : 0;
     }
+    // tail kernel arguments (one block per instance with tail rounds)
+    std::vector<TailArgs> tails;
+    b->tail_smem_len = 0;
+    for (size_t i = 0; i < b->n; i++) {
+        const u32 n_i = b->nv[i], r0 = b->tail_r0[i];
+        if (r0 >= n_i) continue;
+        TailArgs ta;
+        memset(&ta, 0, sizeof ta);
+        ta.L = r0 == 0 ? (1ULL << n_i) : (1ULL << (n_i - r0 + 1));
+        const u32 folds = n_i - r0 - (r0 == 0 ? 1 : 0);
+        const u64 half0 = 1ULL << (n_i - 1);
+        for (int t = 0; t < b->ntab; t++) {
+            u64* inb = b->in[i * b->ntab + t];
+            u64* wk = b->work[i * b->ntab + t];
+            if (r0 <= 1) ta.in[t][0] = inb;
+            else {
+                for (int c = 0; c < F3W; c++) ta.in[t][c] = wk + c * half0;
+                if (F3W == 3) ta.in_ext |= 1u << t;
+            }
+            if (folds)
+                for (int c = 0; c < F3W; c++) ta.out[t][c] = wk + c * half0;
+        }
+        ta.nrounds = n_i - r0;
+        ta.first_fold = r0 >= 1;
+        ta.chal_in = r0 >= 1 ? b->d_chal + 3 * (b->round_off[i] + r0 - 1) : nullptr;
+        ta.tx = b->d_tx + i;
+        ta.proof_wire = b->d_wire + 3 * deg_of(b) * (b->round_off[i] + r0);
+        ta.proof_chal = b->d_chal + 3 * (b->round_off[i] + r0);
+        tails.push_back(ta);
+        b->tail_smem_len = std::max<u64>(b->tail_smem_len, ta.L);
+    }
     cudaStream_t s = b->stream;
     BCK(cudaMallocAsync((void**)&b->d_partials, max_blocks * 12 * sizeof(u64), s));
+    b->n_tail = (u32)tails.size();
+    if (!tails.empty()) {
+        BCK(cudaMallocAsync((void**)&b->d_tail, tails.size() * sizeof(TailArgs), s));
+        BCK(cudaMemcpyAsync(b->d_tail, tails.data(), tails.size() * sizeof(TailArgs), cudaMemcpyHostToDevice, s));
+    }
     // per-instance partial ranges: block-index offsets within each round
     for (u32 r = 0; r < R; r++)
         for (size_t k = 0; k < b->seg_cnt[r]; k++) {
@@ -183,12 +241,17 @@ int plan(effsc_batch* b) {
 int launch_protocol(effsc_batch* b, uint64_t* kernels) {
     const bool ech = b->field == EFFSC_FP3;
     const u32 full = (1u << b->ntab) - 1;
-    for (u32 r = 0; r < b->max_nv; r++) {
+    for (u32 r = 0; r < b->rounds_planned; r++) {
         if (!b->seg_cnt[r]) continue;
         u32 mask = r >= 2 && ech ? full : 0;
         bool ok = launch_batch_round(b->pol, r > 0, mask, r > 0 && ech, b->d_segs + b->seg_off[r], (u32)b->seg_cnt[r],
                                      b->d_args + (size_t)r * b->n, b->grid[r], b->stream);
         if (!ok) return effsc_set_error(EFFSC_UNSUPPORTED, "no batched kernel for this round");
+        (*kernels)++;
+    }
+    if (b->n_tail) {
+        if (!launch_tail(b->pol, b->field == EFFSC_FP3 ? 3 : 1, b->d_tail, nullptr, b->n_tail, b->tail_smem_len, b->stream))
+            return effsc_set_error(EFFSC_UNSUPPORTED, "no tail kernel for this batch");
         (*kernels)++;
     }
     launch_batch_finalize(b->d_fin_args, b->d_ext, (u32)b->n, b->ntab, b->d_final, b->stream);
@@ -304,6 +367,14 @@ int effsc_batch_set_quads_per_thread(effsc_batch* b, int q) {
     return plan(b);
 }
 
+int effsc_batch_set_tail(effsc_batch* b, uint64_t max_len) {
+    if (!b) return effsc_set_error(EFFSC_INVALID_ARG, "NULL batch");
+    if (max_len == b->tail_len && b->planned) return EFFSC_OK;
+    BCK(cudaSetDevice(b->device));
+    b->tail_len = max_len;
+    return plan(b);
+}
+
 int effsc_batch_device_table(effsc_batch* b, size_t inst, int table, const uint64_t** out) {
     if (!b || !out || inst >= b->n || table < 0 || table >= b->ntab) return effsc_set_error(EFFSC_INVALID_ARG, "bad index");
     *out = (const uint64_t*)b->in[inst * b->ntab + table];
@@ -368,49 +439,66 @@ int effsc_batch_prove(effsc_batch* b, const effsc_transcript* const* transcripts
     return EFFSC_OK;
 }
 
-// Autotuner: time the batched protocol for quads-per-thread in {1, 2, 4, 8}
-// (after one warm-up each), keep the fastest, and append the choice to
-// cache_path (one JSON object per line) when it is given.
-int effsc_batch_tune(effsc_batch* b, const effsc_transcript* const* transcripts, const char* cache_path, int* chosen) {
+// Autotuner: time the batched protocol (one warm-up, then 3 replays each)
+// over quadruples per thread {1, 2, 4, 8} x tail switch {off, 2^6, 2^8, 2^10,
+// as large as shared memory allows}, keep the fastest, and append every
+// measurement to cache_path (one JSON object per line) when it is given.
+int effsc_batch_tune(effsc_batch* b, const effsc_transcript* const* transcripts, const char* cache_path,
+                     int* quads_per_thread, uint64_t* tail_len) {
     if (!b || !transcripts) return effsc_set_error(EFFSC_INVALID_ARG, "NULL argument");
     BCK(cudaSetDevice(b->device));
-    const int cands[4] = {1, 2, 4, 8};
+    const int qs[4] = {1, 2, 4, 8};
+    const uint64_t tls[5] = {0, 1ULL << 6, 1ULL << 8, 1ULL << 10, ~0ULL};
     double best_ms = 1e30;
-    int best = b->quads_per_thread;
+    int best_q = b->quads_per_thread;
+    uint64_t best_t = b->tail_len;
     cudaEvent_t e0, e1;
     BCK(cudaEventCreate(&e0));
     BCK(cudaEventCreate(&e1));
-    double times[4] = {0, 0, 0, 0};
-    for (int k = 0; k < 4; k++) {
-        int rc = effsc_batch_set_quads_per_thread(b, cands[k]);
-        if (rc != EFFSC_OK) return rc;
-        rc = effsc_batch_prove(b, transcripts, 1, nullptr, nullptr, nullptr);   // warm-up + capture
-        if (rc != EFFSC_OK) return rc;
-        float ms = 0;
-        const int reps = 3;
-        BCK(cudaEventRecord(e0, b->stream));
-        for (int r = 0; r < reps; r++) {
-            rc = effsc_batch_prove(b, transcripts, 1, nullptr, nullptr, nullptr);
+    double times[5][4];
+    for (int ti = 0; ti < 5; ti++)
+        for (int k = 0; k < 4; k++) {
+            b->quads_per_thread = qs[k];
+            b->tail_len = tls[ti];
+            int rc = plan(b);
             if (rc != EFFSC_OK) return rc;
+            rc = effsc_batch_prove(b, transcripts, 1, nullptr, nullptr, nullptr);   // warm-up + capture
+            if (rc != EFFSC_OK) return rc;
+            float ms = 0;
+            const int reps = 3;
+            BCK(cudaEventRecord(e0, b->stream));
+            for (int r = 0; r < reps; r++) {
+                rc = effsc_batch_prove(b, transcripts, 1, nullptr, nullptr, nullptr);
+                if (rc != EFFSC_OK) return rc;
+            }
+            BCK(cudaEventRecord(e1, b->stream));
+            BCK(cudaEventSynchronize(e1));
+            BCK(cudaEventElapsedTime(&ms, e0, e1));
+            times[ti][k] = ms / reps;
+            if (times[ti][k] < best_ms) { best_ms = times[ti][k]; best_q = qs[k]; best_t = tls[ti]; }
         }
-        BCK(cudaEventRecord(e1, b->stream));
-        BCK(cudaEventSynchronize(e1));
-        BCK(cudaEventElapsedTime(&ms, e0, e1));
-        times[k] = ms / reps;
-        if (times[k] < best_ms) { best_ms = times[k]; best = cands[k]; }
-    }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    int rc = effsc_batch_set_quads_per_thread(b, best);
+    b->quads_per_thread = best_q;
+    b->tail_len = best_t;
+    int rc = plan(b);
     if (rc != EFFSC_OK) return rc;
-    if (chosen) *chosen = best;
+    if (quads_per_thread) *quads_per_thread = best_q;
+    if (tail_len) *tail_len = best_t;
     if (cache_path && *cache_path) {
         FILE* fp = fopen(cache_path, "a");
         if (fp) {
-            int sms = max_grid() / 8;
-            fprintf(fp, "{\"kernel\": \"batch_round\", \"kind\": %d, \"field\": %d, \"instances\": %zu, \"max_num_vars\": %u, "
-                        "\"sms\": %d, \"quads_per_thread\": %d, \"ms\": {\"1\": %.4f, \"2\": %.4f, \"4\": %.4f, \"8\": %.4f}}\n",
-                    b->kind, b->field, b->n, b->max_nv, sms, best, times[0], times[1], times[2], times[3]);
+            const int sms = max_grid() / 8;
+            const u64 tmax = tail_max_len(b->pol, b->field == EFFSC_FP3 ? 3 : 1, TAIL_SMEM_CAP);
+            fprintf(fp, "{\"kernel\": \"batch_round\", \"kind\": %d, \"field\": %d, \"instances\": %zu, "
+                        "\"max_num_vars\": %u, \"sms\": %d, \"quads_per_thread\": %d, \"tail_len\": %llu, \"ms\": {",
+                    b->kind, b->field, b->n, b->max_nv, sms, best_q,
+                    (unsigned long long)std::min<uint64_t>(best_t, tmax));
+            for (int ti = 0; ti < 5; ti++)
+                for (int k = 0; k < 4; k++)
+                    fprintf(fp, "%s\"q%d/tail%llu\": %.4f", (ti || k) ? ", " : "", qs[k],
+                            (unsigned long long)std::min<uint64_t>(tls[ti], tmax), times[ti][k]);
+            fprintf(fp, "}}\n");
             fclose(fp);
         }
     }

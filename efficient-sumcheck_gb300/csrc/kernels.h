@@ -67,6 +67,31 @@ struct BatchSeg {
     u32 reserved;
 };
 
+// The last rounds of an MSB Multilinear / InnerProduct proof run by one block
+// with the tables in shared memory: rounds r0 .. r0 + nrounds - 1, each a
+// fold with the previous challenge (except a first round 0) plus evaluation,
+// block reduction and the transcript step, without a kernel boundary.
+struct TailArgs {
+    const u64* in[3][3];   // [table][component] current tables (length L)
+    u64* out[3][3];        // tables after the tail's last fold (null: none)
+    u64 L;                 // power of two, length at the start of round r0
+    u32 in_ext;            // bit t: table t is stored with 3 components
+    u32 nrounds;
+    u32 first_fold;        // 1: the first round folds with chal_in first
+    u32 hook_len;
+    const u64* chal_in;    // challenge of the round before r0 (3 words)
+    void* tx;              // DevTranscript*
+    const uint8_t* hook;
+    u64* proof_wire;       // round r0's wire values (3 * nwire words per round)
+    u64* proof_chal;       // round r0's challenge (3 words per round)
+};
+// Largest table length (a power of two) the tail kernel holds for this
+// policy and field width (1: Fp, 3: Fp3), within `smem_cap` bytes.
+u64 tail_max_len(int pol, int fw, u64 smem_cap);
+constexpr u64 TAIL_SMEM_CAP = 200 * 1024;
+// One block per TailArgs; `smem_len` = largest L among them.
+bool launch_tail(int pol, int fw, const TailArgs* dev_args, const TailArgs* one, u32 n, u64 smem_len, cudaStream_t s);
+
 int pol_ntables(int pol);
 int pol_nraw(int pol);
 int pol_nwire(int pol);

@@ -258,6 +258,9 @@ struct effsc_prover {
     uint64_t g_kernels = 0;                    // kernel nodes in the graph
     TabState g_post[3];
     size_t g_post_rounds = 0;
+    // effsc_prove: tables of at most this length finish in the one-block tail
+    // kernel (SIZE_MAX: as large as shared memory allows; 0: never)
+    size_t tail_len = SIZE_MAX;
 };
 
 namespace {
@@ -482,6 +485,64 @@ int round_std(effsc_prover* P, const Chal& ch, const TxIO& tx, bool dry) {
     uint64_t bytes = 0;
     for (int i = 0; i < nt; i++) bytes += L * wbytes(P->t[i].ext);
     if (!dry) TRY(timed_launch(P->ctx->stream, "evaluate", bytes, [&] { return launch_eval(pol, sem, mask_of(P, idx, nt), a, grid_for(work), P->ctx->stream); }));
+    return EFFSC_OK;
+}
+
+// Whether rounds r .. num_rounds-1 of effsc_prove can run in the one-block
+// tail kernel: MSB Multilinear / InnerProduct, equal power-of-two tables that
+// fit in shared memory, challenges in device memory, and every round still
+// folding to at least two entries (the length-1 cases stay on the per-round
+// path).
+bool tail_ok(const effsc_prover* P, size_t r, size_t num_rounds, const Chal& ch) {
+    if ((P->kind != EFFSC_ML && P->kind != EFFSC_IP) || P->order != EFFSC_MSB || !P->tail_len) return false;
+    if (r >= num_rounds || (ch.has && !ch.dev)) return false;
+    const size_t L = P->t[0].len;
+    for (int i = 1; i < P->ntab; i++)
+        if (P->t[i].len != L) return false;
+    if (!is_pow2(L)) return false;
+    const int fw = P->field == EFFSC_FP3 ? 3 : 1;
+    const size_t lim = std::min<size_t>(P->tail_len, (size_t)tail_max_len(pol_of(P), fw, TAIL_SMEM_CAP));
+    if (L > lim) return false;
+    const size_t rounds = num_rounds - r, folds = rounds - (ch.has ? 0 : 1);
+    return folds < 63 && (L >> folds) >= 2;
+}
+
+int do_tail(effsc_prover* P, size_t r, size_t num_rounds, const Chal& ch, const TxIO& tx, bool dry) {
+    const int pol = pol_of(P), fw = P->field == EFFSC_FP3 ? 3 : 1, nt = P->ntab;
+    const size_t L = P->t[0].len, rounds = num_rounds - r, folds = rounds - (ch.has ? 0 : 1);
+    TailArgs ta;
+    memset(&ta, 0, sizeof ta);
+    ta.L = L;
+    ta.nrounds = (u32)rounds;
+    ta.first_fold = ch.has ? 1 : 0;
+    ta.chal_in = ch.dev;
+    ta.tx = tx.tx;
+    ta.hook = tx.hook;
+    ta.hook_len = tx.hook_len;
+    ta.proof_wire = tx.proof_wire;
+    ta.proof_chal = tx.proof_chal;
+    const bool out_ext = fw == 3;
+    int bi[3] = {0, 0, 0};
+    uint64_t bytes = 0;
+    for (int i = 0; i < nt; i++) {
+        Table& T = P->t[i];
+        for (int c = 0; c < 3; c++) ta.in[i][c] = T.bufs[T.cur].p[c];
+        if (T.ext) ta.in_ext |= 1u << i;
+        bytes += L * wbytes(T.ext);
+        if (folds) {
+            TRY(out_buffer(P, T, out_ext, L >> folds, true, &bi[i]));
+            for (int c = 0; c < 3; c++) ta.out[i][c] = T.bufs[bi[i]].p[c];
+            bytes += (L >> folds) * wbytes(out_ext);
+        }
+    }
+    if (!dry) TRY(timed_launch(P->ctx->stream, "tail", bytes, [&] { return launch_tail(pol, fw, nullptr, &ta, 1, L, P->ctx->stream); }));
+    if (folds)
+        for (int i = 0; i < nt; i++) {
+            Table& T = P->t[i];
+            T.cur = bi[i];
+            T.len = L >> folds;
+            T.ext = out_ext;
+        }
     return EFFSC_OK;
 }
 
@@ -1104,6 +1165,13 @@ int effsc_prover_read_table(effsc_prover* P, int table, uint64_t* out) {
     return EFFSC_OK;
 }
 
+int effsc_prover_set_tail(effsc_prover* P, size_t max_len) {
+    if (!P) return fail(EFFSC_INVALID_ARG, "prover is NULL");
+    if (max_len != P->tail_len && P->gexec) { cudaGraphExecDestroy(P->gexec); P->gexec = nullptr; }
+    P->tail_len = max_len;
+    return EFFSC_OK;
+}
+
 int effsc_prover_reset(effsc_prover* P) {
     if (!P) return fail(EFFSC_INVALID_ARG, "prover is NULL");
     for (int i = 0; i < 3; i++) {
@@ -1160,6 +1228,10 @@ int effsc_prove(effsc_prover* P, size_t num_rounds, effsc_transcript* T, const u
             tx.proof_wire = P->d_wire + (size_t)r * 3 * d;
             tx.proof_chal = P->d_chals + 3 * r;
             tx.chal_next = nullptr;
+            if (tail_ok(P, r, num_rounds, ch)) {
+                TRY(do_tail(P, r, num_rounds, ch, tx, dry));
+                break;
+            }
             TRY(do_round(P, ch, tx, dry));
         }
         if (num_rounds) {

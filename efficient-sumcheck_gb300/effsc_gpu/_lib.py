@@ -58,12 +58,14 @@ SIGNATURES = {
     "effsc_build_eq_table": (ci, [vp, ci, ci, u64p, sz, u64p]),
     "effsc_gen_uniform": (ci, [vp, ctypes.c_uint64, ctypes.c_uint64, u64p, u64p]),
     "effsc_table_seed": (ctypes.c_uint64, [ctypes.c_uint64, ctypes.c_uint64]),
+    "effsc_prover_set_tail": (ci, [vp, sz]),
     "effsc_batch_create": (ci, [vp, ci, ci, sz, ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(u64p), u64p,
                                 ctypes.POINTER(vp)]),
     "effsc_batch_destroy": (ci, [vp]),
     "effsc_batch_prove": (ci, [vp, ctypes.POINTER(vp), ci, u64p, u64p, u64p]),
     "effsc_batch_set_quads_per_thread": (ci, [vp, ci]),
-    "effsc_batch_tune": (ci, [vp, ctypes.POINTER(vp), ctypes.c_char_p, ctypes.POINTER(ci)]),
+    "effsc_batch_set_tail": (ci, [vp, ctypes.c_uint64]),
+    "effsc_batch_tune": (ci, [vp, ctypes.POINTER(vp), ctypes.c_char_p, ctypes.POINTER(ci), u64p]),
     "effsc_batch_device_table": (ci, [vp, sz, ci, ctypes.POINTER(u64p)]),
     "effsc_ip_round_noalloc": (ci, [vp, vp, vp, vp, sz, u64p, vp, ci, vp]),
     "effsc_device_alloc": (ci, [vp, sz, ctypes.POINTER(vp)]),

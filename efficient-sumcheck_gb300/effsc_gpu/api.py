@@ -244,6 +244,11 @@ class _Prover:
     def reset(self):
         check(load().effsc_prover_reset(self.h))
 
+    def set_tail(self, max_len):
+        """prove(): tables of at most max_len entries finish in the one-block
+        tail kernel (None: as large as shared memory allows, 0: never)."""
+        check(load().effsc_prover_set_tail(self.h, (1 << 64) - 1 if max_len is None else int(max_len)))
+
     def prove(self, num_rounds, transcript, hook=b"", use_graph=True):
         """Whole protocol on the device (effsc_prove) with the device transcript."""
         d = self.degree()
@@ -495,12 +500,19 @@ class Batch:
     def set_quads_per_thread(self, q):
         check(load().effsc_batch_set_quads_per_thread(self.h, int(q)))
 
+    def set_tail(self, max_len):
+        """Tables of at most max_len entries finish in the one-block tail
+        kernel (None: as large as shared memory allows, 0: never)."""
+        check(load().effsc_batch_set_tail(self.h, (1 << 64) - 1 if max_len is None else int(max_len)))
+
     def tune(self, transcripts, cache_path=None):
-        """Autotune quadruples per thread; returns the chosen value."""
+        """Autotune quadruples per thread and the tail switch; returns
+        (quads_per_thread, tail_len)."""
         c = ctypes.c_int()
+        t = ctypes.c_uint64()
         path = cache_path.encode() if cache_path else None
-        check(load().effsc_batch_tune(self.h, self._tx_array(transcripts), path, ctypes.byref(c)))
-        return c.value
+        check(load().effsc_batch_tune(self.h, self._tx_array(transcripts), path, ctypes.byref(c), ctypes.byref(t)))
+        return c.value, t.value
 
     def device_table(self, inst, t):
         out = u64p()

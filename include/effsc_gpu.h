@@ -130,6 +130,13 @@ int effsc_prover_final_value(effsc_prover* p, uint64_t* out);
  * Writes table_len() elements of `field` words each (AoS). */
 int effsc_prover_table_len(const effsc_prover* p, int table, size_t* out_len);
 int effsc_prover_read_table(effsc_prover* p, int table, uint64_t* out);
+/* effsc_prove only (no reference counterpart; a tuning knob): once an MSB
+ * Multilinear / InnerProduct prover's power-of-two tables are at most
+ * max_len long, the remaining rounds run in one thread block with the tables
+ * in shared memory (one launch instead of one per round).  Default SIZE_MAX:
+ * as long as shared memory allows; 0 disables.  Proofs are identical. */
+int effsc_prover_set_tail(effsc_prover* p, size_t max_len);
+
 /* Restore the state right after construction (the input tables are never
  * written by the rounds), so a proof can be recomputed without re-upload. */
 int effsc_prover_reset(effsc_prover* p);
@@ -230,9 +237,16 @@ int effsc_batch_prove(effsc_batch* b, const effsc_transcript* const* transcripts
                       uint64_t* round_polys, uint64_t* challenges, uint64_t* final_values);
 /* Work granularity: quadruples per thread of a round's blocks (1..64). */
 int effsc_batch_set_quads_per_thread(effsc_batch* b, int quads_per_thread);
-/* Autotuner: times quads-per-thread 1, 2, 4, 8 on this batch, keeps the
- * fastest and appends the measurement to cache_path (JSON lines) if given. */
-int effsc_batch_tune(effsc_batch* b, const effsc_transcript* const* transcripts, const char* cache_path, int* chosen);
+/* Tail switch: once an instance's tables are at most max_len long, its
+ * remaining rounds run in one thread block (shared memory) of a single tail
+ * launch for the whole batch.  Default ~0: as long as shared memory allows;
+ * 0 disables. */
+int effsc_batch_set_tail(effsc_batch* b, uint64_t max_len);
+/* Autotuner: times quads-per-thread {1, 2, 4, 8} x tail switch {off, 2^6,
+ * 2^8, 2^10, largest} on this batch, keeps the fastest and appends the
+ * measurements to cache_path (JSON lines) if given. */
+int effsc_batch_tune(effsc_batch* b, const effsc_transcript* const* transcripts, const char* cache_path,
+                     int* quads_per_thread, uint64_t* tail_len);
 /* Device address of instance inst's input table (2^num_vars canonical words). */
 int effsc_batch_device_table(effsc_batch* b, size_t inst, int table, const uint64_t** out);
 

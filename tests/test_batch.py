@@ -107,21 +107,42 @@ def test_batch_tune_persists(E, tmp_path):
     tabs = make_tabs(rng, "ip", nv)
     b = E.Batch(E.IP, nv, tables=tabs, field=3)
     path = str(tmp_path / "tune.jsonl")
-    q = b.tune(transcripts(E, 3, len(nv)), cache_path=path)
+    q, tail = b.tune(transcripts(E, 3, len(nv)), cache_path=path)
     assert q in (1, 2, 4, 8)
+    assert tail in (0, 1 << 6, 1 << 8, 1 << 10, (1 << 64) - 1)
     rec = json.loads(open(path).read().strip().splitlines()[-1])
-    assert rec["quads_per_thread"] == q and rec["instances"] == len(nv)
+    assert rec["quads_per_thread"] == q and rec["instances"] == len(nv) and len(rec["ms"]) == 20
     check_against_oracle("ip", 3, nv, tabs, b.prove(transcripts(E, 3, len(nv))))
+
+
+@pytest.mark.parametrize("kind", ["ip", "ml"])
+@pytest.mark.parametrize("field", [1, 3])
+@pytest.mark.parametrize("tail", [0, 4, 8, 64, 1 << 10, None])
+def test_batch_tail_switch(E, kind, field, tail):
+    """Every tail switch point gives the same proofs; instances smaller than
+    the switch run entirely in the tail kernel."""
+    rng = random.Random(31 + field + (tail or 0) % 97)
+    nv = [1, 2, 3, 4, 6, 9, 12, 14, 5, 2, 11]
+    tabs = make_tabs(rng, kind, nv)
+    b = E.Batch(E.IP if kind == "ip" else E.ML, nv, tables=tabs, field=field)
+    b.set_tail(tail)
+    check_against_oracle(kind, field, nv, tabs, b.prove(transcripts(E, field, len(nv))))
 
 
 def test_batch_launches_one_kernel_per_round(E):
     nv = [3, 6, 2, 6]
     rng = random.Random(5)
     b = E.Batch(E.ML, nv, tables=make_tabs(rng, "ml", nv), field=3)
+    b.set_tail(0)
     b.prove_raw(transcripts(E, 3, len(nv)))
     E.launch_count_reset()
     b.prove_raw(transcripts(E, 3, len(nv)))
     assert E.launch_count() == max(nv) + 1     # one per round + one final fold
+    b.set_tail(8)                              # rounds on tables of <= 8 entries: one tail launch
+    b.prove_raw(transcripts(E, 3, len(nv)))
+    E.launch_count_reset()
+    b.prove_raw(transcripts(E, 3, len(nv)))
+    assert E.launch_count() == (6 - 3 + 1) + 1 + 1
 
 
 def test_batch_rejects_bad_input(E):

@@ -252,5 +252,12 @@ def test_kernels_launch(E):
     E.launch_count_reset()
     rng = random.Random(9)
     a = rand_table(rng, 1 << 12, False)
-    E.InnerProductProver(a, a).prove(12, E.Transcript.keccak(3, b"k"), use_graph=False)
+    p = E.InnerProductProver(a, a)
+    p.set_tail(0)        # one kernel per round
+    p.prove(12, E.Transcript.keccak(3, b"k"), use_graph=False)
     assert E.launch_count() >= 12
+    E.launch_count_reset()
+    p.reset()
+    p.set_tail(None)     # all 12 rounds in the one-block tail kernel, then the final folds
+    p.prove(12, E.Transcript.keccak(3, b"k"), use_graph=False)
+    assert 1 <= E.launch_count() <= 3
