@@ -140,30 +140,76 @@ __device__ __forceinline__ void tx_squeeze(WarpTx& w, int lane, u32 len, Put put
     }
 }
 
+// Word-aligned forms of absorb / squeeze (w.pos % 8 == 0): the same bytes in
+// the same order, one 64-bit word per lane instead of one byte per step.
+template <class GetW>
+__device__ __forceinline__ void tx_absorb_words(WarpTx& w, int lane, u32 nwords, GetW getw) {
+    if (w.squeezing) { w.pos = 0; w.squeezing = 0; }
+    u32 done = 0;
+    while (done < nwords) {
+        if (w.pos == TX_RATE) { keccak_f_warp(w.a, lane); w.pos = 0; }
+        const u32 p8 = w.pos >> 3;
+        const u32 chunk = min(nwords - done, (u32)(TX_RATE / 8) - p8);
+        if ((u32)lane >= p8 && (u32)lane < p8 + chunk) w.a ^= getw(done + (u32)lane - p8);
+        w.pos += 8 * chunk;
+        done += chunk;
+    }
+}
+template <class PutW>
+__device__ __forceinline__ void tx_squeeze_words(WarpTx& w, int lane, u32 nwords, PutW putw) {
+    if (!w.squeezing) {
+        if (w.pos == TX_RATE) { keccak_f_warp(w.a, lane); w.pos = 0; }
+        if (lane == (int)(w.pos >> 3)) w.a ^= (u64)0x06 << (8 * (w.pos & 7));
+        if (lane == (TX_RATE - 1) / 8) w.a ^= (u64)0x80 << (8 * ((TX_RATE - 1) & 7));
+        keccak_f_warp(w.a, lane);
+        w.pos = 0;
+        w.squeezing = 1;
+    }
+    u32 done = 0;
+    while (done < nwords) {
+        if (w.pos == TX_RATE) { keccak_f_warp(w.a, lane); w.pos = 0; }
+        const u32 p8 = w.pos >> 3;
+        const u32 chunk = min(nwords - done, (u32)(TX_RATE / 8) - p8);
+        if ((u32)lane >= p8 && (u32)lane < p8 + chunk) putw(done + (u32)lane - p8, w.a);
+        w.pos += 8 * chunk;
+        done += chunk;
+    }
+}
+
 // Absorb `n` field elements (deg components each) from shared memory `v`
 // (layout: element e component c at v[3e + c]).
 __device__ __forceinline__ void tx_send_elems(WarpTx& w, int lane, const u64* v, int n) {
     const u32 deg = w.deg;
+    if ((w.pos & 7) == 0 || w.squeezing) {
+        tx_absorb_words(w, lane, (u32)n * deg, [&](u32 word) -> u64 {
+            const u32 e = deg == 3 ? word / 3 : word, c = deg == 3 ? word % 3 : 0;
+            return v[3 * e + c];
+        });
+        return;
+    }
     tx_absorb(w, lane, (u32)n * deg * 8, [&](u32 k) -> uint8_t {
         u32 word = k >> 3, e = word / deg, c = word % deg;
         return (uint8_t)(v[3 * e + c] >> (8 * (k & 7)));
     });
 }
 // Squeeze one challenge into shared memory `out` (3 words; unused set to 0).
-// `scratch` is 48 bytes of shared memory.
+// `scratch` is 48 bytes of 8-byte aligned shared memory.
 __device__ __forceinline__ void tx_challenge(WarpTx& w, int lane, u64* out, uint8_t* scratch) {
     const u32 deg = w.deg;
-    tx_squeeze(w, lane, 16 * deg, [&](u32 k, uint8_t b) { scratch[k] = b; });
+    // the first squeeze after absorbing pads and restarts at byte 0, so the
+    // word form applies whenever the rate position is a multiple of 8
+    if (!w.squeezing || (w.pos & 7) == 0) {
+        u64* sw = (u64*)scratch;
+        tx_squeeze_words(w, lane, 2 * deg, [&](u32 k, u64 v) { sw[k] = v; });
+    } else {
+        tx_squeeze(w, lane, 16 * deg, [&](u32 k, uint8_t b) { scratch[k] = b; });
+    }
     __syncwarp();
     if (lane < 3) {
         u64 r = 0;
         if ((u32)lane < deg) {
-            u64 lo = 0, hi = 0;
-            for (int k = 0; k < 8; k++) {
-                lo |= (u64)scratch[16 * lane + k] << (8 * k);
-                hi |= (u64)scratch[16 * lane + 8 + k] << (8 * k);
-            }
-            r = gl_reduce128(lo, hi);
+            const u64* sw = (const u64*)scratch;   // little-endian bytes
+            r = gl_reduce128(sw[2 * lane], sw[2 * lane + 1]);
         }
         out[lane] = r;
     }

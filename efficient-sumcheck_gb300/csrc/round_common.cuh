@@ -187,7 +187,7 @@ static __device__ __noinline__ void finalize_warp(int pol, const u64* raw, const
     __shared__ u64 s_wire[9];
     __shared__ u64 s_aux[6];
     __shared__ u64 s_chal[3];
-    __shared__ uint8_t s_scratch[64];
+    __shared__ __align__(8) uint8_t s_scratch[64];
     const int lane = threadIdx.x & 31;
     int nwire = pol_nwire_dev(pol);
     if (lane == 0) {
@@ -235,7 +235,12 @@ static __device__ __noinline__ void finalize_warp(int pol, const u64* raw, const
         tx_send_elems(w, lane, s_wire, nwire);
         if (a.tx.hook_len) {
             const uint8_t* hk = a.tx.hook;
-            tx_absorb(w, lane, a.tx.hook_len, [&](u32 k) -> uint8_t { return hk[k]; });
+            if (((w.pos & 7) == 0 || w.squeezing) && (a.tx.hook_len & 7) == 0 && ((uintptr_t)hk & 7) == 0) {
+                const u64* hw = (const u64*)hk;
+                tx_absorb_words(w, lane, a.tx.hook_len >> 3, [&](u32 k) -> u64 { return hw[k]; });
+            } else {
+                tx_absorb(w, lane, a.tx.hook_len, [&](u32 k) -> uint8_t { return hk[k]; });
+            }
         }
         tx_challenge(w, lane, s_chal, s_scratch);
         tx_store(T, w, lane);

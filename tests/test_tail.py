@@ -86,3 +86,19 @@ def test_tail_cuts_launches(E):
     E.launch_count_reset()
     p.prove(12, E.Transcript.keccak(3, b"x"), use_graph=False)
     assert E.launch_count() < per_round
+
+
+@pytest.mark.parametrize("hook_len", [1, 7, 8, 13, 40, 136, 137, 300])
+@pytest.mark.parametrize("tail", [0, None])
+def test_hook_lengths(E, hook_len, tail):
+    """Hook bytes of every alignment and across the 136-byte rate: the word
+    and byte forms of the device transcript agree with the oracle."""
+    rng = random.Random(hook_len)
+    tabs, p = make(E, "ip", 3, 8, rng)
+    p.set_tail(tail)
+    hook = bytes((7 * i + hook_len) & 0xFF for i in range(hook_len))
+    pf = p.prove(8, E.Transcript.keccak(3, b"h"), hook=hook)
+    rp, ch, fv = O.sumcheck(O.Prover(O.IP, O.MSB, 3, tabs), 8, O.Transcript(3, label=b"h"), hook=hook)
+    assert np.array_equal(pf.round_polys, rp)
+    assert np.array_equal(pf.challenges, ch)
+    assert np.array_equal(pf.final_value, fv)
