@@ -9,8 +9,8 @@
 // reference src/inner_product_sumcheck.rs:143-176 and
 // src/multilinear_sumcheck.rs:132-178), accumulates the round polynomial of
 // the folded tables on the fly (the same quadruple scheme as the fused
-// kernels), reduces across the block, and runs the transcript step
-// (finalize_warp: wire values, hook bytes, challenge squeeze).  After the
+// kernels), reduces across the block, and runs the transcript step (wire
+// values, hook bytes, challenge squeeze) in warp 0.  After the
 // last round the folded tables go back to global memory so that finalize /
 // final_value and the post-state accessors see exactly what the per-round
 // path would leave.  A batch launches one block per instance.
@@ -32,47 +32,51 @@ __device__ __forceinline__ void sm_st(u64* sm, u64 L, int t, u64 i, const F3& v)
     if (FW == 3) { sm[(u64)(t * 3 + 1) * L + i] = v.c1; sm[(u64)(t * 3 + 2) * L + i] = v.c2; }
 }
 
+constexpr int TAIL_TPB = 512;
+constexpr int TAIL_NW = TAIL_TPB / 32;
+
 // Shared-memory layout: table t, component c, element i at sm[(t*FW + c)*L0 + i]
 // with L0 the starting length (rows keep their stride as the tables shrink).
+// Warp 0 keeps the transcript state in registers for the whole tail and the
+// challenge stays in shared memory, so a round costs one block reduction and
+// one transcript step.
 template <int POL, int FW>
 __device__ void tail_body(const TailArgs& a) {
     extern __shared__ __align__(16) u64 sm[];
-    __shared__ RoundArgs ra;
     constexpr int NT = Policy<POL, 0>::NT;
     constexpr u32 MF = FW == 3 ? (1u << NT) - 1 : 0;
     constexpr bool E = FW == 3;
     using P = Policy<POL, MF>;
+    constexpr int NW3 = 3 * P::NRAW;
+    // ML and IP send their raw sums as the wire values: [s0] / [q0, qinf]
+    constexpr int NWIRE = POL == POL_ML ? 1 : 2;
+    __shared__ u64 s_red[TAIL_NW][NW3];
+    __shared__ u64 s_tot[NW3];
+    __shared__ u64 s_chal[3];
+    __shared__ __align__(8) uint8_t s_scr[64];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const u64 L0 = a.L;
-    // load (base components of an Fp3-width table read as zero)
     for (int t = 0; t < NT; t++)
         for (int c = 0; c < FW; c++) {
             const u64* src = (c == 0 || ((a.in_ext >> t) & 1u)) ? a.in[t][c] : nullptr;
             u64* dst = sm + (u64)(t * FW + c) * L0;
-            for (u64 i = threadIdx.x; i < L0; i += TPB) dst[i] = src ? src[i] : 0;
+            for (u64 i = threadIdx.x; i < L0; i += TAIL_TPB) dst[i] = src ? src[i] : 0;
         }
-    if (threadIdx.x == 0) {
-        memset(&ra, 0, sizeof ra);
-        ra.tx.tx = a.tx;
-        ra.tx.hook = a.hook;
-        ra.tx.hook_len = a.hook_len;
-    }
+    if (threadIdx.x < 3) s_chal[threadIdx.x] = a.first_fold ? a.chal_in[threadIdx.x] : 0;
+    DevTranscript* T = (DevTranscript*)a.tx;
+    WarpTx w;
+    if (warp == 0) w = tx_load(T, lane);
     __syncthreads();
-    const int nwire = pol_nwire_dev(POL);
     u64 len = L0;
     bool fold = a.first_fold != 0;
-    F3 ch = fold ? f3_make(a.chal_in[0], a.chal_in[1], a.chal_in[2]) : f3_make(0, 0, 0);
     for (u32 k = 0; k < a.nrounds; k++) {
-        if (threadIdx.x == 0) {
-            ra.tx.proof_wire = a.proof_wire + (u64)k * 3 * nwire;
-            ra.tx.proof_chal = a.proof_chal + (u64)k * 3;
-        }
         P acc;
         acc.init();
         F3 lo[NT], hi[NT];
         if (fold) {
-            const Mul3 m = mul3_prepare<E>(ch);
+            const Mul3 m = mul3_prepare<E>(f3_make(s_chal[0], s_chal[1], s_chal[2]));
             const u64 Q = len >> 2;
-            for (u64 q = threadIdx.x; q < Q; q += TPB) {
+            for (u64 q = threadIdx.x; q < Q; q += TAIL_TPB) {
 #pragma unroll
                 for (int t = 0; t < NT; t++) {
                     F3 x0 = sm_ld<FW>(sm, L0, t, q), x1 = sm_ld<FW>(sm, L0, t, q + Q);
@@ -85,45 +89,79 @@ __device__ void tail_body(const TailArgs& a) {
                 acc.pair(lo, hi);
             }
             len >>= 1;
+        } else if (len == 1) {
+            if (threadIdx.x == 0) {
+#pragma unroll
+                for (int t = 0; t < NT; t++) lo[t] = sm_ld<FW>(sm, L0, t, 0);
+                acc.single(lo);
+            }
         } else {
             const u64 half = len >> 1;
-            if (len == 1) {
-                if (threadIdx.x == 0) {
+            for (u64 j = threadIdx.x; j < half; j += TAIL_TPB) {
 #pragma unroll
-                    for (int t = 0; t < NT; t++) lo[t] = sm_ld<FW>(sm, L0, t, 0);
-                    acc.single(lo);
-                }
-            } else {
-                for (u64 j = threadIdx.x; j < half; j += TPB) {
-#pragma unroll
-                    for (int t = 0; t < NT; t++) { lo[t] = sm_ld<FW>(sm, L0, t, j); hi[t] = sm_ld<FW>(sm, L0, t, j + half); }
-                    acc.pair(lo, hi);
-                }
+                for (int t = 0; t < NT; t++) { lo[t] = sm_ld<FW>(sm, L0, t, j); hi[t] = sm_ld<FW>(sm, L0, t, j + half); }
+                acc.pair(lo, hi);
             }
         }
         F3 raw[P::NRAW];
         acc.result(raw);
-        reduce_and_finalize_seg<P::NRAW>(raw, ra, POL, 1, 0);
+        // block reduction
+#pragma unroll
+        for (int off = 16; off; off >>= 1) {
+#pragma unroll
+            for (int i = 0; i < P::NRAW; i++) {
+                raw[i].c0 = gl_add(raw[i].c0, __shfl_down_sync(0xffffffffu, raw[i].c0, off));
+                raw[i].c1 = gl_add(raw[i].c1, __shfl_down_sync(0xffffffffu, raw[i].c1, off));
+                raw[i].c2 = gl_add(raw[i].c2, __shfl_down_sync(0xffffffffu, raw[i].c2, off));
+            }
+        }
+        if (lane == 0) {
+#pragma unroll
+            for (int i = 0; i < P::NRAW; i++) { s_red[warp][3 * i] = raw[i].c0; s_red[warp][3 * i + 1] = raw[i].c1; s_red[warp][3 * i + 2] = raw[i].c2; }
+        }
         __syncthreads();
-        const u64* c = a.proof_chal + (u64)k * 3;
-        ch = f3_make(c[0], c[1], c[2]);
+        if (warp == 0) {
+            if (lane < NW3) {
+                u64 v = 0;
+#pragma unroll
+                for (int q = 0; q < TAIL_NW; q++) v = gl_add(v, s_red[q][lane]);
+                s_tot[lane] = v;
+            }
+            __syncwarp();
+            // transcript step (src/runner.rs:39-55)
+            tx_send_elems(w, lane, s_tot, NWIRE);
+            if (a.hook_len) {
+                const uint8_t* hk = a.hook;
+                if (((w.pos & 7) == 0 || w.squeezing) && (a.hook_len & 7) == 0 && ((uintptr_t)hk & 7) == 0) {
+                    const u64* hw = (const u64*)hk;
+                    tx_absorb_words(w, lane, a.hook_len >> 3, [&](u32 i) -> u64 { return hw[i]; });
+                } else {
+                    tx_absorb(w, lane, a.hook_len, [&](u32 i) -> uint8_t { return hk[i]; });
+                }
+            }
+            tx_challenge(w, lane, s_chal, s_scr);
+            if (lane < 3 * NWIRE) a.proof_wire[(u64)k * 3 * NWIRE + lane] = s_tot[lane];
+            if (lane < 3) a.proof_chal[(u64)k * 3 + lane] = s_chal[lane];
+        }
+        __syncthreads();
         fold = true;
     }
+    if (warp == 0) tx_store(T, w, lane);
     // write back the tables after the last fold
     if (a.out[0][0]) {
         for (int t = 0; t < NT; t++)
             for (int c = 0; c < FW; c++) {
                 const u64* src = sm + (u64)(t * FW + c) * L0;
                 u64* dst = a.out[t][c];
-                for (u64 i = threadIdx.x; i < len; i += TPB) dst[i] = src[i];
+                for (u64 i = threadIdx.x; i < len; i += TAIL_TPB) dst[i] = src[i];
             }
     }
 }
 
 template <int POL, int FW>
-__global__ void __launch_bounds__(TPB) k_tail_one(TailArgs a) { tail_body<POL, FW>(a); }
+__global__ void __launch_bounds__(TAIL_TPB, 1) k_tail_one(TailArgs a) { tail_body<POL, FW>(a); }
 template <int POL, int FW>
-__global__ void __launch_bounds__(TPB) k_tail_many(const TailArgs* args) { tail_body<POL, FW>(args[blockIdx.x]); }
+__global__ void __launch_bounds__(TAIL_TPB, 1) k_tail_many(const TailArgs* args) { tail_body<POL, FW>(args[blockIdx.x]); }
 
 u64 tail_max_len(int pol, int fw, u64 smem_cap) {
     const u64 per = (u64)pol_ntables(pol) * fw * sizeof(u64);
@@ -138,10 +176,10 @@ static bool tail_inst(const TailArgs* dev_args, const TailArgs* one, u32 n, u64 
     if (bytes > TAIL_SMEM_CAP) return false;
     if (one) {
         cudaFuncSetAttribute(k_tail_one<POL, FW>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TAIL_SMEM_CAP);
-        k_tail_one<POL, FW><<<1, TPB, bytes, s>>>(*one);
+        k_tail_one<POL, FW><<<1, TAIL_TPB, bytes, s>>>(*one);
     } else {
         cudaFuncSetAttribute(k_tail_many<POL, FW>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TAIL_SMEM_CAP);
-        k_tail_many<POL, FW><<<n, TPB, bytes, s>>>(dev_args);
+        k_tail_many<POL, FW><<<n, TAIL_TPB, bytes, s>>>(dev_args);
     }
     return true;
 }
