@@ -92,6 +92,18 @@ constexpr u64 TAIL_SMEM_CAP = 200 * 1024;
 // One block per TailArgs; `smem_len` = largest L among them.
 bool launch_tail(int pol, int fw, const TailArgs* dev_args, const TailArgs* one, u32 n, u64 smem_len, cudaStream_t s);
 
+// Serving steps: one entry per request in the step, sorted by first_block;
+// `code` = SERVE_IP (else ML) | SERVE_FP3 (else Fp) | phase << SERVE_PHASE_SHIFT.
+struct ServeSeg {
+    u32 first_block;
+    u32 nblocks;
+    u32 code;
+    u32 reserved;
+};
+constexpr u32 SERVE_IP = 1, SERVE_FP3 = 2, SERVE_PHASE_SHIFT = 2;
+enum ServePhase { SERVE_EVAL = 0, SERVE_FOLD_BASE = 1, SERVE_FOLD_EXT = 2, SERVE_FINAL_BASE = 3, SERVE_FINAL_EXT = 4 };
+void launch_serve_step(const ServeSeg* segs, u32 nsegs, const RoundArgs* args, u32 grid, cudaStream_t s);
+
 int pol_ntables(int pol);
 int pol_nraw(int pol);
 int pol_nwire(int pol);

@@ -7,7 +7,7 @@ from ._lib import EffscError, ReferencePanic, LIB_PATH, load  # noqa: F401
 from .api import (  # noqa: F401
     CANONICAL, COEF, EQF, FP, FP3, IP, LSB, ML, MONTGOMERY, MSB, T_KECCAK, T_TEST,
     Batch, CoefficientProver, CoefficientProverLSB, Context, EqFactoredProver, InnerProductProver,
-    InnerProductProverLSB, MultilinearProver, MultilinearProverLSB, ProductSumcheck, Sumcheck,
+    InnerProductProverLSB, MultilinearProver, MultilinearProverLSB, ProductSumcheck, Server, Sumcheck,
     SumcheckProof, Transcript, build_eq_table, fold, gen_uniform, inner_product_sumcheck,
     inner_product_sumcheck_partial, launch_count, launch_count_reset, multilinear_sumcheck,
     multilinear_sumcheck_partial, noop_hook, sumcheck, sumcheck_verify, table_seed,

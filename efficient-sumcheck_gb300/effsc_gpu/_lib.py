@@ -67,6 +67,16 @@ SIGNATURES = {
     "effsc_batch_set_tail": (ci, [vp, ctypes.c_uint64]),
     "effsc_batch_tune": (ci, [vp, ctypes.POINTER(vp), ctypes.c_char_p, ctypes.POINTER(ci), u64p]),
     "effsc_batch_device_table": (ci, [vp, sz, ci, ctypes.POINTER(u64p)]),
+    "effsc_server_create": (ci, [vp, ctypes.c_uint64, ctypes.c_uint32, ctypes.POINTER(vp)]),
+    "effsc_server_destroy": (ci, [vp]),
+    "effsc_server_submit": (ci, [vp, ci, ci, ctypes.c_uint32, ctypes.POINTER(u64p), u64p, vp, u64p]),
+    "effsc_server_progress": (ci, [vp, ci, ctypes.POINTER(ctypes.c_uint32)]),
+    "effsc_server_take": (ci, [vp, u64p, ctypes.POINTER(ctypes.c_uint32), u64p, u64p, u64p,
+                               ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]),
+    "effsc_server_run_trace": (ci, [vp, sz, ctypes.POINTER(ci), ci, ctypes.POINTER(ctypes.c_uint32), u64p,
+                                    ctypes.POINTER(vp), ctypes.POINTER(ctypes.c_double),
+                                    ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double), u64p, u64p,
+                                    u64p]),
     "effsc_ip_round_noalloc": (ci, [vp, vp, vp, vp, sz, u64p, vp, ci, vp]),
     "effsc_device_alloc": (ci, [vp, sz, ctypes.POINTER(vp)]),
     "effsc_device_free": (ci, [vp, vp]),

@@ -520,6 +520,126 @@ class Batch:
         return ctypes.cast(out, ctypes.c_void_p).value
 
 
+class Server:
+    """A request loop with continuous batching (effsc_server_*): MSB
+    InnerProduct (kind=IP) / Multilinear (kind=ML) proofs of any size, admitted
+    FIFO while at most ``max_active`` are in flight and their device memory
+    fits in ``hbm_budget`` bytes; every step is one kernel in which each
+    admitted request advances one round.  Each proof equals the one
+    runner::sumcheck (src/runner.rs:29-69) gives for that request alone."""
+
+    def __init__(self, hbm_budget, max_active=64, ctx=None):
+        self.ctx = ctx or Context.default()
+        h = vp()
+        check(load().effsc_server_create(self.ctx.h, int(hbm_budget), int(max_active), ctypes.byref(h)))
+        self.h = h
+        self._meta = {}
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib._lib is not None:
+            _lib._lib.effsc_server_destroy(self.h)
+            self.h = None
+
+    def submit(self, kind, num_vars, transcript, tables=None, seeds=None, field=FP3):
+        """Queue one request; returns its id.  ``tables``: host tables (kept
+        alive by this object until the proof is taken) or ``seeds``."""
+        ntab = 2 if kind == IP else 1
+        tp = sp = None
+        keep = []
+        if tables is not None:
+            arrs = [np.ascontiguousarray(np.asarray(t, dtype=np.uint64).reshape(-1)) for t in tables]
+            if len(arrs) != ntab or any(a.size != 1 << num_vars for a in arrs):
+                raise ValueError("expected %d tables of 2^%d words" % (ntab, num_vars))
+            keep = arrs
+            tp = (u64p * ntab)(*[_p(a) for a in arrs])
+        else:
+            sd = np.ascontiguousarray(np.asarray(seeds, dtype=np.uint64).reshape(-1))
+            if sd.size < ntab:
+                raise ValueError("need %d seeds" % ntab)
+            keep = [sd]
+            sp = _p(sd)
+        rid = ctypes.c_uint64()
+        check(load().effsc_server_submit(self.h, kind, field, int(num_vars), tp, sp, transcript.h, ctypes.byref(rid)))
+        self._meta[rid.value] = (kind, field, int(num_vars), keep)
+        return rid.value
+
+    def progress(self, wait=False):
+        """Admit, launch one step, collect finished proofs; returns the number
+        of requests not yet taken."""
+        n = ctypes.c_uint32()
+        check(load().effsc_server_progress(self.h, 1 if wait else 0, ctypes.byref(n)))
+        return n.value
+
+    def take(self):
+        """(id, SumcheckProof, queue_s, latency_s) of the oldest finished
+        proof, or None."""
+        rid = ctypes.c_uint64()
+        nv = ctypes.c_uint32()
+        rp = np.zeros((34, 2, 3), dtype=np.uint64)
+        ch = np.zeros((34, 3), dtype=np.uint64)
+        fv = np.zeros(3, dtype=np.uint64)
+        qs = ctypes.c_double()
+        ls = ctypes.c_double()
+        check(load().effsc_server_take(self.h, ctypes.byref(rid), ctypes.byref(nv), _p(rp), _p(ch), _p(fv),
+                                       ctypes.byref(qs), ctypes.byref(ls)))
+        if rid.value == (1 << 64) - 1:
+            return None
+        kind, field, n, _ = self._meta.pop(rid.value)
+        d = 2 if kind == IP else 1
+        rpf = rp.reshape(-1)[:n * d * field].reshape(n, d, field).copy()
+        chf = ch.reshape(-1)[:n * field].reshape(n, field).copy()
+        return rid.value, SumcheckProof(rpf, chf, fv[:field].copy()), qs.value, ls.value
+
+    def drain(self):
+        """Run until every submitted request is finished; {id: (proof, queue_s, latency_s)}."""
+        out = {}
+        while True:
+            pending = self.progress(wait=True)
+            while True:
+                r = self.take()
+                if r is None:
+                    break
+                out[r[0]] = r[1:]
+            if pending == 0 and not self._meta:
+                return out
+
+    def run_trace(self, kinds, num_vars, seeds, transcripts, arrival_s, field=FP3, proofs=True):
+        """Open-loop trace: request i arrives arrival_s[i] seconds after the
+        start.  Returns (latency_s array, makespan_s, proofs or None) with the
+        proofs concatenated as in Batch.prove_raw."""
+        n = len(kinds)
+        k = (ctypes.c_int * n)(*[int(x) for x in kinds])
+        nv = (ctypes.c_uint32 * n)(*[int(x) for x in num_vars])
+        sd = np.ascontiguousarray(np.asarray(seeds, dtype=np.uint64).reshape(-1))
+        tx = (vp * n)(*[t.h for t in transcripts])
+        arr = np.ascontiguousarray(np.asarray(arrival_s, dtype=np.float64))
+        lat = np.zeros(n, dtype=np.float64)
+        mk = ctypes.c_double()
+        dpc = ctypes.POINTER(ctypes.c_double)
+        rows = int(sum(int(x) for x in num_vars))
+        rp = ch = fv = None
+        if proofs:
+            rp = np.zeros(rows * 2 * field, dtype=np.uint64)
+            ch = np.zeros(rows * field, dtype=np.uint64)
+            fv = np.zeros(n * field, dtype=np.uint64)
+        check(load().effsc_server_run_trace(self.h, n, k, field, nv, _p(sd), tx, arr.ctypes.data_as(dpc),
+                                            lat.ctypes.data_as(dpc), ctypes.byref(mk),
+                                            _p(rp) if proofs else None, _p(ch) if proofs else None,
+                                            _p(fv) if proofs else None))
+        out = None
+        if proofs:
+            out = []
+            ro = 0
+            for i in range(n):
+                d = 2 if int(kinds[i]) == IP else 1
+                m = int(num_vars[i])
+                rpi = rp[ro * 2 * field:(ro + m) * 2 * field].reshape(m, 2, field)[:, :d, :]
+                out.append(SumcheckProof(rpi, ch[ro * field:(ro + m) * field].reshape(m, field),
+                                         fv[i * field:(i + 1) * field]))
+                ro += m
+        return lat, mk.value, out
+
+
 def gen_uniform(seed, n, ctx=None):
     """Seeded uniform canonical table (host array)."""
     ctx = ctx or Context.default()

@@ -250,6 +250,46 @@ int effsc_batch_tune(effsc_batch* b, const effsc_transcript* const* transcripts,
 /* Device address of instance inst's input table (2^num_vars canonical words). */
 int effsc_batch_device_table(effsc_batch* b, size_t inst, int table, const uint64_t** out);
 
+/* ---- serving: a request loop with continuous batching ---------------------
+ * No reference counterpart.  Requests (MSB InnerProduct or Multilinear
+ * proofs, all num_vars rounds, the Keccak transcript `t` as it stands at
+ * submission, no hook) queue FIFO.  effsc_server_progress admits queued
+ * requests while fewer than max_active are in flight and their device memory
+ * (tables, Fp3 work buffers, proof and transcript state) fits in
+ * hbm_budget_bytes, then launches one step: a single kernel in which every
+ * admitted request advances one round or finalises.  Finished proofs are
+ * returned by effsc_server_take in completion order.  Each proof is
+ * bit-identical to proving the request alone (runner::sumcheck,
+ * src/runner.rs:29-69).  Host tables (host_tables[k], 2^num_vars canonical
+ * words) must stay valid until the request is admitted; with host_tables NULL
+ * the tables are generated on the device from seeds[k] (effsc_gen_uniform).
+ * Not thread-safe: one host thread drives a server. */
+typedef struct effsc_server effsc_server;
+int effsc_server_create(effsc_ctx* ctx, uint64_t hbm_budget_bytes, uint32_t max_active, effsc_server** out);
+int effsc_server_destroy(effsc_server* s);
+int effsc_server_submit(effsc_server* s, int kind, int field, uint32_t num_vars, const uint64_t* const* host_tables,
+                        const uint64_t* seeds, const effsc_transcript* t, uint64_t* id);
+/* Admit, launch one step, collect finished proofs.  wait != 0: block until at
+ * least one proof is finished if any is in flight.  *pending: requests not
+ * yet taken (queued, active or finishing). */
+int effsc_server_progress(effsc_server* s, int wait, uint32_t* pending);
+/* Oldest finished proof: *id (~0 when none), num_vars rows of round_polys
+ * (degree x field words) and challenges (field words), final_value (field
+ * words); seconds queued and seconds from submission to completion. */
+int effsc_server_take(effsc_server* s, uint64_t* id, uint32_t* num_vars, uint64_t* round_polys, uint64_t* challenges,
+                      uint64_t* final_value, double* queue_s, double* latency_s);
+/* Open-loop driver: request i (kinds[i], num_vars[i], seeds[2i..2i+1],
+ * transcripts[i]) is submitted arrival_s[i] seconds after the start; runs
+ * until every proof is finished.  latency_s[i] = completion - arrival; the
+ * proofs are concatenated in request order: request i's rounds start at row
+ * R_i = num_vars[0] + ... + num_vars[i-1], a round_polys row holds 2
+ * elements (Multilinear rows: [h(0), 0]), a challenges row 1 element; NULL
+ * outputs are skipped. */
+int effsc_server_run_trace(effsc_server* s, size_t n, const int* kinds, int field, const uint32_t* num_vars,
+                           const uint64_t* seeds, const effsc_transcript* const* transcripts, const double* arrival_s,
+                           double* latency_s, double* makespan_s, uint64_t* round_polys, uint64_t* challenges,
+                           uint64_t* final_values);
+
 /* ---- one round without allocation -----------------------------------------
  * No counterpart in the reference.  For callers that must not allocate device
  * memory (a host application whose own pool has reserved the HBM, or work
