@@ -48,6 +48,10 @@ def parse():
     ap.add_argument("--batch-instances", type=int, default=512,
                     help="batching leg: this many IP instances, num_vars uniform on 10..=22 (0 = skip)")
     ap.add_argument("--batch-steps", type=int, default=10)
+    ap.add_argument("--serve-requests", type=int, default=20000,
+                    help="serving leg: this many requests, 70%% IP / 30%% ML, num_vars uniform on 14..=26 (0 = skip)")
+    ap.add_argument("--serve-slots", type=int, default=128)
+    ap.add_argument("--serve-budget-gb", type=float, default=150.0)
     return ap.parse_args()
 
 
@@ -359,6 +363,9 @@ def run_ours(args):
     batch = None
     if args.batch_instances and world == 1:
         batch = run_batch(args, E, L, ctx, stream, rank)
+    serving = None
+    if args.serve_requests and world == 1:
+        serving = run_serving(args, E, ctx)
 
     if rank == 0:
         line = {
@@ -386,6 +393,7 @@ def run_ours(args):
                            for k, v in per.items()},
             "bit_exact_vs_oracle": bit_exact,
             "batching": batch,
+            "serving": serving,
         }
         print(json.dumps(line), flush=True)
     if dist is not None:
@@ -513,6 +521,87 @@ def run_batch(args, E, L, ctx, stream, rank):
         "speedup_proofs_per_s": ms_solo / ms_batch,
         "autotune": tune_rec,
         "bit_exact": {"batched_vs_one_at_a_time": count, "batched_vs_oracle": oracle_checked},
+    }
+
+
+# ---------------------------------------------------------------------------
+# serving: open-loop Poisson stream under an HBM budget
+# ---------------------------------------------------------------------------
+SERVE_SEED = 0x5E7E_2026
+
+
+def serve_workload(count):
+    """70% InnerProduct / 30% Multilinear, num_vars uniform on the integers
+    14..=26 (table size log-uniform), per-request seeds; all seeded."""
+    import random
+    rng = random.Random(SERVE_SEED)
+    kinds, nv = [], []
+    for _ in range(count):
+        kinds.append(1 if rng.random() < 0.7 else 0)
+        nv.append(rng.randint(14, 26))
+    return kinds, nv
+
+
+def serve_label(i):
+    return ("effsc-gpu/serve/%d" % i).encode()
+
+
+def run_serving(args, E, ctx):
+    import numpy as np
+    count = args.serve_requests
+    kinds, nv = serve_workload(count)
+    seeds = np.array([[E.table_seed(SERVE_SEED + i, t) for t in range(2)] for i in range(count)], dtype=np.uint64)
+    srv = E.Server(hbm_budget=int(args.serve_budget_gb * 1e9), max_active=args.serve_slots, ctx=ctx)
+
+    def trace(arrivals, sub=None, proofs=False):
+        idx = range(count) if sub is None else sub
+        txs = [E.Transcript.keccak(E.FP3, serve_label(i)) for i in idx]
+        return srv.run_trace([kinds[i] for i in idx], [nv[i] for i in idx], seeds[list(idx)], txs,
+                             arrivals, proofs=proofs)
+
+    # warm-up: fills the server's memory pool up to the budget's working set
+    warm = list(range(min(count, 400)))
+    trace(np.zeros(len(warm)), sub=warm)
+    # saturation: every request offered at t = 0
+    lat_sat, mk_sat, proofs_sat = trace(np.zeros(count), proofs=True)
+    sat = count / mk_sat
+    rng = np.random.default_rng(SERVE_SEED)
+    levels = {}
+    proofs_full = None
+    for frac in (0.5, 0.8, 1.0):
+        rate = frac * sat
+        arrivals = np.cumsum(rng.exponential(1.0 / rate, size=count))
+        lat, mk, pr = trace(arrivals, proofs=frac == 1.0)
+        if pr is not None:
+            proofs_full = pr
+        levels["%d%%" % int(frac * 100)] = {
+            "offered_proofs_per_s": rate, "sustained_proofs_per_s": count / mk,
+            "p50_ms": float(np.percentile(lat, 50) * 1e3), "p99_ms": float(np.percentile(lat, 99) * 1e3),
+            "mean_ms": float(lat.mean() * 1e3), "makespan_s": mk}
+    # the same request gives the same proof in both mixes, and alone
+    same_mix = all(np.array_equal(proofs_sat[i].round_polys, proofs_full[i].round_polys)
+                   and np.array_equal(proofs_sat[i].final_value, proofs_full[i].final_value) for i in range(count))
+    assert same_mix, "a serving proof depends on the mix"
+    sample = sorted(set([int(i) for i in np.linspace(0, count - 1, 12)]) | {int(np.argmax(nv)), int(np.argmin(nv))})
+    for i in sample:
+        n = nv[i]
+        tabs = [E.gen_uniform(int(seeds[i][t]), 1 << n, ctx=ctx) for t in range(2 if kinds[i] == 1 else 1)]
+        p = (E.InnerProductProver(tabs[0], tabs[1], ctx=ctx) if kinds[i] == 1 else E.MultilinearProver(tabs[0], ctx=ctx))
+        ref = p.prove(n, E.Transcript.keccak(E.FP3, serve_label(i)))
+        assert np.array_equal(ref.round_polys, proofs_full[i].round_polys) and \
+            np.array_equal(ref.final_value, proofs_full[i].final_value), "serving proof %d differs from alone" % i
+        del p, tabs
+    del srv
+    return {
+        "workload": "%d requests, 70%% InnerProductProver / 30%% MultilinearProver (MSB), num_vars uniform on "
+                    "14..=26 (seed 0x%X), uniform Goldilocks tables generated on the device per request, Fp3 "
+                    "challenges, labels effsc-gpu/serve/{i}; open-loop Poisson arrivals" % (count, SERVE_SEED),
+        "hbm_budget_gb": args.serve_budget_gb, "slots": args.serve_slots,
+        "saturation": {"proofs_per_s": sat, "p50_ms": float(np.percentile(lat_sat, 50) * 1e3),
+                       "p99_ms": float(np.percentile(lat_sat, 99) * 1e3), "makespan_s": mk_sat},
+        "rates": levels,
+        "latency": "submission (arrival) to the proof in host memory",
+        "bit_exact": {"same_in_both_mixes": count, "equal_to_alone_sample": len(sample)},
     }
 
 
