@@ -48,6 +48,8 @@ def parse():
     ap.add_argument("--batch-instances", type=int, default=512,
                     help="batching leg: this many IP instances, num_vars uniform on 10..=22 (0 = skip)")
     ap.add_argument("--batch-steps", type=int, default=10)
+    ap.add_argument("--no-configs", action="store_true",
+                    help="skip the Multilinear n=20 and Coefficient/EqFactored n=24 legs")
     ap.add_argument("--serve-requests", type=int, default=20000,
                     help="serving leg: this many requests, 70%% IP / 30%% ML, num_vars uniform on 14..=26 (0 = skip)")
     ap.add_argument("--serve-slots", type=int, default=128)
@@ -360,6 +362,9 @@ def run_ours(args):
                          "of the reference algorithms (oracle/), not the Rust binary" % (n_vars, dt)}
         assert bit_exact, "GPU proof differs from the oracle at full size"
 
+    configs = None
+    if not args.no_configs and world == 1:
+        configs = run_configs(args, E, L, ctx, stream, rank)
     batch = None
     if args.batch_instances and world == 1:
         batch = run_batch(args, E, L, ctx, stream, rank)
@@ -392,6 +397,7 @@ def run_ours(args):
                                "GB/s": v["bytes"] / (v["ms"] * 1e-3) / 1e9 if v["ms"] else None}
                            for k, v in per.items()},
             "bit_exact_vs_oracle": bit_exact,
+            "other_workloads": configs,
             "batching": batch,
             "serving": serving,
         }
@@ -522,6 +528,149 @@ def run_batch(args, E, L, ctx, stream, rank):
         "autotune": tune_rec,
         "bit_exact": {"batched_vs_one_at_a_time": count, "batched_vs_oracle": oracle_checked},
     }
+
+
+# ---------------------------------------------------------------------------
+# the other single-proof workloads: Multilinear n=20 (Fp) and the degree-3
+# Coefficient / EqFactored pair at n=24 (16 partial rounds, 32-byte hook)
+# ---------------------------------------------------------------------------
+def gl_mul_vec(a, b):
+    """Elementwise Goldilocks product of two canonical uint64 arrays (input
+    preparation only): 32-bit limb products, then 2^64 = 2^32 - 1 and
+    2^96 = -1 (mod p)."""
+    import numpy as np
+    u = np.uint64
+    M = u(0xFFFFFFFF)
+    EPS = u(0xFFFFFFFF)
+    P = u(0xFFFFFFFF00000001)
+    a0, a1, b0, b1 = a & M, a >> u(32), b & M, b >> u(32)
+    p00, p01, p10, p11 = a0 * b0, a0 * b1, a1 * b0, a1 * b1
+    mid = p01 + p10
+    c_mid = (mid < p01).astype(np.uint64)
+    lo = p00 + (mid << u(32))
+    c_lo = (lo < p00).astype(np.uint64)
+    hi = p11 + (mid >> u(32)) + (c_mid << u(32)) + c_lo
+    h0, h1 = hi & M, hi >> u(32)
+    t0 = lo - h1
+    t0 = t0 - EPS * (lo < h1).astype(np.uint64)
+    r = t0 + h0 * EPS
+    r = r + EPS * (r < t0).astype(np.uint64)
+    return np.where(r >= P, r - P, r)
+
+
+def profile_bytes(E, L, fn):
+    """Algorithmic bytes of every kernel one call of fn launches (profiled,
+    outside any graph)."""
+    from effsc_gpu import _lib
+    L.effsc_profile_clear()
+    L.effsc_profile_enable(1)
+    fn()
+    L.effsc_profile_enable(0)
+    tot, ms = 0, 0.0
+    for i in range(L.effsc_profile_count()):
+        name = _lib.ctypes.create_string_buffer(64)
+        msv = _lib.ctypes.c_double()
+        by = _lib.ctypes.c_uint64()
+        _lib.check(L.effsc_profile_get(i, name, 64, _lib.ctypes.byref(msv), _lib.ctypes.byref(by)))
+        tot += by.value
+        ms += msv.value
+    L.effsc_profile_clear()
+    return tot, ms
+
+
+def time_proofs(torch, stream, fn, steps):
+    for _ in range(3):
+        fn()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        out = fn()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / steps, out
+
+
+def run_configs(args, E, L, ctx, stream, rank):
+    import numpy as np
+    import torch
+    res = {}
+    check = rank == 0 and not args.no_cpu_baseline
+    if check:
+        from oracle import oracle as O
+        O.set_threads(os.cpu_count() or 1)
+    # Multilinear MSB, Fp, num_vars = 20, all rounds
+    n = 20
+    v = E.gen_uniform(E.table_seed(0x3170_2026, 0), 1 << n, ctx=ctx)
+    ml = E.MultilinearProver(v, field=E.FP, ctx=ctx)
+    lab = b"effsc-gpu/ml/v1"
+
+    def ml_proof(use_graph=True):
+        ml.reset()
+        return ml.prove(n, E.Transcript.keccak(E.FP, lab), use_graph=use_graph)
+
+    ms, pf = time_proofs(torch, stream, ml_proof, 200)
+    by, _ = profile_bytes(E, L, lambda: ml_proof(False))
+    ok = None
+    if check:
+        rp, ch, fv = O.sumcheck(O.Prover(O.ML, O.MSB, 1, [v]), n, O.Transcript(1, label=lab))
+        ok = bool(np.array_equal(pf.round_polys.reshape(n, 1), rp[:, :, 0]) and
+                  np.array_equal(pf.final_value.reshape(1), fv[:1]))
+        assert ok, "Multilinear n=20 proof differs from the oracle"
+    res["multilinear_fp_n20"] = {
+        "workload": "MultilinearProver MSB over Fp, num_vars=20, seeded uniform table, Fp challenges, label %s, "
+                    "20 rounds + finalize; one CUDA graph per proof (L2-resident, latency-bound)" % lab.decode(),
+        "us_per_proof": ms * 1e3, "evals_per_s": (1 << n) / (ms * 1e-3), "algorithmic_bytes": by,
+        "hbm_gbs": by / (ms * 1e-3) / 1e9, "bit_exact_vs_oracle": ok}
+    del ml
+    # Coefficient (eq * f * g, degree 3) and EqFactored (p = f . g), num_vars = 24
+    n, rounds = 24, 16
+    hook = bytes(range(32))
+    w = E.gen_uniform(E.table_seed(0x3C03_2026, 0), 3 * n, ctx=ctx).reshape(n, 3)
+    f = E.gen_uniform(E.table_seed(0x3C03_2026, 1), 1 << n, ctx=ctx)
+    g = E.gen_uniform(E.table_seed(0x3C03_2026, 2), 1 << n, ctx=ctx)
+    eq = E.build_eq_table(w, ctx=ctx)
+    coef = E.CoefficientProver([eq, f, g], ctx=ctx)
+    lab_c = b"effsc-gpu/coef3/v1"
+
+    def coef_proof(use_graph=True):
+        coef.reset()
+        return coef.prove(rounds, E.Transcript.keccak(E.FP3, lab_c), hook=hook, use_graph=use_graph)
+
+    ms_c, pf_c = time_proofs(torch, stream, coef_proof, 20)
+    by_c, _ = profile_bytes(E, L, lambda: coef_proof(False))
+    pvals = gl_mul_vec(f, g)
+    eqf = E.EqFactoredProver(w, pvals, ctx=ctx)
+    lab_e = b"effsc-gpu/eqf/v1"
+
+    def eqf_proof(use_graph=True):
+        eqf.reset()
+        return eqf.prove(rounds, E.Transcript.keccak(E.FP3, lab_e), hook=hook, use_graph=use_graph)
+
+    ms_e, pf_e = time_proofs(torch, stream, eqf_proof, 20)
+    by_e, _ = profile_bytes(E, L, lambda: eqf_proof(False))
+    ok_c = ok_e = None
+    if check:
+        rp, ch, fv = O.sumcheck(O.Prover(O.COEF, O.MSB, 3, [eq, f, g]), rounds, O.Transcript(3, label=lab_c),
+                                hook=hook)
+        ok_c = bool(np.array_equal(pf_c.round_polys, rp) and np.array_equal(pf_c.final_value, fv))
+        assert ok_c, "Coefficient n=24 proof differs from the oracle"
+        rp, ch, fv = O.sumcheck(O.Prover.eq_factored(3, w, pvals), rounds, O.Transcript(3, label=lab_e), hook=hook)
+        ok_e = bool(np.array_equal(pf_e.round_polys, rp) and np.array_equal(pf_e.final_value, fv))
+        assert ok_e, "EqFactored n=24 proof differs from the oracle"
+    res["coefficient_eqfg_n24"] = {
+        "workload": "CoefficientProver MSB with the degree-3 product evaluator on [eq(r, .) (Fp3), f, g (Fp)], "
+                    "num_vars=24, r seeded uniform Fp3, 16 partial rounds + finalize, hook absorbs 0x00..0x1f per "
+                    "round, label %s" % lab_c.decode(),
+        "ms_per_proof": ms_c, "evals_per_s": 3 * (1 << n) / (ms_c * 1e-3), "algorithmic_bytes": by_c,
+        "hbm_gbs": by_c / (ms_c * 1e-3) / 1e9, "bit_exact_vs_oracle": ok_c}
+    res["eq_factored_n24"] = {
+        "workload": "EqFactoredProver, w = the same r, p = f . g (one base table), num_vars=24, 16 partial "
+                    "rounds + finalize, same hook, label %s" % lab_e.decode(),
+        "ms_per_proof": ms_e, "evals_per_s": (1 << n) / (ms_e * 1e-3), "algorithmic_bytes": by_e,
+        "hbm_gbs": by_e / (ms_e * 1e-3) / 1e9, "bit_exact_vs_oracle": ok_e}
+    del coef, eqf
+    return res
 
 
 # ---------------------------------------------------------------------------
