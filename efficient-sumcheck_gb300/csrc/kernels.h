@@ -27,7 +27,9 @@ enum Sem { SEM_MSB_PAD = 0, SEM_MSB_FLOOR = 1, SEM_LSB = 2 };
 //  POL_IP  : q0 = sum lo_a lo_b, qinf = sum (da)(db)        (2 tables)
 //  POL_C1..3: coefficients of prod_i (lo_i + x d_i)         (1..3 tables)
 //  POL_EQFR: POL_IP on (eq_r, p), times the scalar eq_l[0]  (2 tables)
-enum Pol { POL_ML = 0, POL_IP = 1, POL_C1 = 2, POL_C2 = 3, POL_C3 = 4, POL_EQFR = 5, POL_EQFL = 6 };
+//  POL_IP01: InnerProduct rounds 0 and 1 from one pass over the base tables
+//            (eight base-field sums, two transcript steps)
+enum Pol { POL_ML = 0, POL_IP = 1, POL_C1 = 2, POL_C2 = 3, POL_C3 = 4, POL_EQFR = 5, POL_EQFL = 6, POL_IP01 = 7 };
 
 struct TabIO {
     const u64* in[3];   // SoA component arrays; [1],[2] null for base tables
@@ -50,6 +52,7 @@ struct RoundArgs {
     u32 m_shift;           // EqFactored left phase: log2 |eq_r|
     u64 el_len;            // EqFactored left phase: current |eq_l|
     const u64* chal_ptr;   // challenge in device memory, or null to use `chal`
+    const u64* chal2_ptr;  // second challenge (InnerProduct double fold of round 2)
     u64 chal[3];
     const u64* scalar[3];  // EqFactored right phase: eq_l[0] (c1, c2 null if base)
     u64* partials;         // gridDim * 12 words
@@ -117,6 +120,11 @@ bool launch_eqf_left(bool fused, u32 mask, bool ech, const RoundArgs& a, int gri
 // if no kernel is instantiated for the combination.
 bool launch_fused_tma(int pol, u32 mask, bool ech, const RoundArgs& a, u32 ntiles, int grid, cudaStream_t s);
 int fused_tma_blocks_per_sm(void);
+// InnerProduct MSB over Fp3 challenges, base tables of length L = 2^n >= 8:
+// rounds 0 and 1 from one read of the tables (launch_ip01), then round 2's
+// fold-twice-and-evaluate from a second read (launch_ip2x).
+bool launch_ip01(const RoundArgs& a, int grid, cudaStream_t s);
+bool launch_ip2x(const RoundArgs& a, int grid, cudaStream_t s);
 bool launch_batch_round(int pol, bool fused, u32 mask, bool ech, const BatchSeg* segs, u32 nsegs,
                         const RoundArgs* args, u32 grid, cudaStream_t s);
 void launch_batch_finalize(const RoundArgs* args, const unsigned char* ext, u32 n, int ntab, u64* finals, cudaStream_t s);

@@ -182,8 +182,59 @@ __device__ __forceinline__ int pol_nwire_dev(int pol) {
     }
 }
 
+// POL_IP01: the last block holds the eight base-field sums of one pass over
+// the InnerProduct base tables (quadruples x_j = x[k + jQ], Q = L/4,
+// da = x2 - x0, da' = x3 - x1):
+//   T0 = sum a0 b0, T1 = sum a0 db + da b0, T2 = sum da db,
+//   U0 = sum ea eb, U1 = sum ea fb + fa eb, U2 = sum fa fb
+//       (ea = a1 - a0, fa = da' - da),
+//   V0 = sum a1 b1, V2 = sum da' db'.
+// Round 0 (src/provers/inner_product.rs:94-103): [T0 + V0, T2 + V2].
+// Round 1 on the tables folded with r0 is a quadratic in r0:
+//   h(0) = T0 + r0 T1 + r0^2 T2, h(inf) = U0 + r0 U1 + r0^2 U2.
+// Both rounds run the transcript step in order (wire, hook, challenge).
+static __device__ __noinline__ void finalize_ip01(const u64* raw, const RoundArgs& a) {
+    __shared__ u64 s_w[2][6];
+    __shared__ u64 s_c[2][3];
+    __shared__ __align__(8) uint8_t s_scr[64];
+    const int lane = threadIdx.x & 31;
+    if (lane == 0) {
+        s_w[0][0] = gl_add(raw[0], raw[6]); s_w[0][1] = 0; s_w[0][2] = 0;
+        s_w[0][3] = gl_add(raw[2], raw[7]); s_w[0][4] = 0; s_w[0][5] = 0;
+    }
+    __syncwarp();
+    DevTranscript* T = (DevTranscript*)a.tx.tx;
+    WarpTx w = tx_load(T, lane);
+    for (int rd = 0; rd < 2; rd++) {
+        if (rd == 1 && lane == 0) {
+            const F3 r = f3_make(s_c[0][0], s_c[0][1], s_c[0][2]);
+            F3 q0 = f3_make(raw[2], 0, 0), qi = f3_make(raw[5], 0, 0);
+            q0 = f3_add<true>(f3_mul<true, true>(q0, r), f3_make(raw[1], 0, 0));
+            q0 = f3_add<true>(f3_mul<true, true>(q0, r), f3_make(raw[0], 0, 0));
+            qi = f3_add<true>(f3_mul<true, true>(qi, r), f3_make(raw[4], 0, 0));
+            qi = f3_add<true>(f3_mul<true, true>(qi, r), f3_make(raw[3], 0, 0));
+            s_w[1][0] = q0.c0; s_w[1][1] = q0.c1; s_w[1][2] = q0.c2;
+            s_w[1][3] = qi.c0; s_w[1][4] = qi.c1; s_w[1][5] = qi.c2;
+        }
+        __syncwarp();
+        tx_send_elems(w, lane, s_w[rd], 2);
+        if (a.tx.hook_len) {
+            const uint8_t* hk = a.tx.hook;
+            tx_absorb(w, lane, a.tx.hook_len, [&](u32 k) -> uint8_t { return hk[k]; });
+        }
+        tx_challenge(w, lane, s_c[rd], s_scr);
+    }
+    tx_store(T, w, lane);
+    if (lane < 12) a.tx.proof_wire[lane] = s_w[lane / 6][lane % 6];
+    if (lane < 6) a.tx.proof_chal[lane] = s_c[lane / 3][lane % 3];
+}
+
 // raw: NRAW Fp3 values in shared memory (3 words each).  Run by warp 0.
 static __device__ __noinline__ void finalize_warp(int pol, const u64* raw, const RoundArgs& a) {
+    if (pol == POL_IP01) {
+        finalize_ip01(raw, a);
+        return;
+    }
     __shared__ u64 s_wire[9];
     __shared__ u64 s_aux[6];
     __shared__ u64 s_chal[3];

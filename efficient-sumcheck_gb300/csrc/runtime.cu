@@ -261,6 +261,8 @@ struct effsc_prover {
     // effsc_prove: tables of at most this length finish in the one-block tail
     // kernel (SIZE_MAX: as large as shared memory allows; 0: never)
     size_t tail_len = SIZE_MAX;
+    // effsc_prove: InnerProduct rounds 0-2 in two passes (k_ip01.cu)
+    bool fuse_first = true;
 };
 
 namespace {
@@ -543,6 +545,48 @@ int do_tail(effsc_prover* P, size_t r, size_t num_rounds, const Chal& ch, const 
             T.len = L >> folds;
             T.ext = out_ext;
         }
+    return EFFSC_OK;
+}
+
+// effsc_prove of an MSB InnerProduct prover over Fp3 challenges whose base
+// tables are powers of two: rounds 0 and 1 from one pass, round 2 (with the
+// folds by r0 and r1) from a second (k_ip01.cu).  Leaves the state the
+// per-round path leaves after round 2.
+bool fuse_first_ok(const effsc_prover* P, size_t num_rounds) {
+    if (!P->fuse_first || P->kind != EFFSC_IP || P->order != EFFSC_MSB || P->field != EFFSC_FP3) return false;
+    if (num_rounds < 3) return false;
+    const size_t L = P->t[0].len;
+    if (P->t[1].len != L || !is_pow2(L) || L < 8 || P->t[0].ext || P->t[1].ext) return false;
+    if (P->t[0].cur != 0 || P->t[1].cur != 0) return false;
+    Chal none;
+    return !tail_ok(P, 0, num_rounds, none);
+}
+
+int do_fuse_first(effsc_prover* P, const TxIO& tx0, const TxIO& tx2, const u64* chals, bool dry) {
+    const size_t L = P->t[0].len;
+    RoundArgs a = base_args(P);
+    a.tx = tx0;
+    a.L = L;
+    for (int i = 0; i < 2; i++) set_in(a, i, P->t[i]);
+    if (!dry) TRY(timed_launch(P->ctx->stream, "ip_rounds_0_1", 16 * (uint64_t)L, [&] { return launch_ip01(a, grid_for(L / 4), P->ctx->stream); }));
+    int bi[2];
+    for (int i = 0; i < 2; i++) TRY(out_buffer(P, P->t[i], true, L / 4, true, &bi[i]));
+    RoundArgs b = base_args(P);
+    b.tx = tx2;
+    b.L = L;
+    b.chal_ptr = chals;
+    b.chal2_ptr = chals + 3;
+    for (int i = 0; i < 2; i++) {
+        set_in(b, i, P->t[i]);
+        set_out(b, i, P->t[i].bufs[bi[i]]);
+    }
+    if (!dry) TRY(timed_launch(P->ctx->stream, "ip_round_2_double_fold", 16 * (uint64_t)L + 12 * (uint64_t)L, [&] { return launch_ip2x(b, grid_for(L / 8), P->ctx->stream); }));
+    for (int i = 0; i < 2; i++) {
+        Table& T = P->t[i];
+        T.cur = bi[i];
+        T.len = L / 4;
+        T.ext = true;
+    }
     return EFFSC_OK;
 }
 
@@ -1165,6 +1209,13 @@ int effsc_prover_read_table(effsc_prover* P, int table, uint64_t* out) {
     return EFFSC_OK;
 }
 
+int effsc_prover_set_first_rounds(effsc_prover* P, int fused) {
+    if (!P) return fail(EFFSC_INVALID_ARG, "prover is NULL");
+    if ((fused != 0) != P->fuse_first && P->gexec) { cudaGraphExecDestroy(P->gexec); P->gexec = nullptr; }
+    P->fuse_first = fused != 0;
+    return EFFSC_OK;
+}
+
 int effsc_prover_set_tail(effsc_prover* P, size_t max_len) {
     if (!P) return fail(EFFSC_INVALID_ARG, "prover is NULL");
     if (max_len != P->tail_len && P->gexec) { cudaGraphExecDestroy(P->gexec); P->gexec = nullptr; }
@@ -1218,7 +1269,22 @@ int effsc_prove(effsc_prover* P, size_t num_rounds, effsc_transcript* T, const u
         if (!P->t[i].bufs.empty() && (P->t[i].cur != 0 || P->t[i].len != P->len0[i])) at_reset = false;
 
     auto launch_all = [&](bool dry) -> int {
-        for (size_t r = 0; r < num_rounds; r++) {
+        size_t r0 = 0;
+        if (fuse_first_ok(P, num_rounds)) {
+            TxIO t0, t2;
+            memset(&t0, 0, sizeof t0);
+            t0.tx = P->d_tx;
+            t0.hook = P->d_hook;
+            t0.hook_len = (u32)hook_len;
+            t2 = t0;
+            t0.proof_wire = P->d_wire;
+            t0.proof_chal = P->d_chals;
+            t2.proof_wire = P->d_wire + (size_t)2 * 3 * d;
+            t2.proof_chal = P->d_chals + 3 * 2;
+            TRY(do_fuse_first(P, t0, t2, P->d_chals, dry));
+            r0 = 3;
+        }
+        for (size_t r = r0; r < num_rounds; r++) {
             Chal ch;
             if (r > 0) { ch.has = true; ch.ext = P->field == EFFSC_FP3; ch.dev = P->d_chals + 3 * (r - 1); }
             TxIO tx;

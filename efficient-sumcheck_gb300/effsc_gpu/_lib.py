@@ -59,6 +59,7 @@ SIGNATURES = {
     "effsc_gen_uniform": (ci, [vp, ctypes.c_uint64, ctypes.c_uint64, u64p, u64p]),
     "effsc_table_seed": (ctypes.c_uint64, [ctypes.c_uint64, ctypes.c_uint64]),
     "effsc_prover_set_tail": (ci, [vp, sz]),
+    "effsc_prover_set_first_rounds": (ci, [vp, ci]),
     "effsc_batch_create": (ci, [vp, ci, ci, sz, ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(u64p), u64p,
                                 ctypes.POINTER(vp)]),
     "effsc_batch_destroy": (ci, [vp]),

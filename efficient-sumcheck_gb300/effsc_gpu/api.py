@@ -244,6 +244,10 @@ class _Prover:
     def reset(self):
         check(load().effsc_prover_reset(self.h))
 
+    def set_first_rounds(self, fused):
+        """prove(): InnerProduct rounds 0-2 in two passes (True) or three."""
+        check(load().effsc_prover_set_first_rounds(self.h, 1 if fused else 0))
+
     def set_tail(self, max_len):
         """prove(): tables of at most max_len entries finish in the one-block
         tail kernel (None: as large as shared memory allows, 0: never)."""

@@ -136,6 +136,12 @@ int effsc_prover_read_table(effsc_prover* p, int table, uint64_t* out);
  * in shared memory (one launch instead of one per round).  Default SIZE_MAX:
  * as long as shared memory allows; 0 disables.  Proofs are identical. */
 int effsc_prover_set_tail(effsc_prover* p, size_t max_len);
+/* effsc_prove only (no reference counterpart; a tuning knob): for an MSB
+ * InnerProduct prover over Fp3 challenges with power-of-two base tables,
+ * compute rounds 0-2 in two passes over the base tables (round 1 from sums
+ * gathered during round 0; round 2 folds with both challenges).  Default 1;
+ * 0 runs one pass per round.  Proofs are identical. */
+int effsc_prover_set_first_rounds(effsc_prover* p, int fused);
 
 /* Restore the state right after construction (the input tables are never
  * written by the rounds), so a proof can be recomputed without re-upload. */

@@ -1,0 +1,78 @@
+"""InnerProduct rounds 0-2 in two passes (round 1 from base-field sums of
+round 0's pass, round 2 folding with r0 and r1): proofs, challenges, final
+values and post-state tables identical to one pass per round and to the
+oracle, for full and partial runs, with and without hooks."""
+import random
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def E():
+    import effsc_gpu
+    effsc_gpu.load()
+    return effsc_gpu
+
+
+def tables(n, seed):
+    g = np.random.default_rng(seed)
+    return [g.integers(0, O.P, size=1 << n, dtype=np.uint64) for _ in range(2)]
+
+
+@pytest.mark.parametrize("n", [3, 4, 5, 7, 10, 13, 16])
+@pytest.mark.parametrize("hook", [b"", bytes(range(32)), b"\x05\x06\x07"])
+def test_full_runs(E, n, hook):
+    a, b = tables(n, 100 + n + len(hook))
+    p = E.InnerProductProver(a, b)
+    p.set_tail(0)
+    q = E.InnerProductProver(a, b)
+    q.set_tail(0)
+    q.set_first_rounds(False)
+    for use_graph in (True, True, False):
+        p.reset()
+        q.reset()
+        x = p.prove(n, E.Transcript.keccak(3, b"fr"), hook=hook, use_graph=use_graph)
+        y = q.prove(n, E.Transcript.keccak(3, b"fr"), hook=hook, use_graph=use_graph)
+        assert np.array_equal(x.round_polys, y.round_polys)
+        assert np.array_equal(x.challenges, y.challenges)
+        assert np.array_equal(x.final_value, y.final_value)
+    rp, ch, fv = O.sumcheck(O.Prover(O.IP, O.MSB, 3, [a, b]), n, O.Transcript(3, label=b"fr"), hook=hook)
+    assert np.array_equal(x.round_polys, rp)
+    assert np.array_equal(x.challenges, ch)
+    assert np.array_equal(x.final_value, fv)
+
+
+@pytest.mark.parametrize("rounds", [1, 2, 3, 4, 6])
+def test_partial_runs_post_state(E, rounds):
+    n = 9
+    a, b = tables(n, rounds)
+    p = E.InnerProductProver(a, b)
+    p.set_tail(0)
+    q = E.InnerProductProver(a, b)
+    q.set_tail(0)
+    q.set_first_rounds(False)
+    x = p.prove(rounds, E.Transcript.keccak(3, b"pr"), hook=bytes(range(32)))
+    y = q.prove(rounds, E.Transcript.keccak(3, b"pr"), hook=bytes(range(32)))
+    assert np.array_equal(x.round_polys, y.round_polys)
+    assert np.array_equal(x.final_value, y.final_value)
+    for t in range(2):
+        assert np.array_equal(p.table(t), q.table(t))
+    rp, ch, fv = O.sumcheck(O.Prover(O.IP, O.MSB, 3, [a, b]), rounds, O.Transcript(3, label=b"pr"),
+                            hook=bytes(range(32)))
+    assert np.array_equal(x.round_polys, rp)
+    assert np.array_equal(x.final_value, fv)
+
+
+def test_default_path_large(E):
+    """n = 20 with the default plan (two-pass start, TMA rounds, tail)."""
+    n = 20
+    a, b = tables(n, 7)
+    x = E.InnerProductProver(a, b).prove(n, E.Transcript.keccak(3, b"big"))
+    rp, ch, fv = O.sumcheck(O.Prover(O.IP, O.MSB, 3, [a, b]), n, O.Transcript(3, label=b"big"))
+    assert np.array_equal(x.round_polys, rp)
+    assert np.array_equal(x.final_value, fv)
