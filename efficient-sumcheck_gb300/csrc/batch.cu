@@ -1,7 +1,11 @@
 // batch.cu -- many independent Multilinear / InnerProduct (MSB) provers of
-// uneven size proved together: one kernel launch per round for every instance
-// still active, each instance with its own grid reduction and Keccak
-// transcript, and the whole multi-round protocol captured once as a CUDA graph.
+// uneven size proved together: one kernel launch per step for every instance
+// still in its multi-block rounds (k_serve_step: each instance's segment runs
+// its own round, or the two-pass start of an InnerProduct proof over Fp3),
+// one launch of the one-block tail kernel for every instance's last rounds,
+// one launch for all final folds; each instance keeps its own grid reduction
+// and Keccak transcript, and the whole protocol is captured once as a CUDA
+// graph.
 //
 // Instance i has num_vars[i] = n_i variables (tables of 2^n_i elements) and is
 // proved with all n_i rounds, exactly as runner::sumcheck (src/runner.rs:29-69)
@@ -52,11 +56,11 @@ struct effsc_batch {
     TailArgs* d_tail = nullptr;
     u32 n_tail = 0;
     u64 tail_smem_len = 0;
-    u32 rounds_planned = 0;                // batched round kernels before the tail
-    std::vector<size_t> seg_off, seg_cnt;  // per round into d_segs
-    std::vector<u32> grid;                 // blocks per round
-    BatchSeg* d_segs = nullptr;
-    RoundArgs* d_args = nullptr;           // per round: one RoundArgs per instance (index by instance)
+    u32 rounds_planned = 0;                // step launches before the tail
+    std::vector<size_t> seg_off, seg_cnt;  // per step into d_segs / d_args
+    std::vector<u32> grid;                 // blocks per step
+    ServeSeg* d_segs = nullptr;
+    RoundArgs* d_args = nullptr;           // one RoundArgs per segment, steps concatenated
     RoundArgs* d_fin_args = nullptr;
     unsigned char* d_ext = nullptr;
     u64* d_partials = nullptr;
@@ -100,68 +104,93 @@ int plan(effsc_batch* b) {
     u32 tail_log = 0;
     while ((2ULL << tail_log) <= tl) tail_log++;
     b->tail_r0.assign(b->n, 0);
-    u32 R = 0;
     for (size_t i = 0; i < b->n; i++) {
         const u32 n_i = b->nv[i];
         if (tail_log < 2) b->tail_r0[i] = n_i;
         else b->tail_r0[i] = n_i <= tail_log ? 0 : n_i - tail_log + 1;
-        R = std::max<u32>(R, b->tail_r0[i]);
     }
+    // steps: one launch each.  An InnerProduct instance over Fp3 whose first
+    // three rounds are all multi-block takes two steps for them (ip01.cuh:
+    // rounds 0-1, then round 2 with the double fold); every other round is
+    // one step.  Step s of instance i runs round s, or for the two-pass
+    // start: rounds 0-1 (s = 0), round 2 (s = 1), round s + 1 (s >= 2).
     const int maxb = max_grid();
-    std::vector<BatchSeg> segs;
-    std::vector<RoundArgs> args((size_t)R * b->n);
-    b->rounds_planned = R;
-    b->seg_off.assign(R, 0);
-    b->seg_cnt.assign(R, 0);
-    b->grid.assign(R, 0);
+    std::vector<char> two(b->n, 0);
+    std::vector<u32> nsteps(b->n, 0);
+    u32 S = 0;
+    for (size_t i = 0; i < b->n; i++) {
+        two[i] = b->kind == EFFSC_IP && F3W == 3 && b->tail_r0[i] >= 3;
+        nsteps[i] = two[i] ? b->tail_r0[i] - 1 : b->tail_r0[i];
+        S = std::max<u32>(S, nsteps[i]);
+    }
+    std::vector<ServeSeg> segs;
+    std::vector<RoundArgs> args;
+    b->rounds_planned = S;
+    b->seg_off.assign(S, 0);
+    b->seg_cnt.assign(S, 0);
+    b->grid.assign(S, 0);
     size_t max_blocks = 1;
     std::vector<RoundArgs> fin(b->n);
     std::vector<unsigned char> ext(b->n, 0);
-    for (u32 r = 0; r < R; r++) {
-        b->seg_off[r] = segs.size();
+    const u64 per_block = (u64)KERNEL_TPB * b->quads_per_thread;
+    const u32 kind_code = (b->kind == EFFSC_IP ? SERVE_IP : 0) | (F3W == 3 ? SERVE_FP3 : 0);
+    for (u32 st = 0; st < S; st++) {
+        b->seg_off[st] = segs.size();
         u32 first = 0;
         for (size_t i = 0; i < b->n; i++) {
+            if (st >= nsteps[i]) continue;
             const u32 n_i = b->nv[i];
-            if (b->tail_r0[i] <= r) continue;
-            const u64 L = r == 0 ? (1ULL << n_i) : (1ULL << (n_i - r + 1));
-            const u64 work = r == 0 ? L / 2 : L / 4;
-            u64 nb = (work + (u64)KERNEL_TPB * b->quads_per_thread - 1) / ((u64)KERNEL_TPB * b->quads_per_thread);
-            nb = std::max<u64>(1, std::min<u64>(nb, (u64)maxb));
-            BatchSeg sg;
-            sg.first_block = first;
-            sg.nblocks = (u32)nb;
-            sg.inst = (u32)i;
-            sg.reserved = 0;
-            segs.push_back(sg);
+            const u64 half0 = 1ULL << (n_i - 1);      // work buffer length (one component)
             RoundArgs a;
             memset(&a, 0, sizeof a);
-            for (int t = 0; t < b->ntab; t++) {
-                u64* inb = b->in[i * b->ntab + t];
-                u64* wk = b->work[i * b->ntab + t];
-                const u64 half0 = 1ULL << (n_i - 1);      // work buffer length (one component)
-                const bool cur_ext = r >= 2 && F3W == 3;
-                if (r <= 1) { a.t[t].in[0] = inb; }
-                else for (int c = 0; c < (cur_ext ? 3 : 1); c++) a.t[t].in[c] = wk + c * half0;
-                if (r >= 1)
-                    for (int c = 0; c < F3W; c++) a.t[t].out[c] = wk + c * half0;
+            u32 phase, r;
+            u64 L, work;
+            if (two[i] && st < 2) {
+                r = st == 0 ? 0 : 2;
+                phase = st == 0 ? SERVE_IP01 : SERVE_IP2X;
+                L = 1ULL << n_i;
+                work = st == 0 ? L / 4 : L / 8;
+                for (int t = 0; t < 2; t++) {
+                    a.t[t].in[0] = b->in[i * 2 + t];
+                    if (st) for (int c = 0; c < 3; c++) a.t[t].out[c] = b->work[i * 2 + t] + c * half0;
+                }
+                a.chal_ptr = st ? b->d_chal + 3 * b->round_off[i] : nullptr;
+                a.chal2_ptr = st ? b->d_chal + 3 * (b->round_off[i] + 1) : nullptr;
+            } else {
+                r = two[i] ? st + 1 : st;
+                L = r == 0 ? (1ULL << n_i) : (1ULL << (n_i - r + 1));
+                work = r == 0 ? L / 2 : L / 4;
+                phase = r == 0 ? SERVE_EVAL : (r == 1 || F3W == 1) ? SERVE_FOLD_BASE : SERVE_FOLD_EXT;
+                for (int t = 0; t < b->ntab; t++) {
+                    u64* inb = b->in[i * b->ntab + t];
+                    u64* wk = b->work[i * b->ntab + t];
+                    const bool cur_ext = r >= 2 && F3W == 3;
+                    if (r <= 1) a.t[t].in[0] = inb;
+                    else for (int c = 0; c < (cur_ext ? 3 : 1); c++) a.t[t].in[c] = wk + c * half0;
+                    if (r >= 1)
+                        for (int c = 0; c < F3W; c++) a.t[t].out[c] = wk + c * half0;
+                }
+                a.chal_ptr = r ? b->d_chal + 3 * (b->round_off[i] + r - 1) : nullptr;
             }
+            u64 nb = (work + per_block - 1) / per_block;
+            nb = std::max<u64>(1, std::min<u64>(nb, (u64)maxb));
+            ServeSeg sg;
+            sg.first_block = first;
+            sg.nblocks = (u32)nb;
+            sg.code = kind_code | (phase << SERVE_PHASE_SHIFT);
+            sg.reserved = 0;
+            segs.push_back(sg);
             a.L = L;
-            a.chal_ptr = r ? b->d_chal + 3 * (b->round_off[i] + r - 1) : nullptr;
-            a.partials = nullptr;   // set below once offsets are known
             a.counter = b->d_counters + i;
             a.status = b->d_status;
-            a.result = nullptr;
             a.tx.tx = b->d_tx + i;
-            a.tx.hook = nullptr;
-            a.tx.hook_len = 0;
             a.tx.proof_wire = b->d_wire + 3 * deg_of(b) * (b->round_off[i] + r);
             a.tx.proof_chal = b->d_chal + 3 * (b->round_off[i] + r);
-            a.tx.chal_next = nullptr;
-            args[(size_t)r * b->n + i] = a;
+            args.push_back(a);
             first += (u32)nb;
         }
-        b->seg_cnt[r] = segs.size() - b->seg_off[r];
-        b->grid[r] = first;
+        b->seg_cnt[st] = segs.size() - b->seg_off[st];
+        b->grid[st] = first;
         max_blocks = std::max<size_t>(max_blocks, first);
     }
     // finalize: the tables after round n_i - 1 (length 2)
@@ -219,17 +248,13 @@ int plan(effsc_batch* b) {
         BCK(cudaMallocAsync((void**)&b->d_tail, tails.size() * sizeof(TailArgs), s));
         BCK(cudaMemcpyAsync(b->d_tail, tails.data(), tails.size() * sizeof(TailArgs), cudaMemcpyHostToDevice, s));
     }
-    // per-instance partial ranges: block-index offsets within each round
-    for (u32 r = 0; r < R; r++)
-        for (size_t k = 0; k < b->seg_cnt[r]; k++) {
-            const BatchSeg& sg = segs[b->seg_off[r] + k];
-            args[(size_t)r * b->n + sg.inst].partials = b->d_partials + (size_t)sg.first_block * 12;
-        }
-    BCK(cudaMallocAsync((void**)&b->d_segs, std::max<size_t>(1, segs.size()) * sizeof(BatchSeg), s));
+    // per-segment partial ranges: block-index offsets within each step
+    for (size_t k = 0; k < segs.size(); k++) args[k].partials = b->d_partials + (size_t)segs[k].first_block * 12;
+    BCK(cudaMallocAsync((void**)&b->d_segs, std::max<size_t>(1, segs.size()) * sizeof(ServeSeg), s));
     BCK(cudaMallocAsync((void**)&b->d_args, std::max<size_t>(1, args.size()) * sizeof(RoundArgs), s));
     BCK(cudaMallocAsync((void**)&b->d_fin_args, std::max<size_t>(1, fin.size()) * sizeof(RoundArgs), s));
     BCK(cudaMallocAsync((void**)&b->d_ext, std::max<size_t>(1, ext.size()), s));
-    if (!segs.empty()) BCK(cudaMemcpyAsync(b->d_segs, segs.data(), segs.size() * sizeof(BatchSeg), cudaMemcpyHostToDevice, s));
+    if (!segs.empty()) BCK(cudaMemcpyAsync(b->d_segs, segs.data(), segs.size() * sizeof(ServeSeg), cudaMemcpyHostToDevice, s));
     if (!args.empty()) BCK(cudaMemcpyAsync(b->d_args, args.data(), args.size() * sizeof(RoundArgs), cudaMemcpyHostToDevice, s));
     BCK(cudaMemcpyAsync(b->d_fin_args, fin.data(), fin.size() * sizeof(RoundArgs), cudaMemcpyHostToDevice, s));
     BCK(cudaMemcpyAsync(b->d_ext, ext.data(), ext.size(), cudaMemcpyHostToDevice, s));
@@ -239,14 +264,10 @@ int plan(effsc_batch* b) {
 }
 
 int launch_protocol(effsc_batch* b, uint64_t* kernels) {
-    const bool ech = b->field == EFFSC_FP3;
-    const u32 full = (1u << b->ntab) - 1;
-    for (u32 r = 0; r < b->rounds_planned; r++) {
-        if (!b->seg_cnt[r]) continue;
-        u32 mask = r >= 2 && ech ? full : 0;
-        bool ok = launch_batch_round(b->pol, r > 0, mask, r > 0 && ech, b->d_segs + b->seg_off[r], (u32)b->seg_cnt[r],
-                                     b->d_args + (size_t)r * b->n, b->grid[r], b->stream);
-        if (!ok) return effsc_set_error(EFFSC_UNSUPPORTED, "no batched kernel for this round");
+    for (u32 st = 0; st < b->rounds_planned; st++) {
+        if (!b->seg_cnt[st]) continue;
+        launch_serve_step(b->d_segs + b->seg_off[st], (u32)b->seg_cnt[st], b->d_args + b->seg_off[st], b->grid[st],
+                          b->stream);
         (*kernels)++;
     }
     if (b->n_tail) {

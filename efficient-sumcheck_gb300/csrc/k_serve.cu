@@ -4,9 +4,10 @@
 // A step's grid is the concatenation of the requests' block ranges; segment k
 // (sorted by first block) names its RoundArgs (args[k]) and what the request
 // does this step: evaluate round 0 on its base tables, fold + evaluate from
-// base or Fp3 tables, or the final fold and final value.  The branch is
+// base or Fp3 tables, the two-pass start of an InnerProduct proof (rounds 0-1,
+// then round 2 with the double fold), or the final fold and final value.  The branch is
 // uniform per block, so each block runs exactly the single-instance body.
-#include "round_common.cuh"
+#include "ip01.cuh"
 
 namespace effsc {
 
@@ -58,6 +59,8 @@ __device__ __forceinline__ void serve_dispatch(const RoundArgs& sa, u32 code, u3
     case SERVE_FOLD_EXT: fused_body<POL, SEM_MSB_PAD, FULL, true>(sa, bid, nb); break;
     case SERVE_FINAL_BASE: final_body(sa, POL, false); break;
     case SERVE_FINAL_EXT: final_body(sa, POL, true); break;
+    case SERVE_IP01: if (POL == POL_IP) ip01_body(sa, bid, nb); break;
+    case SERVE_IP2X: if (POL == POL_IP) ip2x_body(sa, bid, nb); break;
     default: break;
     }
 }

@@ -62,13 +62,6 @@ struct RoundArgs {
     TxIO tx;
 };
 
-// Batched rounds: one entry per active instance, sorted by first_block.
-struct BatchSeg {
-    u32 first_block;
-    u32 nblocks;
-    u32 inst;
-    u32 reserved;
-};
 
 // The last rounds of an MSB Multilinear / InnerProduct proof run by one block
 // with the tables in shared memory: rounds r0 .. r0 + nrounds - 1, each a
@@ -104,7 +97,12 @@ struct ServeSeg {
     u32 reserved;
 };
 constexpr u32 SERVE_IP = 1, SERVE_FP3 = 2, SERVE_PHASE_SHIFT = 2;
-enum ServePhase { SERVE_EVAL = 0, SERVE_FOLD_BASE = 1, SERVE_FOLD_EXT = 2, SERVE_FINAL_BASE = 3, SERVE_FINAL_EXT = 4 };
+// SERVE_IP01 / SERVE_IP2X: InnerProduct rounds 0-1 / round 2 of the two-pass
+// start (Fp3 challenges, base tables; ip01.cuh).
+enum ServePhase {
+    SERVE_EVAL = 0, SERVE_FOLD_BASE = 1, SERVE_FOLD_EXT = 2, SERVE_FINAL_BASE = 3, SERVE_FINAL_EXT = 4,
+    SERVE_IP01 = 5, SERVE_IP2X = 6
+};
 void launch_serve_step(const ServeSeg* segs, u32 nsegs, const RoundArgs* args, u32 grid, cudaStream_t s);
 
 int pol_ntables(int pol);
@@ -125,8 +123,6 @@ int fused_tma_blocks_per_sm(void);
 // fold-twice-and-evaluate from a second read (launch_ip2x).
 bool launch_ip01(const RoundArgs& a, int grid, cudaStream_t s);
 bool launch_ip2x(const RoundArgs& a, int grid, cudaStream_t s);
-bool launch_batch_round(int pol, bool fused, u32 mask, bool ech, const BatchSeg* segs, u32 nsegs,
-                        const RoundArgs* args, u32 grid, cudaStream_t s);
 void launch_batch_finalize(const RoundArgs* args, const unsigned char* ext, u32 n, int ntab, u64* finals, cudaStream_t s);
 
 // Utility kernels.

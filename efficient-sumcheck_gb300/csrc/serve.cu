@@ -66,6 +66,7 @@ struct Req {
     u64* mem = nullptr;    // tables: per table 2^n input words then F3W * 2^(n-1) work words
     u64* res = nullptr;    // RES_WORDS proof words | transcript | counter
     u32 round = 0;         // next round (n: finalize)
+    bool two_pass = false; // InnerProduct over Fp3, n >= 3: rounds 0-2 in two steps (ip01.cuh)
     int slot = -1;         // pinned result slot
     cudaEvent_t ev = nullptr;
     u64* in(int t) const { return mem + (size_t)t * words_per_table(); }
@@ -240,7 +241,27 @@ int step(effsc_server* s) {
         u32 code = (pol == POL_IP ? SERVE_IP : 0) | (f3 ? SERVE_FP3 : 0);
         const u64 half0 = 1ULL << (r->n - 1);
         const u32 rd = r->round;
-        if (rd < r->n) {
+        if (r->two_pass && rd < 3) {
+            // rounds 0-1 from the base tables, then round 2 with the double fold
+            const u64 L = 1ULL << r->n;
+            code |= (rd == 0 ? SERVE_IP01 : SERVE_IP2X) << SERVE_PHASE_SHIFT;
+            for (int t = 0; t < 2; t++) {
+                a.t[t].in[0] = r->in(t);
+                if (rd) for (int c = 0; c < 3; c++) a.t[t].out[c] = r->work(t) + c * half0;
+            }
+            a.L = L;
+            a.chal_ptr = rd ? r->chal() : nullptr;
+            a.chal2_ptr = rd ? r->chal() + 3 : nullptr;
+            a.counter = r->counter();
+            a.status = s->d_status;
+            a.tx.tx = r->tx();
+            a.tx.proof_wire = r->wire() + (size_t)6 * rd;
+            a.tx.proof_chal = r->chal() + 3 * rd;
+            const u64 work = rd == 0 ? L / 4 : L / 8;
+            u64 nb = (work + per_block - 1) / per_block;
+            nb = std::max<u64>(1, std::min<u64>(nb, (u64)maxb));
+            sg.nblocks = (u32)nb;
+        } else if (rd < r->n) {
             const u64 L = rd == 0 ? (1ULL << r->n) : (1ULL << (r->n - rd + 1));
             const u64 work = rd == 0 ? L / 2 : L / 4;
             const u32 phase = rd == 0 ? SERVE_EVAL : (rd == 1 || !f3) ? SERVE_FOLD_BASE : SERVE_FOLD_EXT;
@@ -310,7 +331,10 @@ int step(effsc_server* s) {
     std::vector<Req*> still;
     still.reserve(s->active.size());
     for (Req* r : s->active) {
-        if (r->round < r->n) { r->round++; still.push_back(r); }
+        if (r->round < r->n) {
+            r->round += (r->two_pass && r->round == 0) ? 2 : 1;
+            still.push_back(r);
+        }
     }
     s->active.swap(still);
     SCK(cudaEventRecord(st.ev, cs));
@@ -338,6 +362,7 @@ int submit_one(effsc_server* s, int kind, int field, uint32_t num_vars, const ui
     }
     effsc_internal_tx_state(t, &r->tx0);
     if ((int)r->tx0.deg != field) { delete r; return effsc_set_error(EFFSC_INVALID_ARG, "transcript: wrong field or kind"); }
+    r->two_pass = kind == EFFSC_IP && field == EFFSC_FP3 && num_vars >= 3;
     r->bytes = req_bytes(*r);
     if (r->bytes > s->budget) {
         size_t b = r->bytes;
