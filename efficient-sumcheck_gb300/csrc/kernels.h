@@ -105,6 +105,18 @@ enum ServePhase {
 };
 void launch_serve_step(const ServeSeg* segs, u32 nsegs, const RoundArgs* args, u32 grid, cudaStream_t s);
 
+// EqFactored left phase from the inner sums (k_eqf.cu).  A Tab3 holds a
+// table's component arrays (components 1, 2 unused for base tables).
+struct Tab3 {
+    const u64* c[3];
+};
+void launch_eqf_inner(bool ee, bool ep, Tab3 p, Tab3 er, u64 m, u64 rows, u64* s0, u64* s1, u64* s2, cudaStream_t s);
+// out = p folded over its top log2(rows) variables with the eq weights e
+// (rows x Lc entries of p; splits row groups summed through `part`, 3 words
+// per entry per split).
+void launch_eqf_fold_rows(bool ew, bool ep, Tab3 p, Tab3 e, u64 Lc, u64 rows, u64 splits, u64* part, int fw, u64* o0,
+                          u64* o1, u64* o2, cudaStream_t s);
+
 int pol_ntables(int pol);
 int pol_nraw(int pol);
 int pol_nwire(int pol);

@@ -710,6 +710,11 @@ __global__ void __launch_bounds__(TPB) k_fold(RoundArgs a, int t) {
 // Tables: t[0] = p, t[1] = eq_l (already folded), t[2] = eq_r.
 // M bit 0: p is Fp3, bit 1: eq tables are Fp3.  FUSED: fold p first (MSB,
 // L a power of two >= 4) and evaluate on the folded table.
+// When an a-block (m = |eq_r| entries of p) spans at least a block's worth of
+// threads, a block walks chunks of C = min(m, 4096) consecutive entries: the
+// inner sums over b are accumulated unreduced per thread and multiplied by
+// eq_l once per chunk, as the split-value structure intends (2 products per
+// entry instead of 4).  Smaller m multiplies per entry.
 template <bool FUSED, u32 M, bool ECH>
 __global__ void __launch_bounds__(TPB) k_eqf_left(RoundArgs a) {
     constexpr bool EPI = ext_of<M>(0), EE = ext_of<M>(1);
@@ -725,6 +730,58 @@ __global__ void __launch_bounds__(TPB) k_eqf_left(RoundArgs a) {
     const u64 ph = FUSED ? (L >> 2) : (L >> 1);           // half of the (folded) p
     const u64 eh = a.el_len >> 1;
     const u64 mmask = (1ULL << a.m_shift) - 1;
+    const u64 m = mmask + 1;
+    if (m >= TPB && ph >= m) {
+        const u64 C = m < 4096 ? m : 4096;
+        const u64 nchunks = ph / C;
+        F3 s0t = f3_zero(), sdt = f3_zero();
+        for (u64 c = blockIdx.x; c < nchunks; c += gridDim.x) {
+            ProdAcc<EE, EP> s0, sd;
+            s0.init();
+            sd.init();
+            const u64 base = c * C;
+            // U entries per thread per step, all loads issued before the
+            // arithmetic (each entry is read and written by this thread only)
+            constexpr int U = (FUSED && EPI) ? 2 : 4;
+            constexpr int NX = FUSED ? 4 : 2;
+            for (u64 k0 = base + threadIdx.x; k0 < base + C; k0 += (u64)U * TPB) {
+                F3 X[U][NX];
+#pragma unroll
+                for (int u = 0; u < U; u++) {
+                    const u64 k = k0 + (u64)u * TPB;
+                    if (k < base + C)
+#pragma unroll
+                        for (int j = 0; j < NX; j++) X[u][j] = ld<EPI>(a.t[0].in, k + j * ph);
+                }
+#pragma unroll
+                for (int u = 0; u < U; u++) {
+                    const u64 k = k0 + (u64)u * TPB;
+                    if (k >= base + C) break;
+                    F3 pl, phv;
+                    if (FUSED) {
+                        if (EPI) { pl = f3_fold<true, true>(X[u][0], X[u][2], r); phv = f3_fold<true, true>(X[u][1], X[u][3], r); }
+                        else if (ECH) { pl = f3_fold<false, true>(X[u][0], X[u][2], r); phv = f3_fold<false, true>(X[u][1], X[u][3], r); }
+                        else { pl = f3_fold<false, false>(X[u][0], X[u][2], r); phv = f3_fold<false, false>(X[u][1], X[u][3], r); }
+                        st<EP>(a.t[0].out, k, pl);
+                        st<EP>(a.t[0].out, k + ph, phv);
+                    } else {
+                        pl = X[u][0];
+                        phv = X[u][1];
+                    }
+                    const F3 er = ld<EE>(a.t[2].in, k & mmask);
+                    s0.mac(er, pl);
+                    sd.mac(er, f3_sub<EP>(phv, pl));
+                }
+            }
+            const u64 ai = base >> a.m_shift;
+            const F3 el = ld<EE>(a.t[1].in, ai), eh_ = ld<EE>(a.t[1].in, ai + eh);
+            s0t = f3_add<true>(s0t, f3_mul<EE, ET>(el, s0.result()));
+            sdt = f3_add<true>(sdt, f3_mul<EE, ET>(f3_sub<EE>(eh_, el), sd.result()));
+        }
+        F3 raw[2] = {s0t, sdt};
+        reduce_and_finalize<2>(raw, a, POL_EQFL);
+        return;
+    }
     const u64 tid = (u64)blockIdx.x * TPB + threadIdx.x, stride = (u64)gridDim.x * TPB;
     for (u64 k = tid; k < ph; k += stride) {
         F3 pl, phv;

@@ -261,8 +261,11 @@ struct effsc_prover {
     // effsc_prove: tables of at most this length finish in the one-block tail
     // kernel (SIZE_MAX: as large as shared memory allows; 0: never)
     size_t tail_len = SIZE_MAX;
-    // effsc_prove: InnerProduct rounds 0-2 in two passes (k_ip01.cu)
+    // effsc_prove: InnerProduct rounds 0-2 in two passes (k_ip01.cu);
+    // EqFactored left phase from the inner sums (k_eqf.cu)
     bool fuse_first = true;
+    u64* eqf_scratch = nullptr;               // inner sums, eq weights, partial sums
+    size_t eqf_cap = 0;
 };
 
 namespace {
@@ -590,6 +593,102 @@ int do_fuse_first(effsc_prover* P, const TxIO& tx0, const TxIO& tx2, const u64* 
     return EFFSC_OK;
 }
 
+// effsc_prove of an EqFactored prover whose run covers the whole left phase
+// (num_rounds >= v_l >= 2) with eq_l small enough for the one-block tail: the
+// left rounds are InnerProduct rounds on (eq_l, S), S[a] = sum_b eq_r[b]
+// p[a m + b] (k_eqf.cu).  Leaves the state the per-round path leaves after
+// round v_l - 1: p folded by r_0 .. r_{v_l-2}, eq_l of length 2, eq_r as is.
+bool eqf_fast_ok(const effsc_prover* P, size_t num_rounds) {
+    if (!P->fuse_first || P->kind != EFFSC_EQF || P->rounds != 0) return false;
+    const size_t vl = P->v_l;
+    if (vl < 2 || num_rounds < vl) return false;
+    const Table &p = P->t[0], &el = P->t[1], &er = P->t[2];
+    if (p.cur != 0 || el.cur != 0 || er.cur != 0) return false;
+    if (p.len != ((size_t)1 << P->v) || el.len != ((size_t)1 << vl) || er.len != ((size_t)1 << (P->v - vl))) return false;
+    const int fw = P->field == EFFSC_FP3 ? 3 : 1;
+    return el.len <= (size_t)tail_max_len(POL_IP, fw, TAIL_SMEM_CAP);
+}
+
+int do_eqf_left(effsc_prover* P, const TxIO& tx, bool dry) {
+    const int fw = P->field == EFFSC_FP3 ? 3 : 1;
+    const size_t vl = P->v_l;
+    Table &p = P->t[0], &el = P->t[1], &er = P->t[2];
+    const u64 m = er.len, rows = el.len;
+    const u64 rows2 = (u64)1 << (vl - 1), Lc = p.len >> (vl - 1);
+    const u64 splits = rows2 < 64 ? rows2 : 64;
+    cudaStream_t s = P->ctx->stream;
+    const size_t need = 3 * rows + 3 * rows2 + 3 * splits * Lc;
+    if (P->eqf_cap < need) {
+        if (P->eqf_scratch) CK(cudaFreeAsync(P->eqf_scratch, s));
+        P->eqf_scratch = nullptr;
+        CK(cudaMallocAsync((void**)&P->eqf_scratch, need * sizeof(u64), s));
+        P->eqf_cap = need;
+    }
+    u64* S = P->eqf_scratch;
+    u64* Ew = S + 3 * rows;
+    u64* part = Ew + 3 * rows2;
+    const bool out_ext = fw == 3;
+    int bp, be;
+    TRY(out_buffer(P, p, p.ext || out_ext, Lc, true, &bp));
+    TRY(out_buffer(P, el, el.ext || out_ext, 2, true, &be));
+    if (!dry) {
+        Tab3 tp, ter, te;
+        for (int c = 0; c < 3; c++) {
+            tp.c[c] = p.bufs[p.cur].p[c];
+            ter.c[c] = er.bufs[er.cur].p[c];
+        }
+        u64* s1 = fw == 3 ? S + rows : nullptr;
+        u64* s2 = fw == 3 ? S + 2 * rows : nullptr;
+        const uint64_t b1 = p.len * wbytes(p.ext) + m * wbytes(er.ext) + rows * wbytes(out_ext);
+        TRY(timed_launch(s, "eqf_inner_sums", b1, [&] {
+            launch_eqf_inner(er.ext, p.ext, tp, ter, m, rows, S, s1, s2, s);
+            return true;
+        }));
+        TailArgs ta;
+        memset(&ta, 0, sizeof ta);
+        for (int c = 0; c < 3; c++) ta.in[0][c] = el.bufs[el.cur].p[c];
+        if (el.ext) ta.in_ext |= 1u;
+        ta.in[1][0] = S;
+        ta.in[1][1] = s1;
+        ta.in[1][2] = s2;
+        if (fw == 3) ta.in_ext |= 2u;
+        for (int c = 0; c < 3; c++) ta.out[0][c] = el.bufs[be].p[c];
+        ta.out[1][0] = S;
+        ta.out[1][1] = s1;
+        ta.out[1][2] = s2;
+        ta.L = rows;
+        ta.nrounds = (u32)vl;
+        ta.first_fold = 0;
+        ta.tx = tx.tx;
+        ta.hook = tx.hook;
+        ta.hook_len = tx.hook_len;
+        ta.proof_wire = tx.proof_wire;
+        ta.proof_chal = tx.proof_chal;
+        TRY(timed_launch(s, "tail", 2 * rows * wbytes(out_ext), [&] { return launch_tail(POL_IP, fw, nullptr, &ta, 1, rows, s); }));
+        // eq weights of r_0 .. r_{v_l-2} (MSB order), then the weighted row sum of p
+        launch_build_eq(P->d_chals, (u32)(vl - 1), fw == 3, Ew, Ew + rows2, Ew + 2 * rows2, s);
+        g_launches++;
+        te.c[0] = Ew;
+        te.c[1] = fw == 3 ? Ew + rows2 : nullptr;
+        te.c[2] = fw == 3 ? Ew + 2 * rows2 : nullptr;
+        const Buf& ob = p.bufs[bp];
+        const uint64_t b2 = p.len * wbytes(p.ext) + Lc * wbytes(p.ext || out_ext) + 2 * splits * Lc * 24;
+        TRY(timed_launch(s, "eqf_fold_left", b2, [&] {
+            launch_eqf_fold_rows(fw == 3, p.ext, tp, te, Lc, rows2, splits, part, fw, ob.p[0], ob.p[1], ob.p[2], s);
+            return true;
+        }));
+        g_launches++;   // the sum over row groups
+    }
+    p.cur = bp;
+    p.len = Lc;
+    p.ext = p.ext || out_ext;
+    el.cur = be;
+    el.len = 2;
+    el.ext = el.ext || out_ext;
+    P->rounds = vl;
+    return EFFSC_OK;
+}
+
 // One round of EqFactoredProver (src/provers/eq_factored.rs:249-270).
 int round_eqf(effsc_prover* P, const Chal& ch, const TxIO& tx, bool dry) {
     Table &p = P->t[0], &el = P->t[1], &er = P->t[2];
@@ -872,6 +971,7 @@ void release_prover(effsc_prover* P) {
         if (P->d_hook) cudaFreeAsync(P->d_hook, s);
         if (P->d_wire) cudaFreeAsync(P->d_wire, s);
         if (P->d_chals) cudaFreeAsync(P->d_chals, s);
+        if (P->eqf_scratch) cudaFreeAsync(P->eqf_scratch, s);
         if (P->gexec) cudaGraphExecDestroy(P->gexec);
         cudaStreamSynchronize(s);
     }
@@ -1283,6 +1383,16 @@ int effsc_prove(effsc_prover* P, size_t num_rounds, effsc_transcript* T, const u
             t2.proof_chal = P->d_chals + 3 * 2;
             TRY(do_fuse_first(P, t0, t2, P->d_chals, dry));
             r0 = 3;
+        } else if (eqf_fast_ok(P, num_rounds)) {
+            TxIO t0;
+            memset(&t0, 0, sizeof t0);
+            t0.tx = P->d_tx;
+            t0.hook = P->d_hook;
+            t0.hook_len = (u32)hook_len;
+            t0.proof_wire = P->d_wire;
+            t0.proof_chal = P->d_chals;
+            TRY(do_eqf_left(P, t0, dry));
+            r0 = P->v_l;
         }
         for (size_t r = r0; r < num_rounds; r++) {
             Chal ch;

@@ -76,3 +76,32 @@ def test_default_path_large(E):
     rp, ch, fv = O.sumcheck(O.Prover(O.IP, O.MSB, 3, [a, b]), n, O.Transcript(3, label=b"big"))
     assert np.array_equal(x.round_polys, rp)
     assert np.array_equal(x.final_value, fv)
+
+
+@pytest.mark.parametrize("v", [4, 5, 9, 12, 15])
+@pytest.mark.parametrize("extra", [0, 1, 99])
+@pytest.mark.parametrize("field", [1, 3])
+def test_eq_factored_left_phase_from_inner_sums(E, v, extra, field):
+    """EqFactored runs that cover the left phase: the left rounds as
+    InnerProduct rounds on (eq_l, inner sums) and p folded by the left
+    challenges in one weighted pass give the per-round path's proof and
+    post-state tables, and the oracle's."""
+    rounds = min(v, v // 2 + extra)
+    g = np.random.default_rng(300 + v + extra + field)
+    w = g.integers(0, O.P, size=(v, 3) if field == 3 else v, dtype=np.uint64)
+    p = g.integers(0, O.P, size=1 << v, dtype=np.uint64)
+    fast = E.EqFactoredProver(w, p, field=field)
+    slow = E.EqFactoredProver(w, p, field=field)
+    slow.set_first_rounds(False)
+    hook = bytes(range(32))
+    x = fast.prove(rounds, E.Transcript.keccak(field, b"eqf"), hook=hook)
+    y = slow.prove(rounds, E.Transcript.keccak(field, b"eqf"), hook=hook)
+    assert np.array_equal(x.round_polys, y.round_polys)
+    assert np.array_equal(x.challenges, y.challenges)
+    assert np.array_equal(x.final_value, y.final_value)
+    for t in range(3):
+        assert np.array_equal(fast.table(t), slow.table(t))
+    w3 = O.as_table(w)
+    rp, ch, fv = O.sumcheck(O.Prover.eq_factored(field, w3, p), rounds, O.Transcript(field, label=b"eqf"), hook=hook)
+    assert np.array_equal(np.asarray(x.round_polys).reshape(rounds, 2, field), rp[:, :, :field])
+    assert np.array_equal(np.asarray(x.final_value).reshape(field), fv[:field])

@@ -121,7 +121,7 @@ def test_device_path_matches_oracle(E, kind, order, n, use_graph):
     check_proof(proof2, field, rp, ch, fv)
 
 
-@pytest.mark.parametrize("v", [0, 1, 2, 3, 4, 5, 8, 13])
+@pytest.mark.parametrize("v", [0, 1, 2, 3, 4, 5, 8, 13, 16, 17, 19])
 @pytest.mark.parametrize("field", [1, 3])
 @pytest.mark.parametrize("device_path", [False, True])
 def test_eq_factored_matches_oracle(E, v, field, device_path):
