@@ -356,6 +356,33 @@ or_prover* or_eqf_new(int deg, const uint64_t* w, size_t v, const uint64_t* pv, 
     return p;
 }
 
+/* GkrProver::new, src/provers/gkr.rs:61-82: w_b[b n + c] = W(b),
+ * w_c[b n + c] = W(c); the gate tables must have n*n entries (assert). */
+or_prover* or_gkr_new(int deg, const uint64_t* add, const uint64_t* mult, const uint64_t* w, size_t n, int ncomp) {
+    or_prover* p = (or_prover*)calloc(1, sizeof(or_prover));
+    p->kind = OR_GKR; p->order = OR_MSB; p->deg = deg; p->ntab = 4;
+    size_t nbc = n * n;
+    p->t[0] = load_table(add, nbc, ncomp);
+    p->t[1] = load_table(mult, nbc, ncomp);
+    or_f* wf = load_table(w, n, ncomp);
+    p->t[2] = (or_f*)malloc(sizeof(or_f) * (nbc ? nbc : 1));
+    p->t[3] = (or_f*)malloc(sizeof(or_f) * (nbc ? nbc : 1));
+    for (size_t b = 0; b < n; b++)
+        for (size_t c = 0; c < n; c++) {
+            p->t[2][b * n + c] = wf[b];
+            p->t[3][b * n + c] = wf[c];
+        }
+    for (int i = 0; i < 4; i++) p->len[i] = nbc;
+    free(wf);
+    return p;
+}
+void or_gkr_claimed_w_values(const or_prover* p, uint64_t* out) {
+    or_f wb = F_ZERO, wc = F_ZERO;
+    if (p->len[2] == 1) { wb = p->t[2][0]; wc = p->t[3][0]; }
+    f_store(out, wb);
+    f_store(out + 3, wc);
+}
+
 void or_prover_free(or_prover* p) {
     if (!p) return;
     for (int i = 0; i < 4; i++) free(p->t[i]);
@@ -526,6 +553,43 @@ static void eqf_right(const or_prover* p, or_f* q0o, or_f* qio) {
     *q0o = f_mul(q0, scalar); *qio = f_mul(qi, scalar);
 }
 
+/* GkrProver::round's sums, src/provers/gkr.rs:105-190:
+ *   f(x) = add(x) (W_b(x) + W_c(x)) + mult(x) W_b(x) W_c(x)
+ * at x = 0, 1, 2 over the pairs (i, i + half), the unpaired tail with an
+ * implicit zero hi, then q(inf) = (q(0) + q(2) - 2 q(1)) / 2; a table of at
+ * most one entry gives [f, 0]. */
+static or_f gkr_term(or_f a, or_f m, or_f wb, or_f wc) {
+    return f_add(f_mul(a, f_add(wb, wc)), f_mul(m, f_mul(wb, wc)));
+}
+static void gkr_compute(const or_prover* p, or_f* q0o, or_f* qio) {
+    const size_t n = p->len[0];
+    const or_f *A = p->t[0], *M = p->t[1], *WB = p->t[2], *WC = p->t[3];
+    if (n <= 1) {
+        *q0o = n == 1 ? gkr_term(A[0], M[0], WB[0], WC[0]) : F_ZERO;
+        *qio = F_ZERO;
+        return;
+    }
+    const size_t half = next_pow2(n) >> 1, paired = n - half;
+    or_f q0 = F_ZERO, q1 = F_ZERO, q2 = F_ZERO;
+    for (size_t i = 0; i < paired; i++) {
+        const or_f al = A[i], ah = A[i + half], ml = M[i], mh = M[i + half];
+        const or_f wbl = WB[i], wbh = WB[i + half], wcl = WC[i], wch = WC[i + half];
+        q0 = f_add(q0, gkr_term(al, ml, wbl, wcl));
+        q1 = f_add(q1, gkr_term(ah, mh, wbh, wch));
+        const or_f a2 = f_sub(f_add(ah, ah), al), m2 = f_sub(f_add(mh, mh), ml);
+        const or_f wb2 = f_sub(f_add(wbh, wbh), wbl), wc2 = f_sub(f_add(wch, wch), wcl);
+        q2 = f_add(q2, gkr_term(a2, m2, wb2, wc2));
+    }
+    for (size_t i = paired; i < half && i < n; i++) {
+        const or_f al = A[i], ml = M[i], wbl = WB[i], wcl = WC[i];
+        q0 = f_add(q0, gkr_term(al, ml, wbl, wcl));
+        q2 = f_add(q2, f_sub(f_mul(al, f_add(wbl, wcl)), f_mul(ml, f_mul(wbl, wcl))));
+    }
+    const or_f inv2 = f_from_u64((OR_P + 1) / 2);
+    *q0o = q0;
+    *qio = f_mul(f_sub(f_add(q0, q2), f_add(q1, q1)), inv2);
+}
+
 /* SumcheckProver::round for every prover (EvalsInfty wire,
  * src/sumcheck_prover.rs:40-59). */
 int or_prover_round(or_prover* p, const uint64_t* chal, uint64_t* out, uint64_t* aux) {
@@ -579,6 +643,12 @@ int or_prover_round(or_prover* p, const uint64_t* chal, uint64_t* out, uint64_t*
         f_store(out, r0); f_store(out + 3, r1);
         break;
     }
+    case OR_GKR:  /* src/provers/gkr.rs:105-190 */
+        if (chal)
+            for (int i = 0; i < 4; i++) fold_msb_pad(p->t[i], &p->len[i], w);
+        gkr_compute(p, &r0, &r1);
+        f_store(out, r0); f_store(out + 3, r1);
+        break;
     default: return -1;
     }
     if (aux) { f_store(aux, r0); f_store(aux + 3, r1); }
@@ -600,6 +670,9 @@ void or_prover_finalize(or_prover* p, const uint64_t* chal) {
         break;
     case OR_COEF:
         coef_reduce(p, w);
+        break;
+    case OR_GKR:   /* src/provers/gkr.rs:193-198 */
+        for (int i = 0; i < 4; i++) fold_msb_pad(p->t[i], &p->len[i], w);
         break;
     case OR_EQF: { /* src/provers/eq_factored.rs:272-280: last_var = v - 1 (wrapping) */
         size_t last_var = p->v - 1;
@@ -634,6 +707,9 @@ void or_prover_final_value(const or_prover* p, uint64_t* out) {
     }
     case OR_EQF:  /* src/provers/eq_factored.rs:282-288 */
         if (p->len[0] == 1) r = f_mul(f_mul(p->t[0][0], p->t[1][0]), p->t[2][0]);
+        break;
+    case OR_GKR:  /* src/provers/gkr.rs:200-208 */
+        if (p->len[0] == 1) r = gkr_term(p->t[0][0], p->t[1][0], p->t[2][0], p->t[3][0]);
         break;
     }
     f_store(out, r);

@@ -75,7 +75,7 @@ void or_transcript_challenge(or_transcript* t, uint64_t* out);
 size_t or_transcript_size(void);
 
 /* ---- provers --------------------------------------------------------------- */
-enum { OR_ML = 0, OR_IP = 1, OR_COEF = 2, OR_EQF = 3 };
+enum { OR_ML = 0, OR_IP = 1, OR_COEF = 2, OR_EQF = 3, OR_GKR = 4 };
 enum { OR_MSB = 0, OR_LSB = 1 };
 
 typedef struct {
@@ -84,6 +84,7 @@ typedef struct {
     size_t len[4];
     or_f* t[4];          /* EQF: t[0] = p, t[1] = eq_l, t[2] = eq_r       */
     int coef_deg;        /* COEF: degree of the product evaluator (ntab)  */
+                         /* GKR: t = add, mult, w_b, w_c (broadcast)      */
     size_t v, v_l, rounds_elapsed;
     int error;           /* set when the reference would panic            */
 } or_prover;
@@ -92,6 +93,11 @@ typedef struct {
 or_prover* or_prover_new(int kind, int order, int deg, int ntab,
                          const uint64_t* const* tables, const size_t* lens, int ncomp);
 or_prover* or_eqf_new(int deg, const uint64_t* w, size_t v, const uint64_t* p, size_t plen, int ncomp);
+/* GkrProver::new (src/provers/gkr.rs:61-82): add, mult of n*n elements, w of
+ * n elements; the witness is expanded into the broadcast tables w_b, w_c. */
+or_prover* or_gkr_new(int deg, const uint64_t* add, const uint64_t* mult, const uint64_t* w, size_t n, int ncomp);
+/* GkrProver::claimed_w_values (src/provers/gkr.rs:87-93): out = 2 elements. */
+void or_gkr_claimed_w_values(const or_prover* p, uint64_t* out);
 void or_prover_free(or_prover* p);
 int  or_prover_degree(const or_prover* p);
 /* out: `degree` elements (wire, EvalsInfty).  aux (optional): the two raw

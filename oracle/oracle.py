@@ -17,7 +17,7 @@ from . import build_oracle
 
 _lib = None
 
-ML, IP, COEF, EQF = 0, 1, 2, 3
+ML, IP, COEF, EQF, GKR = 0, 1, 2, 3, 4
 MSB, LSB = 0, 1
 P = 0xFFFFFFFF00000001
 W = 0xFFFFFFF800000001
@@ -64,6 +64,9 @@ def lib():
                                     ctypes.POINTER(_u64p), ctypes.POINTER(ctypes.c_size_t), ctypes.c_int]
         L.or_eqf_new.restype = ctypes.c_void_p
         L.or_eqf_new.argtypes = [ctypes.c_int, _u64p, ctypes.c_size_t, _u64p, ctypes.c_size_t, ctypes.c_int]
+        L.or_gkr_new.restype = ctypes.c_void_p
+        L.or_gkr_new.argtypes = [ctypes.c_int, _u64p, _u64p, _u64p, ctypes.c_size_t, ctypes.c_int]
+        L.or_gkr_claimed_w_values.argtypes = [ctypes.c_void_p, _u64p]
         L.or_prover_free.argtypes = [ctypes.c_void_p]
         L.or_prover_degree.restype = ctypes.c_int
         L.or_prover_degree.argtypes = [ctypes.c_void_p]
@@ -210,6 +213,24 @@ class Prover:
         h = lib().or_eqf_new(deg, _p(w), w.shape[0], _p(p), p.shape[0], ncomp)
         obj = cls(EQF, MSB, deg, None, _handle=h)
         return obj
+
+    @classmethod
+    def gkr(cls, deg, add, mult, w):
+        """GkrProver (src/provers/gkr.rs): add, mult of n*n, w of n elements."""
+        raw = [np.asarray(t, dtype=np.uint64) for t in (add, mult, w)]
+        if all(r.ndim == 1 for r in raw):
+            arrs, ncomp = [np.ascontiguousarray(r) for r in raw], 1
+        else:
+            arrs, ncomp = [as_table(r) for r in raw], 3
+        h = lib().or_gkr_new(deg, _p(arrs[0]), _p(arrs[1]), _p(arrs[2]), arrs[2].shape[0], ncomp)
+        obj = cls(GKR, MSB, deg, None, _handle=h)
+        obj._keep = arrs
+        return obj
+
+    def claimed_w_values(self):
+        out = np.zeros((2, 3), dtype=np.uint64)
+        lib().or_gkr_claimed_w_values(self.h, _p(out))
+        return out
 
     def __del__(self):
         if getattr(self, "h", None):

@@ -281,3 +281,43 @@ def mle_eval_msb(table, point):
         h = len(cur) // 2
         cur = [add(cur[i], mul(sub(cur[i + h], cur[i]), r)) for i in range(h)]
     return cur[0]
+
+
+class RefGkr:
+    """GkrProver (src/provers/gkr.rs): broadcast witness tables, every round
+    folds all four tables and returns [q(0), (q(0) + q(2) - 2 q(1)) / 2]."""
+
+    def __init__(self, add_, mult_, w):
+        n = len(w)
+        self.t = [list(add_), list(mult_), [w[b] for b in range(n) for _ in range(n)],
+                  [w[c] for _ in range(n) for c in range(n)]]
+
+    @staticmethod
+    def term(a, m, wb, wc):
+        return add(mul(a, add(wb, wc)), mul(m, mul(wb, wc)))
+
+    def round(self, r=None):
+        if r is not None:
+            self.t = [fold_msb_pad(t, r) for t in self.t]
+        A, M, B, C = self.t
+        n = len(A)
+        if n <= 1:
+            return [self.term(A[0], M[0], B[0], C[0]) if n == 1 else ZERO, ZERO]
+        h = np2(n) >> 1
+        q = [ZERO, ZERO, ZERO]
+        for i in range(h):
+            lo = (A[i], M[i], B[i], C[i])
+            hi = (A[i + h], M[i + h], B[i + h], C[i + h]) if i + h < n else (ZERO,) * 4
+            for x in range(3):
+                pt = [add(lo[j], mul(lift(x), sub(hi[j], lo[j]))) for j in range(4)]
+                q[x] = add(q[x], self.term(*pt))
+        inv2 = lift((P + 1) // 2)
+        return [q[0], mul(sub(add(q[0], q[2]), add(q[1], q[1])), inv2)]
+
+    def finalize(self, r):
+        self.t = [fold_msb_pad(t, r) for t in self.t]
+
+    def final_value(self):
+        A, M, B, C = self.t
+        return self.term(A[0], M[0], B[0], C[0]) if len(A) == 1 else ZERO
+

@@ -372,3 +372,79 @@ def test_legacy_ml_sends_s0_s1():
         assert R.add(tup(rp[r, 0]), tup(rp[r, 1])) == (
             R.add(s0, s1) if r == 0 else
             R.add(tup(rp[r - 1, 0]), R.mul(tup(ch[r - 1]), R.sub(tup(rp[r - 1, 1]), tup(rp[r - 1, 0])))))
+
+
+# ------------------------------------------------------------- GKR -----------
+def gkr_inputs(rng, k, ext=False, zero_mult=False, zero_all=False):
+    n = 1 << k
+    add_ = [R.ZERO if zero_all else rnd_f(rng, ext) for _ in range(n * n)]
+    mult_ = [R.ZERO if (zero_mult or zero_all) else rnd_f(rng, ext) for _ in range(n * n)]
+    w = [rnd_f(rng, ext) for _ in range(n)]
+    return add_, mult_, w
+
+
+@pytest.mark.parametrize("k", [0, 1, 2, 3])
+@pytest.mark.parametrize("ext", [False, True])
+@pytest.mark.parametrize("extra", [0, -1, 1])
+def test_gkr_rounds_match_bigint(k, ext, extra):
+    """src/provers/gkr.rs round by round (full, partial and one extra round)."""
+    rng = random.Random(50 + 10 * k + ext + 3 * extra)
+    add_, mult_, w = gkr_inputs(rng, k, ext)
+    ref = R.RefGkr(add_, mult_, w)
+    pr = O.Prover.gkr(3, to_np(add_), to_np(mult_), to_np(w))
+    rounds = max(0, 2 * k + extra)
+    r = None
+    for j in range(rounds):
+        want = ref.round(r)
+        got = pr.round(None if r is None else to_np([r])[0])
+        assert [tup(x) for x in got] == want, j
+        r = rnd_f(rng)
+    if rounds:
+        ref.finalize(r)
+        pr.finalize(to_np([r])[0])
+        assert tup(pr.final_value()) == ref.final_value()
+
+
+@pytest.mark.parametrize("k", [1, 2, 3, 4])
+def test_gkr_verifies_and_claimed_w_values(k):
+    """The reference's run_gkr_test (src/provers/gkr.rs:215-272): the proof
+    verifies against the direct sum, the final claim equals final_value, and
+    claimed_w_values are W's multilinear extension at the b and c challenges."""
+    rng = random.Random(k)
+    add_, mult_, w = gkr_inputs(rng, k)
+    n = 1 << k
+    s = R.ZERO
+    for b in range(n):
+        for c in range(n):
+            s = R.add(s, R.RefGkr.term(add_[b * n + c], mult_[b * n + c], w[b], w[c]))
+    pr = O.Prover.gkr(1, np.array([x[0] for x in add_], np.uint64), np.array([x[0] for x in mult_], np.uint64),
+                      np.array([x[0] for x in w], np.uint64))
+    rp, ch, fv = O.sumcheck(pr, 2 * k, O.Transcript(1, label=b"gkr"))
+    _, fc = O.verify(s, 2, 2 * k, O.Transcript(1, label=b"gkr"), rp)
+    assert (fc == fv).all()
+    wv = pr.claimed_w_values()
+    pts = [tup(c) for c in ch]
+    assert tup(wv[0]) == R.mle_eval_msb(w, pts[:k])
+    assert tup(wv[1]) == R.mle_eval_msb(w, pts[k:])
+
+
+def test_gkr_zero_gates_and_add_only():
+    """src/provers/gkr.rs:281-345: zero gates give all-zero round polynomials;
+    add-only circuits still prove the add sum."""
+    rng = random.Random(99)
+    k = 2
+    add_, mult_, w = gkr_inputs(rng, k, zero_all=True)
+    pr = O.Prover.gkr(3, to_np(add_), to_np(mult_), to_np(w))
+    rp, _, _ = O.sumcheck(pr, 2 * k, O.Transcript(3, label=b"z"))
+    assert not rp.any()
+    add_, mult_, w = gkr_inputs(rng, k, zero_mult=True)
+    n = 1 << k
+    s = R.ZERO
+    for b in range(n):
+        for c in range(n):
+            s = R.add(s, R.mul(add_[b * n + c], R.add(w[b], w[c])))
+    pr = O.Prover.gkr(3, to_np(add_), to_np(mult_), to_np(w))
+    rp, ch, fv = O.sumcheck(pr, 2 * k, O.Transcript(3, label=b"a"))
+    _, fc = O.verify(s, 2, 2 * k, O.Transcript(3, label=b"a"), rp)
+    assert (fc == fv).all()
+
