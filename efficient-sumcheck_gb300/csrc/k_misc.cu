@@ -21,12 +21,13 @@ int pol_ntables(int pol) {
     switch (pol) {
     case POL_ML: case POL_C1: return 1;
     case POL_C3: case POL_EQFL: return 3;
+    case POL_GKR: return 4;
     default: return 2;
     }
 }
 int pol_nraw(int pol) {
     switch (pol) {
-    case POL_C2: return 3;
+    case POL_C2: case POL_GKR: return 3;
     case POL_C3: return 4;
     default: return 2;
     }

@@ -29,7 +29,12 @@ enum Sem { SEM_MSB_PAD = 0, SEM_MSB_FLOOR = 1, SEM_LSB = 2 };
 //  POL_EQFR: POL_IP on (eq_r, p), times the scalar eq_l[0]  (2 tables)
 //  POL_IP01: InnerProduct rounds 0 and 1 from one pass over the base tables
 //            (eight base-field sums, two transcript steps)
-enum Pol { POL_ML = 0, POL_IP = 1, POL_C1 = 2, POL_C2 = 3, POL_C3 = 4, POL_EQFR = 5, POL_EQFL = 6, POL_IP01 = 7 };
+//  POL_GKR : GkrProver, q(0), q(1), q(2) of add (W_b + W_c) + mult W_b W_c;
+//            the wire is [q(0), (q(0) + q(2) - 2 q(1)) / 2]
+enum Pol {
+    POL_ML = 0, POL_IP = 1, POL_C1 = 2, POL_C2 = 3, POL_C3 = 4, POL_EQFR = 5, POL_EQFL = 6, POL_IP01 = 7,
+    POL_GKR = 8
+};
 
 struct TabIO {
     const u64* in[3];   // SoA component arrays; [1],[2] null for base tables
@@ -47,9 +52,9 @@ struct TxIO {
 };
 
 struct RoundArgs {
-    TabIO t[3];
+    TabIO t[4];
     u64 L;                 // length before folding (fold/fused) or current length (eval)
-    u32 m_shift;           // EqFactored left phase: log2 |eq_r|
+    u32 m_shift;           // EqFactored left phase: log2 |eq_r|; GkrProver: k = log2 |W|
     u64 el_len;            // EqFactored left phase: current |eq_l|
     const u64* chal_ptr;   // challenge in device memory, or null to use `chal`
     const u64* chal2_ptr;  // second challenge (InnerProduct double fold of round 2)
@@ -130,6 +135,12 @@ bool launch_eqf_left(bool fused, u32 mask, bool ech, const RoundArgs& a, int gri
 // if no kernel is instantiated for the combination.
 bool launch_fused_tma(int pol, u32 mask, bool ech, const RoundArgs& a, u32 ntiles, int grid, cudaStream_t s);
 int fused_tma_blocks_per_sm(void);
+// GkrProver round: t[0] = add, t[1] = mult (both Fp3 when ea), t[2] = W_b,
+// t[3] = W_c (Fp3 when ew; the compact witness tables of 2^(k - bound b
+// variables) and 2^(k - bound c variables) entries).  fused: fold add and
+// mult with the challenge (L a power of two >= 4) and evaluate the folded
+// tables; otherwise evaluate the current ones.
+bool launch_gkr(bool fused, bool ea, bool ew, bool ech, const RoundArgs& a, int grid, cudaStream_t s);
 // InnerProduct MSB over Fp3 challenges, base tables of length L = 2^n >= 8:
 // rounds 0 and 1 from one read of the tables (launch_ip01), then round 2's
 // fold-twice-and-evaluate from a second read (launch_ip2x).

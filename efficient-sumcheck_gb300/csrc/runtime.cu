@@ -237,10 +237,11 @@ struct effsc_prover {
     effsc_ctx* ctx = nullptr;
     int kind = 0, order = 0, field = 1, repr = 0;
     int ntab = 0;
-    Table t[3];
+    Table t[4];                                // GkrProver: add, mult, W_b, W_c
     size_t v = 0, v_l = 0, rounds = 0;        // EqFactored: t[0] = p, t[1] = eq_l, t[2] = eq_r
-    size_t len0[3] = {0, 0, 0};
-    bool ext0[3] = {false, false, false};
+                                               // GkrProver: v = 2k, v_l = k
+    size_t len0[4] = {0, 0, 0, 0};
+    bool ext0[4] = {false, false, false, false};
     u64* partials = nullptr;
     u32* counter = nullptr;
     u32* status = nullptr;
@@ -256,7 +257,7 @@ struct effsc_prover {
     cudaGraphExec_t gexec = nullptr;
     size_t g_rounds = 0, g_hook = 0;
     uint64_t g_kernels = 0;                    // kernel nodes in the graph
-    TabState g_post[3];
+    TabState g_post[4];
     size_t g_post_rounds = 0;
     // effsc_prove: tables of at most this length finish in the one-block tail
     // kernel (SIZE_MAX: as large as shared memory allows; 0: never)
@@ -282,6 +283,7 @@ int pol_of(const effsc_prover* p) {
     case EFFSC_ML: return POL_ML;
     case EFFSC_IP: return POL_IP;
     case EFFSC_COEF: return p->ntab == 1 ? POL_C1 : p->ntab == 2 ? POL_C2 : POL_C3;
+    case EFFSC_GKR: return POL_GKR;
     default: return POL_EQFR;
     }
 }
@@ -783,7 +785,59 @@ int check_status(effsc_prover* P) {
     return fail(EFFSC_TIMEOUT, "a round kernel timed out waiting for its staged loads (status %u)", v);
 }
 
+// One round of GkrProver (src/provers/gkr.rs:105-190) on the compact witness
+// tables (k_gkr.cu): fold W_b when the variable just bound is a b variable
+// (the first k), else W_c; fold add and mult fused with the evaluation.
+int round_gkr(effsc_prover* P, const Chal& ch, const TxIO& tx, bool dry) {
+    Table &A = P->t[0], &M = P->t[1], &WB = P->t[2], &WC = P->t[3];
+    RoundArgs a = base_args(P);
+    a.tx = tx;
+    put_chal(a, ch);
+    a.m_shift = (u32)P->v_l;
+    bool fused = false;
+    bool ech = false;
+    if (ch.has) {
+        const size_t prev_var = P->rounds - 1;   // wraps like the reference's release build
+        ech = ch.ext || A.ext || M.ext || WB.ext || WC.ext;
+        TRY(fold_table(P, prev_var < P->v_l ? 2 : 3, SEM_MSB_PAD, ch, ech, dry));
+        const size_t L = A.len;
+        if (is_pow2(L) && L >= 4) {
+            fused = true;
+        } else {
+            TRY(fold_table(P, 0, SEM_MSB_PAD, ch, ech, dry));
+            TRY(fold_table(P, 1, SEM_MSB_PAD, ch, ech, dry));
+        }
+    }
+    const size_t L = A.len;
+    for (int i = 0; i < 4; i++) set_in(a, i, P->t[i]);
+    a.L = L;
+    int bi[2] = {0, 0};
+    const bool ea = A.ext;
+    if (fused)
+        for (int i = 0; i < 2; i++) {
+            TRY(out_buffer(P, P->t[i], P->t[i].ext || ech, L / 2, true, &bi[i]));
+            set_out(a, i, P->t[i].bufs[bi[i]]);
+        }
+    const bool ew = WB.ext;
+    const u64 Ln = fused ? L / 2 : L;
+    uint64_t bytes = 2 * (L * wbytes(ea) + (fused ? (L / 2) * wbytes(ea || ech) : 0)) +
+                     (WB.len + WC.len) * wbytes(ew);
+    if (!dry) TRY(timed_launch(P->ctx->stream, fused ? "gkr_fused_round" : "gkr_evaluate", bytes, [&] {
+        return launch_gkr(fused, ea, ew, fused && (ech || ea), a, grid_for(Ln > 1 ? Ln / 2 : 1), P->ctx->stream);
+    }));
+    if (fused)
+        for (int i = 0; i < 2; i++) {
+            Table& T = P->t[i];
+            T.cur = bi[i];
+            T.len = L / 2;
+            T.ext = T.ext || ech;
+        }
+    P->rounds++;
+    return EFFSC_OK;
+}
+
 int do_round(effsc_prover* P, const Chal& ch, const TxIO& tx, bool dry) {
+    if (P->kind == EFFSC_GKR) return round_gkr(P, ch, tx, dry);
     return P->kind == EFFSC_EQF ? round_eqf(P, ch, tx, dry) : round_std(P, ch, tx, dry);
 }
 
@@ -795,6 +849,17 @@ int do_finalize(effsc_prover* P, const Chal& ch, bool dry) {
         size_t last_var = P->v - 1;
         TRY(fold_table(P, 0, SEM_MSB_PAD, ch, ech, dry));
         TRY(fold_table(P, last_var < P->v_l ? 1 : 2, SEM_MSB_PAD, ch, ech, dry));
+        return EFFSC_OK;
+    }
+    if (P->kind == EFFSC_GKR) {
+        // src/provers/gkr.rs:193-198 folds all four tables; with the compact
+        // witness only the table of the variable being bound changes
+        bool ech = ch.ext;
+        for (int i = 0; i < 4; i++) ech |= P->t[i].ext;
+        const size_t last_var = P->rounds - 1;
+        TRY(fold_table(P, 0, SEM_MSB_PAD, ch, ech, dry));
+        TRY(fold_table(P, 1, SEM_MSB_PAD, ch, ech, dry));
+        TRY(fold_table(P, last_var < P->v_l ? 2 : 3, SEM_MSB_PAD, ch, ech, dry));
         return EFFSC_OK;
     }
     bool ech = ch.ext;
@@ -840,6 +905,16 @@ int final_value(effsc_prover* P, HF* out) {
         }
         // coefficients c(x) = prod (x_i - x x_i): h(0) = prod x_i, h(1) = 0
         *out = acc;
+        return EFFSC_OK;
+    }
+    case EFFSC_GKR: { // src/provers/gkr.rs:200-208
+        if (P->t[0].len != 1) return EFFSC_OK;
+        HF a, m, wb, wc;
+        TRY(read_first(P, 0, &a));
+        TRY(read_first(P, 1, &m));
+        TRY(read_first(P, 2, &wb));
+        TRY(read_first(P, 3, &wc));
+        *out = hf_add(hf_mul(a, hf_add(wb, wc)), hf_mul(m, hf_mul(wb, wc)));
         return EFFSC_OK;
     }
     default: {       // src/provers/eq_factored.rs:282-288
@@ -935,6 +1010,13 @@ int promote(effsc_prover* P, Table& T) {
 // tables are promoted except the (Fp3, base, base) CoefficientProver shape
 // (eq(r, x) * f * g with base f, g).
 int normalize_masks(effsc_prover* P) {
+    if (P->kind == EFFSC_GKR) {
+        // the witness tables are Fp3 whenever the challenges are; add and
+        // mult share one representation
+        if (P->field == EFFSC_FP3 || P->t[2].ext) { TRY(promote(P, P->t[2])); TRY(promote(P, P->t[3])); }
+        if (P->t[0].ext != P->t[1].ext) { TRY(promote(P, P->t[0])); TRY(promote(P, P->t[1])); }
+        return EFFSC_OK;
+    }
     if (P->kind == EFFSC_EQF) {
         if (P->field == EFFSC_FP3 || P->t[0].ext) { TRY(promote(P, P->t[1])); TRY(promote(P, P->t[2])); }
         return EFFSC_OK;
@@ -949,7 +1031,7 @@ int normalize_masks(effsc_prover* P) {
 }
 
 void snapshot_initial(effsc_prover* P) {
-    for (int i = 0; i < 3; i++) { P->len0[i] = P->t[i].len; P->ext0[i] = P->t[i].ext; }
+    for (int i = 0; i < 4; i++) { P->len0[i] = P->t[i].len; P->ext0[i] = P->t[i].ext; }
 }
 
 int check_field(int field) {
@@ -962,7 +1044,7 @@ void release_prover(effsc_prover* P) {
     if (P->ctx) {
         cudaSetDevice(P->ctx->device);
         cudaStreamSynchronize(P->ctx->stream);
-        for (int i = 0; i < 3; i++)
+        for (int i = 0; i < 4; i++)
             for (auto& b : P->t[i].bufs) free_buf(P, b);
         cudaStream_t s = P->ctx->stream;
         if (P->partials) cudaFreeAsync(P->partials, s);
@@ -1173,6 +1255,47 @@ int effsc_prover_create_device(effsc_ctx* ctx, int kind, int order, int field, i
     return EFFSC_OK;
 }
 
+int effsc_gkr_create(effsc_ctx* ctx, int field, int repr, const uint64_t* add, const uint64_t* mult, const uint64_t* w,
+                     size_t n, int ncomp, effsc_prover** out) {
+    if (!ctx || !out || !add || !mult || !w) return fail(EFFSC_INVALID_ARG, "NULL argument");
+    TRY(check_field(field));
+    if (ncomp != 1 && ncomp != 3) return fail(EFFSC_INVALID_ARG, "ncomp must be 1 or 3");
+    if (!is_pow2(n) || n > ((size_t)1 << 17))
+        return fail(EFFSC_UNSUPPORTED, "GkrProver on the device needs |w| a power of two up to 2^17 (got %zu)", n);
+    if (ncomp == 3 && field != EFFSC_FP3) return fail(EFFSC_INVALID_ARG, "Fp3 tables for an Fp prover");
+    CK(cudaSetDevice(ctx->device));
+    effsc_prover* P = new effsc_prover();
+    P->ctx = ctx; P->kind = EFFSC_GKR; P->order = EFFSC_MSB; P->field = field; P->repr = repr; P->ntab = 4;
+    size_t k = 0;
+    while (((size_t)1 << k) < n) k++;
+    P->v = 2 * k; P->v_l = k;
+    int rc = prover_common_init(P);
+    if (rc == EFFSC_OK) rc = upload_table(P, P->t[0], add, n * n, ncomp, repr);
+    if (rc == EFFSC_OK) rc = upload_table(P, P->t[1], mult, n * n, ncomp, repr);
+    if (rc == EFFSC_OK) rc = upload_table(P, P->t[2], w, n, ncomp, repr);
+    if (rc == EFFSC_OK) rc = upload_table(P, P->t[3], w, n, ncomp, repr);
+    if (rc == EFFSC_OK) rc = normalize_masks(P);
+    if (rc == EFFSC_OK) { cudaError_t e = cudaStreamSynchronize(ctx->stream); if (e != cudaSuccess) rc = fail(EFFSC_CUDA_ERROR, "%s", cudaGetErrorString(e)); }
+    if (rc != EFFSC_OK) { release_prover(P); return rc; }
+    snapshot_initial(P);
+    *out = P;
+    return EFFSC_OK;
+}
+
+int effsc_gkr_claimed_w_values(effsc_prover* P, uint64_t* out) {
+    if (!P || !out) return fail(EFFSC_INVALID_ARG, "NULL argument");
+    if (P->kind != EFFSC_GKR) return fail(EFFSC_INVALID_ARG, "not a GkrProver");
+    CK(cudaSetDevice(P->ctx->device));
+    HF wb = hf(0), wc = hf(0);
+    if (P->t[0].len == 1) {
+        TRY(read_first(P, 2, &wb));
+        TRY(read_first(P, 3, &wc));
+    }
+    store_elem(out, wb, P->field, P->repr);
+    store_elem(out + P->field, wc, P->field, P->repr);
+    return EFFSC_OK;
+}
+
 int effsc_eqf_create(effsc_ctx* ctx, int field, int repr, const uint64_t* w, size_t num_vars, const uint64_t* pv,
                      size_t p_len, int p_ncomp, effsc_prover** out) {
     if (!ctx || !out || (num_vars && !w) || (p_len && !pv)) return fail(EFFSC_INVALID_ARG, "NULL argument");
@@ -1283,7 +1406,7 @@ int effsc_prover_final_value(effsc_prover* P, uint64_t* out) {
 
 int effsc_prover_table_len(const effsc_prover* P, int table, size_t* out) {
     if (!P || !out) return fail(EFFSC_INVALID_ARG, "NULL argument");
-    int nt = P->kind == EFFSC_EQF ? 3 : P->ntab;
+    int nt = P->kind == EFFSC_EQF ? 3 : P->kind == EFFSC_GKR ? 4 : P->ntab;
     if (table < 0 || table >= nt) return fail(EFFSC_INVALID_ARG, "table index out of range");
     *out = P->t[table].len;
     return EFFSC_OK;
@@ -1325,7 +1448,7 @@ int effsc_prover_set_tail(effsc_prover* P, size_t max_len) {
 
 int effsc_prover_reset(effsc_prover* P) {
     if (!P) return fail(EFFSC_INVALID_ARG, "prover is NULL");
-    for (int i = 0; i < 3; i++) {
+    for (int i = 0; i < 4; i++) {
         if (P->t[i].bufs.empty()) continue;
         P->t[i].cur = 0;
         P->t[i].len = P->len0[i];
@@ -1365,7 +1488,7 @@ int effsc_prove(effsc_prover* P, size_t num_rounds, effsc_transcript* T, const u
     if (hook_len) CK(cudaMemcpyAsync(P->d_hook, hook, hook_len, cudaMemcpyHostToDevice, s));
 
     bool at_reset = P->rounds == 0;
-    for (int i = 0; i < 3; i++)
+    for (int i = 0; i < 4; i++)
         if (!P->t[i].bufs.empty() && (P->t[i].cur != 0 || P->t[i].len != P->len0[i])) at_reset = false;
 
     auto launch_all = [&](bool dry) -> int {
@@ -1421,15 +1544,15 @@ int effsc_prove(effsc_prover* P, size_t num_rounds, effsc_transcript* T, const u
     if (use_graph && at_reset && P->gexec && P->g_rounds == num_rounds && P->g_hook == hook_len) {
         CK(cudaGraphLaunch(P->gexec, s));
         g_launches += P->g_kernels;
-        for (int i = 0; i < 3; i++) { P->t[i].cur = P->g_post[i].cur; P->t[i].len = P->g_post[i].len; P->t[i].ext = P->g_post[i].ext; }
+        for (int i = 0; i < 4; i++) { P->t[i].cur = P->g_post[i].cur; P->t[i].len = P->g_post[i].len; P->t[i].ext = P->g_post[i].ext; }
         P->rounds = P->g_post_rounds;
     } else if (use_graph) {
         // plan once without launching so that every buffer exists before capture
-        TabState pre[3];
-        for (int i = 0; i < 3; i++) pre[i] = {P->t[i].cur, P->t[i].len, P->t[i].ext};
+        TabState pre[4];
+        for (int i = 0; i < 4; i++) pre[i] = {P->t[i].cur, P->t[i].len, P->t[i].ext};
         size_t pre_rounds = P->rounds;
         TRY(launch_all(true));
-        for (int i = 0; i < 3; i++) { P->t[i].cur = pre[i].cur; P->t[i].len = pre[i].len; P->t[i].ext = pre[i].ext; }
+        for (int i = 0; i < 4; i++) { P->t[i].cur = pre[i].cur; P->t[i].len = pre[i].len; P->t[i].ext = pre[i].ext; }
         P->rounds = pre_rounds;
         CK(cudaStreamSynchronize(s));
         cudaGraph_t graph;
@@ -1452,7 +1575,7 @@ int effsc_prove(effsc_prover* P, size_t num_rounds, effsc_transcript* T, const u
             P->gexec = ge;
             P->g_rounds = num_rounds;
             P->g_hook = hook_len;
-            for (int i = 0; i < 3; i++) P->g_post[i] = {P->t[i].cur, P->t[i].len, P->t[i].ext};
+            for (int i = 0; i < 4; i++) P->g_post[i] = {P->t[i].cur, P->t[i].len, P->t[i].ext};
             P->g_post_rounds = P->rounds;
         } else {
             CK(cudaStreamSynchronize(s));

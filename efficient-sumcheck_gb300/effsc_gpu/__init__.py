@@ -5,8 +5,8 @@ this package is its ctypes front end.  See include/effsc_gpu.h for the C ABI.
 """
 from ._lib import EffscError, ReferencePanic, LIB_PATH, load  # noqa: F401
 from .api import (  # noqa: F401
-    CANONICAL, COEF, EQF, FP, FP3, IP, LSB, ML, MONTGOMERY, MSB, T_KECCAK, T_TEST,
-    Batch, CoefficientProver, CoefficientProverLSB, Context, EqFactoredProver, InnerProductProver,
+    CANONICAL, COEF, EQF, FP, FP3, GKR, IP, LSB, ML, MONTGOMERY, MSB, T_KECCAK, T_TEST,
+    Batch, CoefficientProver, GkrProver, CoefficientProverLSB, Context, EqFactoredProver, InnerProductProver,
     InnerProductProverLSB, MultilinearProver, MultilinearProverLSB, ProductSumcheck, Server, Sumcheck,
     SumcheckProof, Transcript, build_eq_table, fold, gen_uniform, inner_product_sumcheck,
     inner_product_sumcheck_partial, launch_count, launch_count_reset, multilinear_sumcheck,

@@ -29,7 +29,7 @@ import numpy as np
 from . import _lib
 from ._lib import check, load, u64p, u8p, vp
 
-ML, IP, COEF, EQF = 0, 1, 2, 3
+ML, IP, COEF, EQF, GKR = 0, 1, 2, 3, 4
 MSB, LSB = 0, 1
 FP, FP3 = 1, 3
 CANONICAL, MONTGOMERY = 0, 1
@@ -357,6 +357,35 @@ class EqFactoredProver(_Prover):
 # ---------------------------------------------------------------------------
 # runner, verifier, free functions
 # ---------------------------------------------------------------------------
+class GkrProver(_Prover):
+    """src/provers/gkr.rs:41-208.  add_evals, mult_evals: n*n elements;
+    w_evals: n elements (n a power of two).  Tables: 0 = add, 1 = mult,
+    2 = W_b, 3 = W_c (the witness, compact)."""
+    kind, order = GKR, MSB
+
+    def __init__(self, add_evals, mult_evals, w_evals, field=FP3, repr=CANONICAL, ctx=None):
+        self.ctx = ctx or Context.default()
+        self.field, self.repr = field, repr
+        arrs = [_as_table(t, field) for t in (add_evals, mult_evals, w_evals)]
+        nc = max(c for _, c in arrs)
+        if nc == 3:
+            arrs = [(a if c == 3 else np.stack([a, np.zeros_like(a), np.zeros_like(a)], axis=1), 3) for a, c in arrs]
+        (ad, _), (mu, _), (w, _) = arrs
+        n = w.shape[0]
+        if ad.shape[0] != n * n or mu.shape[0] != n * n:
+            raise AssertionError("add_evals and mult_evals must have len w^2")   # the reference asserts
+        h = vp()
+        check(load().effsc_gkr_create(self.ctx.h, field, repr, _p(np.ascontiguousarray(ad)),
+                                      _p(np.ascontiguousarray(mu)), _p(np.ascontiguousarray(w)), n, nc,
+                                      ctypes.byref(h)))
+        self.h = h
+
+    def claimed_w_values(self):
+        out = np.zeros((2, self.field), dtype=np.uint64)
+        check(load().effsc_gkr_claimed_w_values(self.h, _p(out)))
+        return out
+
+
 def sumcheck(prover, num_rounds, transcript, hook=None):
     """runner::sumcheck (src/runner.rs:29-69) on the host, one prover round per
     C-ABI call.  hook(round, transcript) runs after the round's messages."""

@@ -43,7 +43,7 @@ typedef enum {
     EFFSC_PANIC = 6
 } effsc_status;
 
-typedef enum { EFFSC_ML = 0, EFFSC_IP = 1, EFFSC_COEF = 2, EFFSC_EQF = 3 } effsc_kind;
+typedef enum { EFFSC_ML = 0, EFFSC_IP = 1, EFFSC_COEF = 2, EFFSC_EQF = 3, EFFSC_GKR = 4 } effsc_kind;
 typedef enum { EFFSC_MSB = 0, EFFSC_LSB = 1 } effsc_order;
 typedef enum { EFFSC_FP = 1, EFFSC_FP3 = 3 } effsc_field;
 typedef enum { EFFSC_CANONICAL = 0, EFFSC_MONTGOMERY = 1 } effsc_repr;
@@ -101,6 +101,18 @@ int effsc_prover_create(effsc_ctx* ctx, int kind, int order, int field, int repr
  * p_ncomp words (zero-padded to 2^num_vars; longer is EFFSC_PANIC). */
 int effsc_eqf_create(effsc_ctx* ctx, int field, int repr, const uint64_t* w, size_t num_vars,
                      const uint64_t* p, size_t p_len, int p_ncomp, effsc_prover** out);
+/* GkrProver::new(add_evals, mult_evals, w_evals), src/provers/gkr.rs:61-82:
+ * add and mult hold n * n elements, w holds n (a power of two, n <= 2^17),
+ * `ncomp` u64 per element, `repr` as above.  The prover runs 2 log2(n)
+ * rounds of degree 2; its tables are add, mult and the witness kept as two
+ * n-element tables W_b (0..n-1 over b) and W_c (over c) instead of the
+ * reference's broadcast n*n tables (same values).  The reference's
+ * constructor asserts the lengths; here the caller passes n. */
+int effsc_gkr_create(effsc_ctx* ctx, int field, int repr, const uint64_t* add, const uint64_t* mult, const uint64_t* w,
+                     size_t n, int ncomp, effsc_prover** out);
+/* GkrProver::claimed_w_values, src/provers/gkr.rs:87-93: (W(b*), W(c*)) once
+ * all 2 log2(n) variables are bound, else zeros; out = 2 elements. */
+int effsc_gkr_claimed_w_values(effsc_prover* p, uint64_t* out);
 /* Same constructors with the tables already in device memory (canonical,
  * structure-of-arrays: c0 of every element, then c1, then c2 when ncomp = 3);
  * the prover copies nothing and does not take ownership: the caller keeps the

@@ -1,0 +1,93 @@
+"""GkrProver (src/provers/gkr.rs) on the GPU: the witness kept as two compact
+tables W_b, W_c instead of the reference's broadcast tables.  Every round
+polynomial, challenge, final value and claimed W value must equal the
+oracle's (which expands the broadcast tables exactly as the reference does),
+for full, partial and over-long runs, through the per-round API and the
+device-resident protocol."""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def E():
+    import effsc_gpu
+    effsc_gpu.load()
+    return effsc_gpu
+
+
+def inputs(k, ext, seed):
+    g = np.random.default_rng(seed)
+    n = 1 << k
+    shape = lambda m: (m, 3) if ext else (m,)  # noqa: E731
+    return (g.integers(0, O.P, size=shape(n * n), dtype=np.uint64),
+            g.integers(0, O.P, size=shape(n * n), dtype=np.uint64),
+            g.integers(0, O.P, size=shape(n), dtype=np.uint64))
+
+
+def check(E, proof, field, rp, ch, fv):
+    n = rp.shape[0]
+    assert np.array_equal(np.asarray(proof.round_polys).reshape(n, 2, field), rp[:, :, :field])
+    assert np.array_equal(np.asarray(proof.challenges).reshape(n, field), ch[:, :field])
+    assert np.array_equal(np.asarray(proof.final_value).reshape(field), fv[:field])
+
+
+@pytest.mark.parametrize("k", [0, 1, 2, 3, 4, 6, 8])
+@pytest.mark.parametrize("field,ext", [(1, False), (3, False), (3, True)])
+@pytest.mark.parametrize("path", ["device_graph", "device", "host"])
+def test_gkr_full_runs(E, k, field, ext, path):
+    add, mult, w = inputs(k, ext, 10 * k + field + ext)
+    rounds = 2 * k
+    orc = O.Prover.gkr(field, add, mult, w)
+    rp, ch, fv = O.sumcheck(orc, rounds, O.Transcript(field, label=b"gkr"), hook=bytes(range(32)))
+    g = E.GkrProver(add, mult, w, field=field)
+    if path == "host":
+        proof = E.sumcheck(g, rounds, E.Transcript.keccak(field, b"gkr"),
+                           hook=lambda r, t: t.absorb(bytes(range(32))))
+    else:
+        proof = g.prove(rounds, E.Transcript.keccak(field, b"gkr"), hook=bytes(range(32)),
+                        use_graph=path == "device_graph")
+    if rounds:
+        check(E, proof, field, rp, ch, fv)
+    cw = orc.claimed_w_values()
+    assert np.array_equal(g.claimed_w_values(), cw[:, :field])
+
+
+@pytest.mark.parametrize("k", [2, 3, 5])
+@pytest.mark.parametrize("rounds_of", [lambda k: 1, lambda k: k, lambda k: k + 1, lambda k: 2 * k + 2])
+def test_gkr_partial_and_extra_rounds(E, k, rounds_of):
+    rounds = rounds_of(k)
+    add, mult, w = inputs(k, False, 77 + k + rounds)
+    orc = O.Prover.gkr(3, add, mult, w)
+    rp, ch, fv = O.sumcheck(orc, rounds, O.Transcript(3, label=b"p"))
+    g = E.GkrProver(add, mult, w)
+    proof = g.prove(rounds, E.Transcript.keccak(3, b"p"))
+    check(E, proof, 3, rp, ch, fv)
+    assert np.array_equal(g.claimed_w_values(), orc.claimed_w_values())
+    # add and mult after the run equal the oracle's tables
+    for t in range(2):
+        assert np.array_equal(g.table(t).reshape(-1, 3), orc.table(t))
+
+
+def test_gkr_large_and_verifies(E):
+    k = 10
+    add, mult, w = inputs(k, False, 5)
+    rounds = 2 * k
+    orc = O.Prover.gkr(3, add, mult, w)
+    rp, ch, fv = O.sumcheck(orc, rounds, O.Transcript(3, label=b"L"))
+    g = E.GkrProver(add, mult, w)
+    proof = g.prove(rounds, E.Transcript.keccak(3, b"L"))
+    check(E, proof, 3, rp, ch, fv)
+    g.reset()
+    proof2 = g.prove(rounds, E.Transcript.keccak(3, b"L"))
+    check(E, proof2, 3, rp, ch, fv)
+
+
+def test_gkr_rejects(E):
+    with pytest.raises(AssertionError):
+        E.GkrProver(np.zeros(8, np.uint64), np.zeros(9, np.uint64), np.zeros(3, np.uint64))
+    with pytest.raises(E.EffscError):      # |w| not a power of two
+        E.GkrProver(np.zeros(9, np.uint64), np.zeros(9, np.uint64), np.zeros(3, np.uint64))
