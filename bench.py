@@ -721,6 +721,33 @@ def run_configs(args, E, L, ctx, stream, rank):
         "ms_per_proof": ms_e, "evals_per_s": (1 << n) / (ms_e * 1e-3), "algorithmic_bytes": by_e,
         "hbm_gbs": by_e / (ms_e * 1e-3) / 1e9, "bit_exact_vs_oracle": ok_e}
     del coef, eqf
+    # GkrProver, k = 12: add, mult of 2^24 base entries, w of 2^12, 24 rounds
+    k = 12
+    add = E.gen_uniform(E.table_seed(0x6C12_2026, 0), 1 << (2 * k), ctx=ctx)
+    mult = E.gen_uniform(E.table_seed(0x6C12_2026, 1), 1 << (2 * k), ctx=ctx)
+    wv = E.gen_uniform(E.table_seed(0x6C12_2026, 2), 1 << k, ctx=ctx)
+    gk = E.GkrProver(add, mult, wv, ctx=ctx)
+    lab_g = b"effsc-gpu/gkr/v1"
+
+    def gkr_proof(use_graph=True):
+        gk.reset()
+        return gk.prove(2 * k, E.Transcript.keccak(E.FP3, lab_g), use_graph=use_graph)
+
+    ms_g, pf_g = time_proofs(torch, stream, gkr_proof, 20)
+    by_g, _ = profile_bytes(E, L, lambda: gkr_proof(False))
+    ok_g = None
+    if check:
+        orc = O.Prover.gkr(3, add, mult, wv)
+        rp, ch, fv = O.sumcheck(orc, 2 * k, O.Transcript(3, label=lab_g))
+        ok_g = bool(np.array_equal(pf_g.round_polys, rp) and np.array_equal(pf_g.final_value, fv)
+                    and np.array_equal(gk.claimed_w_values(), orc.claimed_w_values()))
+        assert ok_g, "GkrProver k=12 proof differs from the oracle"
+    res["gkr_k12"] = {
+        "workload": "GkrProver (MSB), k=12: add, mult seeded uniform tables of 2^24 Goldilocks values, w of 2^12, "
+                    "Fp3 challenges, 24 rounds + finalize, label %s; witness kept as two 2^12 tables" % lab_g.decode(),
+        "ms_per_proof": ms_g, "evals_per_s": 2 * (1 << (2 * k)) / (ms_g * 1e-3), "algorithmic_bytes": by_g,
+        "hbm_gbs": by_g / (ms_g * 1e-3) / 1e9, "bit_exact_vs_oracle": ok_g}
+    del gk
     return res
 
 
