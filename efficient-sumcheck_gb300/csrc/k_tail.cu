@@ -70,49 +70,58 @@ __device__ void tail_body(const TailArgs& a) {
     u64 len = L0;
     bool fold = a.first_fold != 0;
     for (u32 k = 0; k < a.nrounds; k++) {
+        // warps without entries this round skip the arithmetic and the
+        // reduction of their (zero) sums; every warp reaches both barriers
+        const u64 nwork = fold ? (len >> 2) : len == 1 ? 1 : (len >> 1);
+        const bool active = (u64)warp * 32 < nwork;
         P acc;
-        acc.init();
-        F3 lo[NT], hi[NT];
-        if (fold) {
-            const Mul3 m = mul3_prepare<E>(f3_make(s_chal[0], s_chal[1], s_chal[2]));
-            const u64 Q = len >> 2;
-            for (u64 q = threadIdx.x; q < Q; q += TAIL_TPB) {
-#pragma unroll
-                for (int t = 0; t < NT; t++) {
-                    F3 x0 = sm_ld<FW>(sm, L0, t, q), x1 = sm_ld<FW>(sm, L0, t, q + Q);
-                    F3 x2 = sm_ld<FW>(sm, L0, t, q + 2 * Q), x3 = sm_ld<FW>(sm, L0, t, q + 3 * Q);
-                    lo[t] = f3_fold<E, E>(x0, x2, m);
-                    hi[t] = f3_fold<E, E>(x1, x3, m);
-                    sm_st<FW>(sm, L0, t, q, lo[t]);
-                    sm_st<FW>(sm, L0, t, q + Q, hi[t]);
-                }
-                acc.pair(lo, hi);
-            }
-            len >>= 1;
-        } else if (len == 1) {
-            if (threadIdx.x == 0) {
-#pragma unroll
-                for (int t = 0; t < NT; t++) lo[t] = sm_ld<FW>(sm, L0, t, 0);
-                acc.single(lo);
-            }
-        } else {
-            const u64 half = len >> 1;
-            for (u64 j = threadIdx.x; j < half; j += TAIL_TPB) {
-#pragma unroll
-                for (int t = 0; t < NT; t++) { lo[t] = sm_ld<FW>(sm, L0, t, j); hi[t] = sm_ld<FW>(sm, L0, t, j + half); }
-                acc.pair(lo, hi);
-            }
-        }
         F3 raw[P::NRAW];
-        acc.result(raw);
-        // block reduction
 #pragma unroll
-        for (int off = 16; off; off >>= 1) {
+        for (int i = 0; i < P::NRAW; i++) raw[i] = f3_zero();
+        if (fold && !active) len >>= 1;
+        if (active) {
+            acc.init();
+            F3 lo[NT], hi[NT];
+            if (fold) {
+                const Mul3 m = mul3_prepare<E>(f3_make(s_chal[0], s_chal[1], s_chal[2]));
+                const u64 Q = len >> 2;
+                for (u64 q = threadIdx.x; q < Q; q += TAIL_TPB) {
 #pragma unroll
-            for (int i = 0; i < P::NRAW; i++) {
-                raw[i].c0 = gl_add(raw[i].c0, __shfl_down_sync(0xffffffffu, raw[i].c0, off));
-                raw[i].c1 = gl_add(raw[i].c1, __shfl_down_sync(0xffffffffu, raw[i].c1, off));
-                raw[i].c2 = gl_add(raw[i].c2, __shfl_down_sync(0xffffffffu, raw[i].c2, off));
+                    for (int t = 0; t < NT; t++) {
+                        F3 x0 = sm_ld<FW>(sm, L0, t, q), x1 = sm_ld<FW>(sm, L0, t, q + Q);
+                        F3 x2 = sm_ld<FW>(sm, L0, t, q + 2 * Q), x3 = sm_ld<FW>(sm, L0, t, q + 3 * Q);
+                        lo[t] = f3_fold<E, E>(x0, x2, m);
+                        hi[t] = f3_fold<E, E>(x1, x3, m);
+                        sm_st<FW>(sm, L0, t, q, lo[t]);
+                        sm_st<FW>(sm, L0, t, q + Q, hi[t]);
+                    }
+                    acc.pair(lo, hi);
+                }
+                len >>= 1;
+            } else if (len == 1) {
+                if (threadIdx.x == 0) {
+#pragma unroll
+                    for (int t = 0; t < NT; t++) lo[t] = sm_ld<FW>(sm, L0, t, 0);
+                    acc.single(lo);
+                }
+            } else {
+                const u64 half = len >> 1;
+                for (u64 j = threadIdx.x; j < half; j += TAIL_TPB) {
+#pragma unroll
+                    for (int t = 0; t < NT; t++) { lo[t] = sm_ld<FW>(sm, L0, t, j); hi[t] = sm_ld<FW>(sm, L0, t, j + half); }
+                    acc.pair(lo, hi);
+                }
+            }
+            acc.result(raw);
+            // block reduction
+#pragma unroll
+            for (int off = 16; off; off >>= 1) {
+#pragma unroll
+                for (int i = 0; i < P::NRAW; i++) {
+                    raw[i].c0 = gl_add(raw[i].c0, __shfl_down_sync(0xffffffffu, raw[i].c0, off));
+                    raw[i].c1 = gl_add(raw[i].c1, __shfl_down_sync(0xffffffffu, raw[i].c1, off));
+                    raw[i].c2 = gl_add(raw[i].c2, __shfl_down_sync(0xffffffffu, raw[i].c2, off));
+                }
             }
         }
         if (lane == 0) {

@@ -48,7 +48,7 @@ __device__ __forceinline__ u64 rotl64d(u64 x, int r) {
 }
 
 // One Keccak-f[1600] permutation; lane i (< 25) holds lane A[i], i = x + 5y.
-__device__ __forceinline__ void keccak_f_warp(u64& a, int lane) {
+static __device__ __noinline__ void keccak_f_warp(u64& a, int lane) {
     const int i = lane < 25 ? lane : 0;
     const int x = i % 5, y = i / 5;
     const int my_rot = c_keccak_rot[i];
