@@ -203,19 +203,12 @@ def run_ours(args):
     import effsc_gpu as E
     from effsc_gpu import _lib
 
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
+    from effsc_gpu.replicas import Replicas, job_rate, replica_seed
     local = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(local)
-    dist = None
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
-
-    def barrier():
-        if dist is not None:
-            dist.barrier()
-        torch.cuda.synchronize()
+    rep = Replicas()
+    world, rank = rep.world, rep.rank
+    barrier = rep.barrier
 
     L = E.load()
     ctx = E.Context(local)
@@ -227,7 +220,7 @@ def run_ours(args):
     # inputs generated on the device (seeded), resident in HBM
     a_dev = torch.empty(n, dtype=torch.int64, device="cuda")
     b_dev = torch.empty(n, dtype=torch.int64, device="cuda")
-    seed = SEED + 7919 * rank
+    seed = replica_seed(SEED, rank)
     for t, buf in enumerate((a_dev, b_dev)):
         _lib.check(L.effsc_gen_uniform(ctx.h, E.table_seed(seed, t), n,
                                        _lib.ctypes.cast(_lib.ctypes.c_void_p(buf.data_ptr()), _lib.u64p), None))
@@ -266,12 +259,9 @@ def run_ours(args):
     clocks = summarize_clocks(sampler.stop())
     if extra:
         clocks["sampled_during"] = "timed region + %d more identical steps" % extra
-    if dist is not None:
-        tt = torch.tensor([ms], device="cuda", dtype=torch.float64)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        ms = float(tt.item())
+    ms = rep.max(ms)
     evals_per_step = 2 * n
-    value = world * args.steps * evals_per_step / (ms * 1e-3)
+    value = job_rate(evals_per_step, args.steps, world, ms)
 
     # ---- per-kernel timing (one proof outside the graph) -> roofline ----
     peaks = {}
@@ -343,11 +333,8 @@ def run_ours(args):
     e1.record(stream)
     barrier()
     e2e_ms = e0.elapsed_time(e1)
-    if dist is not None:
-        tt = torch.tensor([e2e_ms], device="cuda", dtype=torch.float64)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        e2e_ms = float(tt.item())
-    e2e_value = world * args.e2e_steps * evals_per_step / (e2e_ms * 1e-3)
+    e2e_ms = rep.max(e2e_ms)
+    e2e_value = job_rate(evals_per_step, args.e2e_steps, world, e2e_ms)
     proof_words = n_vars * 2 * 3 + n_vars * 3 + 3
     d2h = 8 * proof_words + 216 + 2 * 24
     assert (pf_e2e.round_polys == proof.round_polys).all(), "e2e proof differs from the device-resident proof"
@@ -417,8 +404,7 @@ def run_ours(args):
             "serving": serving,
         }
         print(json.dumps(line), flush=True)
-    if dist is not None:
-        dist.destroy_process_group()
+    rep.close()
 
 
 # ---------------------------------------------------------------------------
