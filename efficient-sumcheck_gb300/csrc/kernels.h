@@ -156,6 +156,9 @@ void launch_fill(u64* dst, u64 n, u64 v, cudaStream_t s);
 bool launch_build_eq(const u64* w, u32 v, int ext, u64* c0, u64* c1, u64* c2, cudaStream_t s);
 void launch_gen_uniform(u64 seed, u64 n, u64* out, cudaStream_t s);
 bool diag_mulmod_rate(cudaStream_t s, double* mulmod_per_s, double* fp3_mul_per_s);
+// One thread waits on an mbarrier with the round kernels' bounded wait;
+// `arrive`: complete the phase first.  *status = 0 or EFFSC_STATUS_TIMEOUT.
+void launch_diag_bounded_wait(u64 limit_ns, int arrive, u32* status, cudaStream_t s);
 int max_grid(void);
 void kernels_init(int device);
 

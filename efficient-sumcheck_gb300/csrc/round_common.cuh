@@ -542,12 +542,12 @@ __device__ __forceinline__ u64 global_ns() {
     asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
     return t;
 }
-// Wait for phase `phase` of `bar`; false after ~1 s.
-__device__ __forceinline__ bool mbar_wait_bounded(u64* bar, u32 phase) {
+// Wait for phase `phase` of `bar`; false after `limit_ns` (default 1 s).
+__device__ __forceinline__ bool mbar_wait_bounded(u64* bar, u32 phase, u64 limit_ns = 1000000000ULL) {
     if (mbar_try_wait(bar, phase)) return true;
     const u64 t0 = global_ns();
     while (!mbar_try_wait(bar, phase))
-        if (global_ns() - t0 > 1000000000ULL) return false;
+        if (global_ns() - t0 > limit_ns) return false;
     return true;
 }
 

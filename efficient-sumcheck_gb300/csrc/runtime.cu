@@ -1432,6 +1432,28 @@ int effsc_prover_read_table(effsc_prover* P, int table, uint64_t* out) {
     return EFFSC_OK;
 }
 
+int effsc_diag_bounded_wait(effsc_ctx* ctx, uint64_t limit_ns, int arrive, uint32_t* status_out) {
+    if (!ctx || !status_out) return fail(EFFSC_INVALID_ARG, "NULL argument");
+    if (limit_ns > 2000000000ULL) return fail(EFFSC_INVALID_ARG, "limit above 2 s");
+    CK(cudaSetDevice(ctx->device));
+    u32* h = nullptr;
+    u32* d = nullptr;
+    CK(cudaHostAlloc((void**)&h, sizeof(u32), cudaHostAllocMapped));
+    *h = 0xFFFFFFFFu;
+    cudaError_t e = cudaHostGetDevicePointer((void**)&d, h, 0);
+    if (e == cudaSuccess) {
+        launch_diag_bounded_wait(limit_ns, arrive, d, ctx->stream);
+        g_launches++;
+        e = cudaGetLastError();
+        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    }
+    const u32 v = *(volatile u32*)h;
+    cudaFreeHost(h);
+    if (e != cudaSuccess) return fail(EFFSC_CUDA_ERROR, "bounded-wait self-test: %s", cudaGetErrorString(e));
+    *status_out = v;
+    return EFFSC_OK;
+}
+
 int effsc_prover_set_first_rounds(effsc_prover* P, int fused) {
     if (!P) return fail(EFFSC_INVALID_ARG, "prover is NULL");
     if ((fused != 0) != P->fuse_first && P->gexec) { cudaGraphExecDestroy(P->gexec); P->gexec = nullptr; }

@@ -60,6 +60,7 @@ SIGNATURES = {
     "effsc_table_seed": (ctypes.c_uint64, [ctypes.c_uint64, ctypes.c_uint64]),
     "effsc_gkr_create": (ci, [vp, ci, ci, u64p, u64p, u64p, sz, ci, ctypes.POINTER(vp)]),
     "effsc_gkr_claimed_w_values": (ci, [vp, u64p]),
+    "effsc_diag_bounded_wait": (ci, [vp, ctypes.c_uint64, ci, ctypes.POINTER(ctypes.c_uint32)]),
     "effsc_prover_set_tail": (ci, [vp, sz]),
     "effsc_prover_set_first_rounds": (ci, [vp, ci]),
     "effsc_batch_create": (ci, [vp, ci, ci, sz, ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(u64p), u64p,

@@ -231,6 +231,14 @@ uint64_t effsc_table_seed(uint64_t seed, uint64_t table);
  * thread of a full grid; the denominator of the integer-multiply roofline. */
 int effsc_diag_mulmod_rate(effsc_ctx* ctx, double* mulmod_per_s, double* fp3_mul_per_s);
 
+/* Self-test of the bounded wait that the TMA-staged round kernel uses on its
+ * own mbarriers (no reference counterpart): one thread waits on a barrier
+ * that nothing completes (arrive = 0) or that it completed itself (arrive =
+ * 1), giving up after limit_ns (at most 2 s).  *status = 0 when the wait
+ * completed, EFFSC_STATUS_TIMEOUT (4) when it gave up; the context stays
+ * usable either way. */
+int effsc_diag_bounded_wait(effsc_ctx* ctx, uint64_t limit_ns, int arrive, uint32_t* status);
+
 /* ---- batches: many independent provers, one launch per round -------------
  * No reference counterpart (the crate proves one instance per call).  A batch
  * holds n_inst InnerProductProver (kind EFFSC_IP, tables a and b) or
