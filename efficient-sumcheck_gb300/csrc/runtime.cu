@@ -219,6 +219,7 @@ struct Buf {
     size_t cap = 0;
     bool ext = false;
     bool owned = true;
+    bool host = false;      // the caller's host memory, read in place (never bulk-copied)
 };
 struct Table {
     std::vector<Buf> bufs;  // bufs[0]: the input table, never written by a round
@@ -460,6 +461,7 @@ int round_std(effsc_prover* P, const Chal& ch, const TxIO& tx, bool dry) {
             // large power-of-two MSB rounds: the TMA-staged kernel
             const u64 Q = L / 4;
             bool tma = pol == POL_IP && sem == SEM_MSB_PAD && is_pow2(L) && Q >= TMA_MIN_QUADS && Q % KERNEL_TPB == 0;
+            for (int i = 0; i < nt; i++) tma &= !P->t[i].bufs[P->t[i].cur].host;
             for (int i = 0; i < nt && tma; i++)
                 for (int c = 0; c < (P->t[i].ext ? 3 : 1); c++)
                     tma &= ((uintptr_t)a.t[i].in[c] % 16) == 0;
@@ -873,7 +875,7 @@ int read_first(effsc_prover* P, int ti, HF* out) {
     const Buf& b = T.bufs[T.cur];
     u64 w[3] = {0, 0, 0};
     for (int c = 0; c < (T.ext ? 3 : 1); c++)
-        CK(cudaMemcpyAsync(&w[c], b.p[c], sizeof(u64), cudaMemcpyDeviceToHost, P->ctx->stream));
+        CK(cudaMemcpyAsync(&w[c], b.p[c], sizeof(u64), cudaMemcpyDefault, P->ctx->stream));
     CK(cudaStreamSynchronize(P->ctx->stream));
     *out = hf(w[0], w[1], w[2]);
     return EFFSC_OK;
@@ -994,7 +996,7 @@ int promote(effsc_prover* P, Table& T) {
     TRY(alloc_buf(P, nb, T.len, true));
     Buf& ob = T.bufs[T.cur];
     if (T.len) {
-        CK(cudaMemcpyAsync(nb.p[0], ob.p[0], T.len * sizeof(u64), cudaMemcpyDeviceToDevice, s));
+        CK(cudaMemcpyAsync(nb.p[0], ob.p[0], T.len * sizeof(u64), cudaMemcpyDefault, s));
         CK(cudaMemsetAsync(nb.p[1], 0, T.len * sizeof(u64), s));
         CK(cudaMemsetAsync(nb.p[2], 0, T.len * sizeof(u64), s));
     }
@@ -1074,11 +1076,23 @@ Chal host_chal(const effsc_prover* P, const uint64_t* c) {
 
 }  // namespace
 
-// Internal accessors used by batch.cu / serve.cu.
+// Internal accessors used by batch.cu / serve.cu / streams.cu.
+const u64* effsc_internal_device_view(int device, const uint64_t* ptr, bool* is_host);
 void effsc_internal_tx_state(const effsc_transcript* t, void* out) {
     DevTranscript st = t->st;
     if (t->kind != EFFSC_T_KECCAK) st.deg = 0;   // marks a transcript the device cannot run
     memcpy(out, &st, sizeof st);
+}
+const u64* effsc_internal_device_view(int device, const uint64_t* ptr, bool* is_host) {
+    cudaPointerAttributes at;
+    *is_host = false;
+    if (cudaPointerGetAttributes(&at, ptr) != cudaSuccess) { cudaGetLastError(); return nullptr; }
+    if (at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged) return (const u64*)ptr;
+    *is_host = true;
+    if (at.type == cudaMemoryTypeHost) return (const u64*)at.devicePointer;
+    int pageable = 0;
+    cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, device);
+    return pageable ? (const u64*)ptr : nullptr;
 }
 int effsc_internal_ctx_device(const effsc_ctx* c) { return c->device; }
 cudaStream_t effsc_internal_ctx_stream(const effsc_ctx* c) { return c->stream; }
@@ -1213,9 +1227,18 @@ int effsc_prover_create(effsc_ctx* ctx, int kind, int order, int field, int repr
     return EFFSC_OK;
 }
 
-int effsc_prover_create_device(effsc_ctx* ctx, int kind, int order, int field, int n_tables,
-                               const uint64_t* const* dev_tables, const size_t* lens, const int* ncomp,
-                               effsc_prover** out) {
+// A pointer the kernels can read: device memory as is, pinned or registered
+// host memory through its device alias, pageable host memory when the GPU
+// reads host page tables (cudaDevAttrPageableMemoryAccess); else null.
+static const u64* device_view(int device, const uint64_t* ptr, bool* is_host) {
+    return effsc_internal_device_view(device, ptr, is_host);
+}
+
+// Provers over caller-owned tables read in place (device or host memory).
+static int create_in_place(effsc_ctx* ctx, int kind, int order, int field, int n_tables,
+                           const uint64_t* const* tables, const size_t* lens, const int* ncomp, bool host,
+                           effsc_prover** out) {
+    const uint64_t* const* dev_tables = tables;
     if (!ctx || !out || !dev_tables || !lens || !ncomp) return fail(EFFSC_INVALID_ARG, "NULL argument");
     TRY(check_field(field));
     if (kind != EFFSC_ML && kind != EFFSC_IP && kind != EFFSC_COEF) return fail(EFFSC_INVALID_ARG, "kind must be ML, IP or COEF");
@@ -1236,6 +1259,13 @@ int effsc_prover_create_device(effsc_ctx* ctx, int kind, int order, int field, i
         b.cap = lens[i];
         b.ext = ncomp[i] == 3;
         b.p[0] = (u64*)dev_tables[i];
+        if (host) {
+            bool is_host = false;
+            const u64* v = device_view(ctx->device, dev_tables[i], &is_host);
+            if (!v) { rc = fail(EFFSC_UNSUPPORTED, "table %d: host memory the GPU cannot read (register or pin it)", i); break; }
+            b.p[0] = (u64*)v;
+            b.host = is_host;
+        }
         if (b.ext) { b.p[1] = b.p[0] + lens[i]; b.p[2] = b.p[0] + 2 * lens[i]; }
         Table& T = P->t[i];
         T.bufs.assign(1, b);
@@ -1253,6 +1283,18 @@ int effsc_prover_create_device(effsc_ctx* ctx, int kind, int order, int field, i
     snapshot_initial(P);
     *out = P;
     return EFFSC_OK;
+}
+
+int effsc_prover_create_device(effsc_ctx* ctx, int kind, int order, int field, int n_tables,
+                               const uint64_t* const* dev_tables, const size_t* lens, const int* ncomp,
+                               effsc_prover** out) {
+    return create_in_place(ctx, kind, order, field, n_tables, dev_tables, lens, ncomp, false, out);
+}
+
+int effsc_prover_create_host(effsc_ctx* ctx, int kind, int order, int field, int n_tables,
+                             const uint64_t* const* host_tables, const size_t* lens, const int* ncomp,
+                             effsc_prover** out) {
+    return create_in_place(ctx, kind, order, field, n_tables, host_tables, lens, ncomp, true, out);
 }
 
 int effsc_gkr_create(effsc_ctx* ctx, int field, int repr, const uint64_t* add, const uint64_t* mult, const uint64_t* w,

@@ -58,6 +58,10 @@ SIGNATURES = {
     "effsc_build_eq_table": (ci, [vp, ci, ci, u64p, sz, u64p]),
     "effsc_gen_uniform": (ci, [vp, ctypes.c_uint64, ctypes.c_uint64, u64p, u64p]),
     "effsc_table_seed": (ctypes.c_uint64, [ctypes.c_uint64, ctypes.c_uint64]),
+    "effsc_prover_create_host": (ci, [vp, ci, ci, ci, ci, ctypes.POINTER(u64p), ctypes.POINTER(sz),
+                                      ctypes.POINTER(ci), ctypes.POINTER(vp)]),
+    "effsc_reorder_msb": (ci, [vp, u64p, sz, ci, u64p]),
+    "effsc_stream_claim": (ci, [vp, ci, ci, ctypes.POINTER(u64p), sz, ci, u64p]),
     "effsc_gkr_create": (ci, [vp, ci, ci, u64p, u64p, u64p, sz, ci, ctypes.POINTER(vp)]),
     "effsc_gkr_claimed_w_values": (ci, [vp, u64p]),
     "effsc_diag_bounded_wait": (ci, [vp, ctypes.c_uint64, ci, ctypes.POINTER(ctypes.c_uint32)]),

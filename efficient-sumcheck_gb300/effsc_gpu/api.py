@@ -204,6 +204,38 @@ class _Prover:
         _Prover.__init__(obj, None, field, CANONICAL, ctx, _h=h)
         return obj
 
+    @classmethod
+    def from_host(cls, host_tables, field=FP3, ctx=None):
+        """Construct over canonical tables left in host memory (numpy arrays,
+        memory maps, pinned buffers) and read in place by the kernels; base
+        tables are 1-D, Fp3 tables (n, 3) are passed as three component rows.
+        The arrays are kept alive by the prover."""
+        ctx = ctx or Context.default()
+        keep = []
+        ptrs, lens, ncomp = [], [], []
+        for t in host_tables:
+            a = np.asarray(t, dtype=np.uint64)
+            if a.ndim == 2:
+                a = np.ascontiguousarray(a.T)        # component-major (SoA)
+                ncomp.append(3)
+                lens.append(a.shape[1])
+            else:
+                if not (a.flags["C_CONTIGUOUS"]):
+                    a = np.ascontiguousarray(a)
+                ncomp.append(1)
+                lens.append(a.shape[0])
+            keep.append(a)
+            ptrs.append(a.ctypes.data_as(u64p))
+        n = len(keep)
+        h = vp()
+        check(load().effsc_prover_create_host(ctx.h, cls.kind, cls.order, field, n, (u64p * n)(*ptrs),
+                                              (ctypes.c_size_t * n)(*lens), (ctypes.c_int * n)(*ncomp),
+                                              ctypes.byref(h)))
+        obj = cls.__new__(cls)
+        _Prover.__init__(obj, None, field, CANONICAL, ctx, _h=h)
+        obj._host_tables = keep
+        return obj
+
     def __del__(self):
         if getattr(self, "h", None) and _lib._lib is not None:
             _lib._lib.effsc_prover_destroy(self.h)
@@ -671,6 +703,96 @@ class Server:
                                          fv[i * field:(i + 1) * field]))
                 ro += m
         return lat, mk.value, out
+
+
+# ---------------------------------------------------------------------------
+# streams (src/streams/)
+# ---------------------------------------------------------------------------
+def reorder_vec_msb(evaluations, ctx=None):
+    """src/streams/memory/core.rs:20-47: out[i] = src[bit_reverse(i)]."""
+    ctx = ctx or Context.default()
+    a = np.ascontiguousarray(np.asarray(evaluations, dtype=np.uint64))
+    ncomp = 3 if a.ndim == 2 else 1
+    out = np.empty_like(a)
+    check(load().effsc_reorder_msb(ctx.h, _p(a), a.shape[0], ncomp, _p(out)))
+    return out
+
+
+def multivariate_product_claim(streams, field=FP3, ctx=None):
+    """src/streams/stream.rs:14-40: sum over the hypercube of the product."""
+    ctx = ctx or Context.default()
+    tabs = []
+    for st in streams:
+        t = st.evaluations if isinstance(st, (MemoryStream, FileStream)) else st
+        tabs.append(np.asarray(t, dtype=np.uint64))
+    if not tabs:
+        raise AssertionError("should be given at least one stream")    # the reference asserts
+    n = tabs[0].shape[0]
+    if any(t.shape[0] != n for t in tabs):
+        raise AssertionError("all streams should have the same number of variables")
+    ncomp = 3 if any(t.ndim == 2 for t in tabs) else 1
+    if ncomp == 3:
+        tabs = [t if t.ndim == 2 else np.stack([t, np.zeros_like(t), np.zeros_like(t)], axis=1) for t in tabs]
+    tabs = [t if t.flags["C_CONTIGUOUS"] else np.ascontiguousarray(t) for t in tabs]
+    out = np.zeros(field, dtype=np.uint64)
+    ptrs = (u64p * len(tabs))(*[t.ctypes.data_as(u64p) for t in tabs])
+    check(load().effsc_stream_claim(ctx.h, field, len(tabs), ptrs, n, ncomp, _p(out)))
+    return out
+
+
+def multivariate_claim(stream, field=FP3, ctx=None):
+    """src/streams/stream.rs:3-12: sum of a stream's evaluations."""
+    return multivariate_product_claim([stream], field, ctx)
+
+
+class MemoryStream:
+    """src/streams/memory/core.rs:9-66: evaluations in MSB order."""
+
+    def __init__(self, evaluations):
+        e = np.asarray(evaluations, dtype=np.uint64)
+        n = e.shape[0]
+        if n == 0 or n & (n - 1):
+            raise AssertionError("evaluations must be a non-empty power of two")
+        self.evaluations = e
+
+    @classmethod
+    def new_from_lex_msb(cls, evaluations):
+        return cls(reorder_vec_msb(evaluations))
+
+    def evaluation(self, point):
+        return self.evaluations[point]
+
+    def num_variables(self):
+        return int(self.evaluations.shape[0]).bit_length() - 1
+
+
+class FileStream:
+    """src/streams/file/core.rs: a file of base-field elements, 8
+    little-endian canonical bytes each (arkworks' uncompressed encoding of a
+    64-bit prime field element), memory-mapped; provers read it in place
+    through from_host."""
+
+    def __init__(self, path):
+        self.path = path
+        self.evaluations = np.memmap(path, dtype="<u8", mode="r")
+        n = self.evaluations.shape[0]
+        if n == 0 or n & (n - 1):
+            raise AssertionError("file length must be a power of two elements")
+
+    @staticmethod
+    def write_to_file(path, data):
+        np.asarray(data, dtype="<u8").tofile(path)
+
+    @staticmethod
+    def delete_file(path):
+        import os
+        os.remove(path)
+
+    def evaluation(self, point):
+        return self.evaluations[point]
+
+    def num_variables(self):
+        return int(self.evaluations.shape[0]).bit_length() - 1
 
 
 def gen_uniform(seed, n, ctx=None):

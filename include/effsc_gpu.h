@@ -101,6 +101,30 @@ int effsc_prover_create(effsc_ctx* ctx, int kind, int order, int field, int repr
  * p_ncomp words (zero-padded to 2^num_vars; longer is EFFSC_PANIC). */
 int effsc_eqf_create(effsc_ctx* ctx, int field, int repr, const uint64_t* w, size_t num_vars,
                      const uint64_t* p, size_t p_len, int p_ncomp, effsc_prover** out);
+/* The constructors above over tables left in HOST memory and read in place by
+ * the kernels (no bulk copy; for tables larger than HBM: only the folded
+ * tables are allocated on the device).  Layout as effsc_prover_create_device.
+ * Pinned or registered memory always works; plain pageable memory (including
+ * a memory-mapped file) works when the GPU reads host page tables
+ * (cudaDevAttrPageableMemoryAccess), else EFFSC_UNSUPPORTED.  The memory must
+ * stay valid and unchanged while the prover exists (its input tables are
+ * never written).  No reference counterpart (the crate's FileStream /
+ * MemoryStream, src/streams/, feed provers from memory or mmap). */
+int effsc_prover_create_host(effsc_ctx* ctx, int kind, int order, int field, int n_tables,
+                             const uint64_t* const* host_tables, const size_t* lens, const int* ncomp,
+                             effsc_prover** out);
+
+/* reorder_vec_msb, src/streams/memory/core.rs:20-47: dst[i] = src[bit_reverse(i)]
+ * over n (a power of two, else EFFSC_PANIC as the reference asserts) elements
+ * of ncomp words; src and dst in host or device memory. */
+int effsc_reorder_msb(effsc_ctx* ctx, const uint64_t* src, size_t n, int ncomp, uint64_t* dst);
+/* multivariate_claim (n_tables = 1) and multivariate_product_claim
+ * (src/streams/stream.rs:3-40): out = sum over i < n of prod_t tables[t][i],
+ * `field` words; tables canonical with ncomp words per element (AoS), in host
+ * or device memory, read in place; 1..4 tables. */
+int effsc_stream_claim(effsc_ctx* ctx, int field, int n_tables, const uint64_t* const* tables, size_t n, int ncomp,
+                       uint64_t* out);
+
 /* GkrProver::new(add_evals, mult_evals, w_evals), src/provers/gkr.rs:61-82:
  * add and mult hold n * n elements, w holds n (a power of two, n <= 2^17),
  * `ncomp` u64 per element, `repr` as above.  The prover runs 2 log2(n)
