@@ -15,6 +15,15 @@ void kernels_init(int device) {
     cudaDeviceGetAttribute(&g_sms, cudaDevAttrMultiProcessorCount, device);
     if (g_sms <= 0) g_sms = 1;
 }
+__global__ void k_gather_first(FirstSrc src, u64* dst) {
+    const int i = threadIdx.x;
+    if (i < 12) {
+        const u64* p = src.p[i / 3][i % 3];
+        dst[i] = p ? p[0] : 0;
+    }
+}
+void launch_gather_first(const FirstSrc& src, u64* dst, cudaStream_t s) { k_gather_first<<<1, 32, 0, s>>>(src, dst); }
+
 int max_grid(void) { return (g_sms > 0 ? g_sms : 1) * 8; }
 
 int pol_ntables(int pol) {

@@ -152,6 +152,11 @@ void launch_batch_finalize(const RoundArgs* args, const unsigned char* ext, u32 
 void launch_split_aos(const u64* aos, u64 n, int ncomp, u64* c0, u64* c1, u64* c2, int from_mont, u32* ext_flag, cudaStream_t s);
 void launch_join_aos(const u64* c0, const u64* c1, const u64* c2, u64 n, int ncomp, u64* aos, int to_mont, cudaStream_t s);
 void launch_copy(const u64* src, u64* dst, u64 n, cudaStream_t s);
+// dst[3 t + c] = p[t][c][0] for the non-null component pointers, else 0.
+struct FirstSrc {
+    const u64* p[4][3];
+};
+void launch_gather_first(const FirstSrc& src, u64* dst, cudaStream_t s);
 void launch_fill(u64* dst, u64 n, u64 v, cudaStream_t s);
 bool launch_build_eq(const u64* w, u32 v, int ext, u64* c0, u64* c1, u64* c2, cudaStream_t s);
 void launch_gen_uniform(u64 seed, u64 n, u64* out, cudaStream_t s);

@@ -268,6 +268,10 @@ struct effsc_prover {
     bool fuse_first = true;
     u64* eqf_scratch = nullptr;               // inner sums, eq weights, partial sums
     size_t eqf_cap = 0;
+    // effsc_prove outputs: pinned staging (wire | challenges | transcript |
+    // first entries of the tables) and the device copy of the first entries
+    u64* h_out = nullptr;
+    u64* d_first = nullptr;
 };
 
 namespace {
@@ -870,7 +874,16 @@ int do_finalize(effsc_prover* P, const Chal& ch, bool dry) {
     return EFFSC_OK;
 }
 
+// Entry 0 of each table's current buffer, gathered on the device by
+// effsc_prove (k_gather_first) so that the final value needs no extra copy.
+thread_local const u64* g_first = nullptr;
+constexpr size_t TX_OUT_WORDS = (sizeof(DevTranscript) + 7) / 8;
+
 int read_first(effsc_prover* P, int ti, HF* out) {
+    if (g_first) {
+        *out = hf(g_first[3 * ti], g_first[3 * ti + 1], g_first[3 * ti + 2]);
+        return EFFSC_OK;
+    }
     Table& T = P->t[ti];
     const Buf& b = T.bufs[T.cur];
     u64 w[3] = {0, 0, 0};
@@ -1056,10 +1069,12 @@ void release_prover(effsc_prover* P) {
         if (P->d_wire) cudaFreeAsync(P->d_wire, s);
         if (P->d_chals) cudaFreeAsync(P->d_chals, s);
         if (P->eqf_scratch) cudaFreeAsync(P->eqf_scratch, s);
+        if (P->d_first) cudaFreeAsync(P->d_first, s);
         if (P->gexec) cudaGraphExecDestroy(P->gexec);
         cudaStreamSynchronize(s);
     }
     if (P->h_res) cudaFreeHost(P->h_res);
+    if (P->h_out) cudaFreeHost(P->h_out);
     delete P;
 }
 
@@ -1545,6 +1560,9 @@ int effsc_prove(effsc_prover* P, size_t num_rounds, effsc_transcript* T, const u
         size_t cap = std::max<size_t>(num_rounds, 1);
         CK(cudaMallocAsync((void**)&P->d_wire, cap * 9 * sizeof(u64), s));
         CK(cudaMallocAsync((void**)&P->d_chals, cap * 3 * sizeof(u64), s));
+        if (P->h_out) { CK(cudaStreamSynchronize(s)); cudaFreeHost(P->h_out); P->h_out = nullptr; }
+        CK(cudaHostAlloc((void**)&P->h_out, (cap * 12 + TX_OUT_WORDS + 12) * sizeof(u64), cudaHostAllocDefault));
+        if (!P->d_first) CK(cudaMallocAsync((void**)&P->d_first, 12 * sizeof(u64), s));
         P->rounds_cap = cap;
         if (P->gexec) { cudaGraphExecDestroy(P->gexec); P->gexec = nullptr; }
     }
@@ -1602,6 +1620,17 @@ int effsc_prove(effsc_prover* P, size_t num_rounds, effsc_transcript* T, const u
             ch.has = true; ch.ext = P->field == EFFSC_FP3; ch.dev = P->d_chals + 3 * (num_rounds - 1);
             TRY(do_finalize(P, ch, dry));
         }
+        if (!dry) {
+            FirstSrc src;
+            memset(&src, 0, sizeof src);
+            for (int i = 0; i < 4; i++) {
+                if (P->t[i].bufs.empty()) continue;
+                const Buf& b = P->t[i].bufs[P->t[i].cur];
+                for (int c = 0; c < (P->t[i].ext ? 3 : 1); c++) src.p[i][c] = b.p[c];
+            }
+            launch_gather_first(src, P->d_first, s);
+            g_launches++;
+        }
         return EFFSC_OK;
     };
 
@@ -1648,26 +1677,35 @@ int effsc_prove(effsc_prover* P, size_t num_rounds, effsc_transcript* T, const u
     } else {
         TRY(launch_all(false));
     }
-    // results
-    std::vector<u64> wire(num_rounds * 3 * d), chal(num_rounds * 3);
+    // results: pinned copies of the wire values, challenges, transcript state
+    // and the tables' first entries, one synchronisation
+    u64* hw = P->h_out;
+    u64* hc = hw + num_rounds * 3 * d;
+    u64* ht = hc + num_rounds * 3;
+    u64* hf_ = ht + TX_OUT_WORDS;
     if (num_rounds) {
-        CK(cudaMemcpyAsync(wire.data(), P->d_wire, wire.size() * sizeof(u64), cudaMemcpyDeviceToHost, s));
-        CK(cudaMemcpyAsync(chal.data(), P->d_chals, chal.size() * sizeof(u64), cudaMemcpyDeviceToHost, s));
+        CK(cudaMemcpyAsync(hw, P->d_wire, num_rounds * 3 * d * sizeof(u64), cudaMemcpyDeviceToHost, s));
+        CK(cudaMemcpyAsync(hc, P->d_chals, num_rounds * 3 * sizeof(u64), cudaMemcpyDeviceToHost, s));
     }
-    CK(cudaMemcpyAsync(&T->st, P->d_tx, sizeof(DevTranscript), cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(ht, P->d_tx, sizeof(DevTranscript), cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(hf_, P->d_first, 12 * sizeof(u64), cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
     TRY(check_status(P));
+    memcpy(&T->st, ht, sizeof(DevTranscript));
     for (size_t r = 0; r < num_rounds; r++) {
         if (round_polys)
             for (int i = 0; i < d; i++) {
-                const u64* q = &wire[(r * d + i) * 3];
+                const u64* q = &hw[(r * d + i) * 3];
                 store_elem(round_polys + (r * d + i) * P->field, hf(q[0], q[1], q[2]), P->field, P->repr);
             }
-        if (challenges) store_elem(challenges + r * P->field, hf(chal[3 * r], chal[3 * r + 1], chal[3 * r + 2]), P->field, P->repr);
+        if (challenges) store_elem(challenges + r * P->field, hf(hc[3 * r], hc[3 * r + 1], hc[3 * r + 2]), P->field, P->repr);
     }
     if (final_value_out) {
         HF v;
-        TRY(final_value(P, &v));
+        g_first = hf_;
+        int rc = final_value(P, &v);
+        g_first = nullptr;
+        TRY(rc);
         store_elem(final_value_out, v, P->field, P->repr);
     }
     return EFFSC_OK;

@@ -258,6 +258,6 @@ def test_kernels_launch(E):
     assert E.launch_count() >= 12
     E.launch_count_reset()
     p.reset()
-    p.set_tail(None)     # all 12 rounds in the one-block tail kernel, then the final folds
+    p.set_tail(None)     # all 12 rounds in the one-block tail kernel, the final folds, the read-back gather
     p.prove(12, E.Transcript.keccak(3, b"k"), use_graph=False)
-    assert 1 <= E.launch_count() <= 3
+    assert 1 <= E.launch_count() <= 4
