@@ -73,6 +73,7 @@ struct effsc_batch {
     u64* d_final = nullptr;
     cudaGraphExec_t gexec = nullptr;
     uint64_t graph_kernels = 0;
+    u64* h_out = nullptr;                  // pinned: wire rows | challenge rows | final values
 };
 
 namespace {
@@ -352,6 +353,9 @@ int effsc_batch_create(effsc_ctx* ctx, int kind, int field, size_t n_inst, const
         cudaMallocAsync((void**)&b->d_chal, std::max<size_t>(1, b->total_rounds) * 3 * sizeof(u64), s) != cudaSuccess ||
         cudaMallocAsync((void**)&b->d_final, n_inst * 3 * sizeof(u64), s) != cudaSuccess)
         return bail(effsc_set_error(EFFSC_OOM, "batch bookkeeping allocation failed"));
+    const size_t rows = std::max<size_t>(1, b->total_rounds);
+    if (cudaHostAlloc((void**)&b->h_out, (rows * 3 * 2 + rows * 3 + n_inst * 3) * sizeof(u64), cudaHostAllocDefault) != cudaSuccess)
+        return bail(effsc_set_error(EFFSC_OOM, "pinned output staging"));
     if (cudaHostAlloc((void**)&b->h_status, sizeof(u32), cudaHostAllocMapped) != cudaSuccess ||
         cudaHostGetDevicePointer((void**)&b->d_status, b->h_status, 0) != cudaSuccess)
         return bail(effsc_set_error(EFFSC_CUDA_ERROR, "mapped status word"));
@@ -376,6 +380,7 @@ int effsc_batch_destroy(effsc_batch* b) {
     if (b->d_final) cudaFreeAsync(b->d_final, s);
     cudaStreamSynchronize(s);
     if (b->h_status) cudaFreeHost(b->h_status);
+    if (b->h_out) cudaFreeHost(b->h_out);
     delete b;
     return EFFSC_OK;
 }
@@ -437,10 +442,12 @@ int effsc_batch_prove(effsc_batch* b, const effsc_transcript* const* transcripts
     }
     effsc_internal_add_launches(kernels);
     const int d = deg_of(b), f = b->field;
-    std::vector<u64> wire(b->total_rounds * 3 * d), chal(b->total_rounds * 3), fin(b->n * 3);
-    if (round_polys) BCK(cudaMemcpyAsync(wire.data(), b->d_wire, wire.size() * 8, cudaMemcpyDeviceToHost, s));
-    if (challenges) BCK(cudaMemcpyAsync(chal.data(), b->d_chal, chal.size() * 8, cudaMemcpyDeviceToHost, s));
-    if (final_values) BCK(cudaMemcpyAsync(fin.data(), b->d_final, fin.size() * 8, cudaMemcpyDeviceToHost, s));
+    u64* wire = b->h_out;
+    u64* chal = wire + b->total_rounds * 3 * d;
+    u64* fin = chal + b->total_rounds * 3;
+    if (round_polys) BCK(cudaMemcpyAsync(wire, b->d_wire, b->total_rounds * 3 * d * 8, cudaMemcpyDeviceToHost, s));
+    if (challenges) BCK(cudaMemcpyAsync(chal, b->d_chal, b->total_rounds * 3 * 8, cudaMemcpyDeviceToHost, s));
+    if (final_values) BCK(cudaMemcpyAsync(fin, b->d_final, b->n * 3 * 8, cudaMemcpyDeviceToHost, s));
     BCK(cudaStreamSynchronize(s));
     if (*(volatile u32*)b->h_status) {
         *(volatile u32*)b->h_status = 0;
