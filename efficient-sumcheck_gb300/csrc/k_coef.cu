@@ -21,6 +21,8 @@ bool launch_eval_coef(int pol, int sem, u32 mask, const RoundArgs& a, int grid, 
 
 #define FUSED(POL, SEM, M, ECH) \
     case ((POL) * 128 + (SEM) * 32 + (M) * 2 + (ECH)): k_fused<POL, SEM, M, ECH><<<grid, TPB, 0, s>>>(a); return true;
+#define FUSED_WIDE(POL, SEM, M, ECH) \
+    case ((POL) * 128 + (SEM) * 32 + (M) * 2 + (ECH)): k_fused_wide<POL, SEM, M, ECH><<<grid, TPB, 0, s>>>(a); return true;
 
 bool launch_fused_coef(int pol, int sem, u32 mask, bool ech, const RoundArgs& a, int grid, cudaStream_t s) {
     switch (pol * 128 + sem * 32 + (int)mask * 2 + (ech ? 1 : 0)) {
@@ -28,10 +30,10 @@ bool launch_fused_coef(int pol, int sem, u32 mask, bool ech, const RoundArgs& a,
         FUSED(POL_C1, SEM_LSB, 0, false) FUSED(POL_C1, SEM_LSB, 0, true) FUSED(POL_C1, SEM_LSB, 1, true)
         FUSED(POL_C2, SEM_MSB_FLOOR, 0, false) FUSED(POL_C2, SEM_MSB_FLOOR, 0, true) FUSED(POL_C2, SEM_MSB_FLOOR, 3, true)
         FUSED(POL_C2, SEM_LSB, 0, false) FUSED(POL_C2, SEM_LSB, 0, true) FUSED(POL_C2, SEM_LSB, 3, true)
-        FUSED(POL_C3, SEM_MSB_FLOOR, 0, false) FUSED(POL_C3, SEM_MSB_FLOOR, 0, true)
-        FUSED(POL_C3, SEM_MSB_FLOOR, 1, true) FUSED(POL_C3, SEM_MSB_FLOOR, 7, true)
-        FUSED(POL_C3, SEM_LSB, 0, false) FUSED(POL_C3, SEM_LSB, 0, true)
-        FUSED(POL_C3, SEM_LSB, 1, true) FUSED(POL_C3, SEM_LSB, 7, true)
+        FUSED_WIDE(POL_C3, SEM_MSB_FLOOR, 0, false) FUSED_WIDE(POL_C3, SEM_MSB_FLOOR, 0, true)
+        FUSED_WIDE(POL_C3, SEM_MSB_FLOOR, 1, true) FUSED_WIDE(POL_C3, SEM_MSB_FLOOR, 7, true)
+        FUSED_WIDE(POL_C3, SEM_LSB, 0, false) FUSED_WIDE(POL_C3, SEM_LSB, 0, true)
+        FUSED_WIDE(POL_C3, SEM_LSB, 1, true) FUSED_WIDE(POL_C3, SEM_LSB, 7, true)
         default: return false;
     }
 }

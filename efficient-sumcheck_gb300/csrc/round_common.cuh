@@ -131,35 +131,33 @@ struct Policy<POL_C2, M> {
     __device__ __forceinline__ void single(const F3*) {}
     __device__ __forceinline__ void result(F3* o) const { o[0] = c0.result(); o[1] = c1.result(); o[2] = c2.result(); }
 };
+// Degree 3 (TripleProductEval, eq * f * g) by point values: h(x) = A(x) B(x)
+// C(x) at x = 0, 1, 2 and the leading coefficient (x = inf), 18 products per
+// point with the first product reduced (72 per pair instead of 90 for the
+// four coefficients); the last block turns them into the wire [h(0), h(inf),
+// h(2)] and the coefficients (c0, c1) of the per-round aux pair.
 template <u32 M>
 struct Policy<POL_C3, M> {
     static constexpr int NT = 3, NRAW = 4;
     static constexpr bool LSB_REMAINDER = false;
     static constexpr bool E0 = ext_of<M>(0), E1 = ext_of<M>(1), E2 = ext_of<M>(2);
     static constexpr bool EU = E0 || E1;
-    ProdAcc<EU, E2> c0, c1, c2, c3;
-    __device__ __forceinline__ void init() { c0.init(); c1.init(); c2.init(); c3.init(); }
-    __device__ __forceinline__ void pair(const F3* lo, const F3* hi) {
-        F3 da = f3_sub<E0>(hi[0], lo[0]), db = f3_sub<E1>(hi[1], lo[1]), dc = f3_sub<E2>(hi[2], lo[2]);
-        // (la + x da)(lb + x db) = u0 + u1 x + u2 x^2
-        F3 u0 = f3_mul<E0, E1>(lo[0], lo[1]);
-        ProdAcc<E0, E1> t;
-        t.init();
-        t.mac(lo[0], db);
-        t.mac(da, lo[1]);
-        F3 u1 = t.result();
-        F3 u2 = f3_mul<E0, E1>(da, db);
-        c0.mac(u0, lo[2]);
-        c1.mac(u0, dc);
-        c1.mac(u1, lo[2]);
-        c2.mac(u1, dc);
-        c2.mac(u2, lo[2]);
-        c3.mac(u2, dc);
+    ProdAcc<EU, E2> h0, h1, h2, hi;
+    __device__ __forceinline__ void init() { h0.init(); h1.init(); h2.init(); hi.init(); }
+    __device__ __forceinline__ void point(ProdAcc<EU, E2>& acc, const F3& a, const F3& b, const F3& c) {
+        acc.mac(f3_mul<E0, E1>(a, b), c);
+    }
+    __device__ __forceinline__ void pair(const F3* lo, const F3* hi_) {
+        const F3 da = f3_sub<E0>(hi_[0], lo[0]), db = f3_sub<E1>(hi_[1], lo[1]), dc = f3_sub<E2>(hi_[2], lo[2]);
+        point(h0, lo[0], lo[1], lo[2]);
+        point(h1, hi_[0], hi_[1], hi_[2]);
+        point(h2, f3_add<E0>(hi_[0], da), f3_add<E1>(hi_[1], db), f3_add<E2>(hi_[2], dc));
+        point(hi, da, db, dc);
     }
     __device__ __forceinline__ void tail(const F3*) {}
     __device__ __forceinline__ void single(const F3*) {}
     __device__ __forceinline__ void result(F3* o) const {
-        o[0] = c0.result(); o[1] = c1.result(); o[2] = c2.result(); o[3] = c3.result();
+        o[0] = h0.result(); o[1] = h1.result(); o[2] = h2.result(); o[3] = hi.result();
     }
 };
 
@@ -258,13 +256,17 @@ static __device__ __noinline__ void finalize_warp(int pol, const u64* raw, const
             w[0] = r[0]; w[1] = r[2];
             break;
         case POL_C3: {
-            w[0] = r[0]; w[1] = r[3];
-            // h(2) by Horner: ((c3*2 + c2)*2 + c1)*2 + c0
-            F3 h = r[3];
-            h = f3_add<true>(f3_add<true>(h, h), r[2]);
-            h = f3_add<true>(f3_add<true>(h, h), r[1]);
-            h = f3_add<true>(f3_add<true>(h, h), r[0]);
-            w[2] = h;
+            // r = h(0), h(1), h(2), h(inf): wire [h(0), h(inf), h(2)]; the
+            // aux pair is (c0, c1) of h = c0 + c1 x + c2 x^2 + c3 x^3:
+            // A = h(1) - c0 - c3 = c1 + c2, B = h(2) - c0 - 8 c3 = 2 c1 + 4 c2
+            w[0] = r[0]; w[1] = r[3]; w[2] = r[2];
+            const u64 inv2 = 0x7FFFFFFF80000001ULL;   // (p + 1) / 2
+            const F3 c3x2 = f3_add<true>(r[3], r[3]), c3x4 = f3_add<true>(c3x2, c3x2);
+            const F3 A = f3_sub<true>(f3_sub<true>(r[1], r[0]), r[3]);
+            const F3 B = f3_sub<true>(f3_sub<true>(r[2], r[0]), f3_add<true>(c3x4, c3x4));
+            const F3 t = f3_sub<true>(B, f3_add<true>(A, A));
+            const F3 c2 = f3_make(gl_mul(t.c0, inv2), gl_mul(t.c1, inv2), gl_mul(t.c2, inv2));
+            r[1] = f3_sub<true>(A, c2);
             break;
         }
         case POL_GKR: {
@@ -504,6 +506,12 @@ __device__ __forceinline__ void fused_body(const RoundArgs& a, u32 bid, u32 nb) 
 }
 template <int POL, int SEM, u32 M, bool ECH>
 __global__ void __launch_bounds__(TPB, 2) k_fused(RoundArgs a) {
+    fused_body<POL, SEM, M, ECH>(a, blockIdx.x, gridDim.x);
+}
+// Policies whose accumulators do not fit 128 registers (the degree-3 product
+// evaluator): one block per SM, no spills.
+template <int POL, int SEM, u32 M, bool ECH>
+__global__ void __launch_bounds__(TPB, 1) k_fused_wide(RoundArgs a) {
     fused_body<POL, SEM, M, ECH>(a, blockIdx.x, gridDim.x);
 }
 
