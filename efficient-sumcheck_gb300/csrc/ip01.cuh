@@ -38,6 +38,11 @@ __device__ __forceinline__ void ip01_quad(Acc (&s)[8], u64 a0, u64 a1, u64 a2, u
     acc_mac(s[7], da1, db1);
 }
 
+// LSB (pairs 2k, 2k+1, src/provers/inner_product_lsb.rs): quadruple k is
+// entries 4k .. 4k+3; round 0 pairs (4k, 4k+1), (4k+2, 4k+3) and round 1
+// pairs their folds, so it is the MSB quadruple with its middle two entries
+// exchanged.
+template <bool LSB>
 __device__ __forceinline__ void ip01_body(const RoundArgs& a, u32 bid, u32 nb) {
     Acc s[8];
 #pragma unroll
@@ -47,16 +52,26 @@ __device__ __forceinline__ void ip01_body(const RoundArgs& a, u32 bid, u32 nb) {
     const u64* B = a.t[1].in[0];
     const u64 tid = (u64)bid * TPB + threadIdx.x, stride = (u64)nb * TPB;
     u64 k = tid;
-    for (; k + stride < Q; k += 2 * stride) {
-        const u64 k2 = k + stride;
-        const u64 a0 = __ldcs(A + k), a1 = __ldcs(A + k + Q), a2 = __ldcs(A + k + 2 * Q), a3 = __ldcs(A + k + 3 * Q);
-        const u64 b0 = __ldcs(B + k), b1 = __ldcs(B + k + Q), b2 = __ldcs(B + k + 2 * Q), b3 = __ldcs(B + k + 3 * Q);
-        const u64 c0 = __ldcs(A + k2), c1 = __ldcs(A + k2 + Q), c2 = __ldcs(A + k2 + 2 * Q), c3 = __ldcs(A + k2 + 3 * Q);
-        const u64 e0 = __ldcs(B + k2), e1 = __ldcs(B + k2 + Q), e2 = __ldcs(B + k2 + 2 * Q), e3 = __ldcs(B + k2 + 3 * Q);
-        ip01_quad(s, a0, a1, a2, a3, b0, b1, b2, b3);
-        ip01_quad(s, c0, c1, c2, c3, e0, e1, e2, e3);
+    if (LSB) {
+        const ulonglong2* A2 = (const ulonglong2*)A;
+        const ulonglong2* B2 = (const ulonglong2*)B;
+        for (; k < Q; k += stride) {
+            const ulonglong2 xa = __ldcs(A2 + 2 * k), ya = __ldcs(A2 + 2 * k + 1);
+            const ulonglong2 xb = __ldcs(B2 + 2 * k), yb = __ldcs(B2 + 2 * k + 1);
+            ip01_quad(s, xa.x, ya.x, xa.y, ya.y, xb.x, yb.x, xb.y, yb.y);
+        }
+    } else {
+        for (; k + stride < Q; k += 2 * stride) {
+            const u64 k2 = k + stride;
+            const u64 a0 = __ldcs(A + k), a1 = __ldcs(A + k + Q), a2 = __ldcs(A + k + 2 * Q), a3 = __ldcs(A + k + 3 * Q);
+            const u64 b0 = __ldcs(B + k), b1 = __ldcs(B + k + Q), b2 = __ldcs(B + k + 2 * Q), b3 = __ldcs(B + k + 3 * Q);
+            const u64 c0 = __ldcs(A + k2), c1 = __ldcs(A + k2 + Q), c2 = __ldcs(A + k2 + 2 * Q), c3 = __ldcs(A + k2 + 3 * Q);
+            const u64 e0 = __ldcs(B + k2), e1 = __ldcs(B + k2 + Q), e2 = __ldcs(B + k2 + 2 * Q), e3 = __ldcs(B + k2 + 3 * Q);
+            ip01_quad(s, a0, a1, a2, a3, b0, b1, b2, b3);
+            ip01_quad(s, c0, c1, c2, c3, e0, e1, e2, e3);
+        }
+        if (k < Q) ip01_quad(s, A[k], A[k + Q], A[k + 2 * Q], A[k + 3 * Q], B[k], B[k + Q], B[k + 2 * Q], B[k + 3 * Q]);
     }
-    if (k < Q) ip01_quad(s, A[k], A[k + Q], A[k + 2 * Q], A[k + 3 * Q], B[k], B[k + Q], B[k + 2 * Q], B[k + 3 * Q]);
     F3 raw[3];
     raw[0] = f3_make(acc_reduce(s[0]), acc_reduce(s[1]), acc_reduce(s[2]));
     raw[1] = f3_make(acc_reduce(s[3]), acc_reduce(s[4]), acc_reduce(s[5]));
@@ -79,6 +94,9 @@ __device__ __forceinline__ F3 fold2(u64 x0, u64 x2, u64 x4, u64 x6, const F3& r0
     return f3_make(acc_reduce(c0), acc_reduce(c1), acc_reduce(c2));
 }
 
+// LSB: octet m is entries 8m .. 8m+7; entries 2m and 2m+1 of the length-L/4
+// table are fold2(y0, y2, y1, y3) and fold2(y4, y6, y5, y7).
+template <bool LSB>
 __device__ __forceinline__ void ip2x_body(const RoundArgs& a, u32 bid, u32 nb) {
     using P = Policy<POL_IP, 3>;
     P acc;
@@ -92,15 +110,37 @@ __device__ __forceinline__ void ip2x_body(const RoundArgs& a, u32 bid, u32 nb) {
     for (u64 m = tid; m < O; m += stride) {
         u64 x[2][8];
 #pragma unroll
-        for (int t = 0; t < 2; t++)
+        for (int t = 0; t < 2; t++) {
+            if (LSB) {
+                const ulonglong2* X2 = (const ulonglong2*)a.t[t].in[0] + 4 * m;
 #pragma unroll
-            for (int j = 0; j < 8; j++) x[t][j] = __ldcs(a.t[t].in[0] + m + j * O);
+                for (int j = 0; j < 4; j++) {
+                    const ulonglong2 v = __ldcs(X2 + j);
+                    x[t][2 * j] = v.x;
+                    x[t][2 * j + 1] = v.y;
+                }
+            } else {
+#pragma unroll
+                for (int j = 0; j < 8; j++) x[t][j] = __ldcs(a.t[t].in[0] + m + j * O);
+            }
+        }
 #pragma unroll
         for (int t = 0; t < 2; t++) {
-            lo[t] = fold2(x[t][0], x[t][2], x[t][4], x[t][6], r0, r1, r01);
-            hi[t] = fold2(x[t][1], x[t][3], x[t][5], x[t][7], r0, r1, r01);
-            st<true>(a.t[t].out, m, lo[t]);
-            st<true>(a.t[t].out, m + O, hi[t]);
+            if (LSB) {
+                lo[t] = fold2(x[t][0], x[t][2], x[t][1], x[t][3], r0, r1, r01);
+                hi[t] = fold2(x[t][4], x[t][6], x[t][5], x[t][7], r0, r1, r01);
+#pragma unroll
+                for (int c = 0; c < 3; c++) {
+                    const u64 l = c == 0 ? lo[t].c0 : c == 1 ? lo[t].c1 : lo[t].c2;
+                    const u64 h = c == 0 ? hi[t].c0 : c == 1 ? hi[t].c1 : hi[t].c2;
+                    ((ulonglong2*)a.t[t].out[c])[m] = make_ulonglong2(l, h);
+                }
+            } else {
+                lo[t] = fold2(x[t][0], x[t][2], x[t][4], x[t][6], r0, r1, r01);
+                hi[t] = fold2(x[t][1], x[t][3], x[t][5], x[t][7], r0, r1, r01);
+                st<true>(a.t[t].out, m, lo[t]);
+                st<true>(a.t[t].out, m + O, hi[t]);
+            }
         }
         acc.pair(lo, hi);
     }

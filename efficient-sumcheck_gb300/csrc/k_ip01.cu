@@ -4,15 +4,19 @@
 
 namespace effsc {
 
-__global__ void __launch_bounds__(TPB, 2) k_ip_r01(RoundArgs a) { ip01_body(a, blockIdx.x, gridDim.x); }
-__global__ void __launch_bounds__(TPB, 2) k_ip_r2x(RoundArgs a) { ip2x_body(a, blockIdx.x, gridDim.x); }
+template <bool LSB>
+__global__ void __launch_bounds__(TPB, 2) k_ip_r01(RoundArgs a) { ip01_body<LSB>(a, blockIdx.x, gridDim.x); }
+template <bool LSB>
+__global__ void __launch_bounds__(TPB, 2) k_ip_r2x(RoundArgs a) { ip2x_body<LSB>(a, blockIdx.x, gridDim.x); }
 
-bool launch_ip01(const RoundArgs& a, int grid, cudaStream_t s) {
-    k_ip_r01<<<grid, TPB, 0, s>>>(a);
+bool launch_ip01(bool lsb, const RoundArgs& a, int grid, cudaStream_t s) {
+    if (lsb) k_ip_r01<true><<<grid, TPB, 0, s>>>(a);
+    else k_ip_r01<false><<<grid, TPB, 0, s>>>(a);
     return true;
 }
-bool launch_ip2x(const RoundArgs& a, int grid, cudaStream_t s) {
-    k_ip_r2x<<<grid, TPB, 0, s>>>(a);
+bool launch_ip2x(bool lsb, const RoundArgs& a, int grid, cudaStream_t s) {
+    if (lsb) k_ip_r2x<true><<<grid, TPB, 0, s>>>(a);
+    else k_ip_r2x<false><<<grid, TPB, 0, s>>>(a);
     return true;
 }
 

@@ -59,8 +59,8 @@ __device__ __forceinline__ void serve_dispatch(const RoundArgs& sa, u32 code, u3
     case SERVE_FOLD_EXT: fused_body<POL, SEM_MSB_PAD, FULL, true>(sa, bid, nb); break;
     case SERVE_FINAL_BASE: final_body(sa, POL, false); break;
     case SERVE_FINAL_EXT: final_body(sa, POL, true); break;
-    case SERVE_IP01: if (POL == POL_IP) ip01_body(sa, bid, nb); break;
-    case SERVE_IP2X: if (POL == POL_IP) ip2x_body(sa, bid, nb); break;
+    case SERVE_IP01: if (POL == POL_IP) ip01_body<false>(sa, bid, nb); break;
+    case SERVE_IP2X: if (POL == POL_IP) ip2x_body<false>(sa, bid, nb); break;
     default: break;
     }
 }

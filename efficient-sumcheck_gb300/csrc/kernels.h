@@ -141,11 +141,11 @@ int fused_tma_blocks_per_sm(void);
 // mult with the challenge (L a power of two >= 4) and evaluate the folded
 // tables; otherwise evaluate the current ones.
 bool launch_gkr(bool fused, bool ea, bool ew, bool ech, const RoundArgs& a, int grid, cudaStream_t s);
-// InnerProduct MSB over Fp3 challenges, base tables of length L = 2^n >= 8:
+// InnerProduct (MSB or LSB) over Fp3 challenges, base tables of length L = 2^n >= 8:
 // rounds 0 and 1 from one read of the tables (launch_ip01), then round 2's
 // fold-twice-and-evaluate from a second read (launch_ip2x).
-bool launch_ip01(const RoundArgs& a, int grid, cudaStream_t s);
-bool launch_ip2x(const RoundArgs& a, int grid, cudaStream_t s);
+bool launch_ip01(bool lsb, const RoundArgs& a, int grid, cudaStream_t s);
+bool launch_ip2x(bool lsb, const RoundArgs& a, int grid, cudaStream_t s);
 void launch_batch_finalize(const RoundArgs* args, const unsigned char* ext, u32 n, int ntab, u64* finals, cudaStream_t s);
 
 // Utility kernels.

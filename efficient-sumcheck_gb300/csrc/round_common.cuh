@@ -475,18 +475,47 @@ __device__ __forceinline__ void fused_body(const RoundArgs& a, u32 bid, u32 nb) 
     const u64 Q = a.L >> 2;
     const u64 tid = (u64)bid * TPB + threadIdx.x, stride = (u64)nb * TPB;
     F3 lo[3], hi[3];
+    // LSB: 16-byte loads and stores when every component array is aligned
+    bool vec = false;
+    if (SEM == SEM_LSB) {
+        uintptr_t bits = 0;
+#pragma unroll
+        for (int t = 0; t < NT; t++)
+            for (int c = 0; c < 3; c++) bits |= (uintptr_t)a.t[t].in[c] | (uintptr_t)a.t[t].out[c];
+        vec = (bits & 15) == 0;
+    }
     for (u64 k = tid; k < Q; k += stride) {
 #pragma unroll
         for (int t = 0; t < NT; t++) {
             const bool EI = ext_of<M>(t);
             F3 x0, x1, x2, x3;
             if (SEM == SEM_LSB) {
-                if (EI) { x0 = ld<true>(a.t[t].in, 4 * k); x1 = ld<true>(a.t[t].in, 4 * k + 1); x2 = ld<true>(a.t[t].in, 4 * k + 2); x3 = ld<true>(a.t[t].in, 4 * k + 3); }
+                if (vec) {
+                    // entries 4k .. 4k+3 of each component as two 16-byte loads
+                    ulonglong2 v[3][2];
+#pragma unroll
+                    for (int c = 0; c < (EI ? 3 : 1); c++) {
+                        v[c][0] = ((const ulonglong2*)a.t[t].in[c])[2 * k];
+                        v[c][1] = ((const ulonglong2*)a.t[t].in[c])[2 * k + 1];
+                    }
+                    x0 = f3_make(v[0][0].x, EI ? v[1][0].x : 0, EI ? v[2][0].x : 0);
+                    x1 = f3_make(v[0][0].y, EI ? v[1][0].y : 0, EI ? v[2][0].y : 0);
+                    x2 = f3_make(v[0][1].x, EI ? v[1][1].x : 0, EI ? v[2][1].x : 0);
+                    x3 = f3_make(v[0][1].y, EI ? v[1][1].y : 0, EI ? v[2][1].y : 0);
+                }
+                else if (EI) { x0 = ld<true>(a.t[t].in, 4 * k); x1 = ld<true>(a.t[t].in, 4 * k + 1); x2 = ld<true>(a.t[t].in, 4 * k + 2); x3 = ld<true>(a.t[t].in, 4 * k + 3); }
                 else { x0 = ld<false>(a.t[t].in, 4 * k); x1 = ld<false>(a.t[t].in, 4 * k + 1); x2 = ld<false>(a.t[t].in, 4 * k + 2); x3 = ld<false>(a.t[t].in, 4 * k + 3); }
                 if (EI) { lo[t] = f3_fold<true, true>(x0, x1, r); hi[t] = f3_fold<true, true>(x2, x3, r); }
                 else if (ECH) { lo[t] = f3_fold<false, true>(x0, x1, r); hi[t] = f3_fold<false, true>(x2, x3, r); }
                 else { lo[t] = f3_fold<false, false>(x0, x1, r); hi[t] = f3_fold<false, false>(x2, x3, r); }
-                if (ext_of<MO>(t)) { st<true>(a.t[t].out, 2 * k, lo[t]); st<true>(a.t[t].out, 2 * k + 1, hi[t]); }
+                if (vec) {
+                    ((ulonglong2*)a.t[t].out[0])[k] = make_ulonglong2(lo[t].c0, hi[t].c0);
+                    if (ext_of<MO>(t)) {
+                        ((ulonglong2*)a.t[t].out[1])[k] = make_ulonglong2(lo[t].c1, hi[t].c1);
+                        ((ulonglong2*)a.t[t].out[2])[k] = make_ulonglong2(lo[t].c2, hi[t].c2);
+                    }
+                }
+                else if (ext_of<MO>(t)) { st<true>(a.t[t].out, 2 * k, lo[t]); st<true>(a.t[t].out, 2 * k + 1, hi[t]); }
                 else { st<false>(a.t[t].out, 2 * k, lo[t]); st<false>(a.t[t].out, 2 * k + 1, hi[t]); }
             } else {
                 if (EI) { x0 = ld<true>(a.t[t].in, k); x1 = ld<true>(a.t[t].in, k + Q); x2 = ld<true>(a.t[t].in, k + 2 * Q); x3 = ld<true>(a.t[t].in, k + 3 * Q); }

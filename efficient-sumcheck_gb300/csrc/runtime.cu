@@ -559,16 +559,20 @@ int do_tail(effsc_prover* P, size_t r, size_t num_rounds, const Chal& ch, const 
     return EFFSC_OK;
 }
 
-// effsc_prove of an MSB InnerProduct prover over Fp3 challenges whose base
+// effsc_prove of an InnerProduct prover (MSB or LSB) over Fp3 challenges whose base
 // tables are powers of two: rounds 0 and 1 from one pass, round 2 (with the
 // folds by r0 and r1) from a second (k_ip01.cu).  Leaves the state the
 // per-round path leaves after round 2.
 bool fuse_first_ok(const effsc_prover* P, size_t num_rounds) {
-    if (!P->fuse_first || P->kind != EFFSC_IP || P->order != EFFSC_MSB || P->field != EFFSC_FP3) return false;
+    if (!P->fuse_first || P->kind != EFFSC_IP || P->field != EFFSC_FP3) return false;
     if (num_rounds < 3) return false;
     const size_t L = P->t[0].len;
     if (P->t[1].len != L || !is_pow2(L) || L < 8 || P->t[0].ext || P->t[1].ext) return false;
     if (P->t[0].cur != 0 || P->t[1].cur != 0) return false;
+    // the LSB pass reads pairs of entries as one 16-byte load
+    if (P->order == EFFSC_LSB)
+        for (int i = 0; i < 2; i++)
+            if (((uintptr_t)P->t[i].bufs[0].p[0] & 15) != 0) return false;
     Chal none;
     return !tail_ok(P, 0, num_rounds, none);
 }
@@ -579,7 +583,7 @@ int do_fuse_first(effsc_prover* P, const TxIO& tx0, const TxIO& tx2, const u64* 
     a.tx = tx0;
     a.L = L;
     for (int i = 0; i < 2; i++) set_in(a, i, P->t[i]);
-    if (!dry) TRY(timed_launch(P->ctx->stream, "ip_rounds_0_1", 16 * (uint64_t)L, [&] { return launch_ip01(a, grid_for(L / 4), P->ctx->stream); }));
+    if (!dry) TRY(timed_launch(P->ctx->stream, "ip_rounds_0_1", 16 * (uint64_t)L, [&] { return launch_ip01(P->order == EFFSC_LSB, a, grid_for(L / 4), P->ctx->stream); }));
     int bi[2];
     for (int i = 0; i < 2; i++) TRY(out_buffer(P, P->t[i], true, L / 4, true, &bi[i]));
     RoundArgs b = base_args(P);
@@ -591,7 +595,7 @@ int do_fuse_first(effsc_prover* P, const TxIO& tx0, const TxIO& tx2, const u64* 
         set_in(b, i, P->t[i]);
         set_out(b, i, P->t[i].bufs[bi[i]]);
     }
-    if (!dry) TRY(timed_launch(P->ctx->stream, "ip_round_2_double_fold", 16 * (uint64_t)L + 12 * (uint64_t)L, [&] { return launch_ip2x(b, grid_for(L / 8), P->ctx->stream); }));
+    if (!dry) TRY(timed_launch(P->ctx->stream, "ip_round_2_double_fold", 16 * (uint64_t)L + 12 * (uint64_t)L, [&] { return launch_ip2x(P->order == EFFSC_LSB, b, grid_for(L / 8), P->ctx->stream); }));
     for (int i = 0; i < 2; i++) {
         Table& T = P->t[i];
         T.cur = bi[i];

@@ -26,11 +26,13 @@ def tables(n, seed):
 
 @pytest.mark.parametrize("n", [3, 4, 5, 7, 10, 13, 16])
 @pytest.mark.parametrize("hook", [b"", bytes(range(32)), b"\x05\x06\x07"])
-def test_full_runs(E, n, hook):
+@pytest.mark.parametrize("order", ["msb", "lsb"])
+def test_full_runs(E, n, hook, order):
     a, b = tables(n, 100 + n + len(hook))
-    p = E.InnerProductProver(a, b)
+    cls = E.InnerProductProver if order == "msb" else E.InnerProductProverLSB
+    p = cls(a, b)
     p.set_tail(0)
-    q = E.InnerProductProver(a, b)
+    q = cls(a, b)
     q.set_tail(0)
     q.set_first_rounds(False)
     for use_graph in (True, True, False):
@@ -41,19 +43,22 @@ def test_full_runs(E, n, hook):
         assert np.array_equal(x.round_polys, y.round_polys)
         assert np.array_equal(x.challenges, y.challenges)
         assert np.array_equal(x.final_value, y.final_value)
-    rp, ch, fv = O.sumcheck(O.Prover(O.IP, O.MSB, 3, [a, b]), n, O.Transcript(3, label=b"fr"), hook=hook)
+    rp, ch, fv = O.sumcheck(O.Prover(O.IP, O.MSB if order == "msb" else O.LSB, 3, [a, b]), n,
+                            O.Transcript(3, label=b"fr"), hook=hook)
     assert np.array_equal(x.round_polys, rp)
     assert np.array_equal(x.challenges, ch)
     assert np.array_equal(x.final_value, fv)
 
 
 @pytest.mark.parametrize("rounds", [1, 2, 3, 4, 6])
-def test_partial_runs_post_state(E, rounds):
+@pytest.mark.parametrize("order", ["msb", "lsb"])
+def test_partial_runs_post_state(E, rounds, order):
     n = 9
     a, b = tables(n, rounds)
-    p = E.InnerProductProver(a, b)
+    cls = E.InnerProductProver if order == "msb" else E.InnerProductProverLSB
+    p = cls(a, b)
     p.set_tail(0)
-    q = E.InnerProductProver(a, b)
+    q = cls(a, b)
     q.set_tail(0)
     q.set_first_rounds(False)
     x = p.prove(rounds, E.Transcript.keccak(3, b"pr"), hook=bytes(range(32)))
@@ -62,8 +67,8 @@ def test_partial_runs_post_state(E, rounds):
     assert np.array_equal(x.final_value, y.final_value)
     for t in range(2):
         assert np.array_equal(p.table(t), q.table(t))
-    rp, ch, fv = O.sumcheck(O.Prover(O.IP, O.MSB, 3, [a, b]), rounds, O.Transcript(3, label=b"pr"),
-                            hook=bytes(range(32)))
+    rp, ch, fv = O.sumcheck(O.Prover(O.IP, O.MSB if order == "msb" else O.LSB, 3, [a, b]), rounds,
+                            O.Transcript(3, label=b"pr"), hook=bytes(range(32)))
     assert np.array_equal(x.round_polys, rp)
     assert np.array_equal(x.final_value, fv)
 
