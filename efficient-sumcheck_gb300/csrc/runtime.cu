@@ -15,6 +15,8 @@
 #include <cstring>
 #include <string>
 #include <vector>
+#include <map>
+#include <mutex>
 
 using namespace effsc;
 
@@ -208,7 +210,35 @@ struct effsc_ctx {
     int device;
     cudaStream_t stream;
     cudaStream_t own;
+    // pinned, mapped host blocks returned by destroyed provers, by size, for
+    // the next provers (pinned allocation costs far more than a proof's
+    // small outputs)
+    std::mutex pin_mu;
+    std::multimap<size_t, void*> pin_free;
 };
+
+namespace {
+void* pinned_get(effsc_ctx* c, size_t bytes) {
+    {
+        std::lock_guard<std::mutex> g(c->pin_mu);
+        auto it = c->pin_free.find(bytes);
+        if (it != c->pin_free.end()) {
+            void* p = it->second;
+            c->pin_free.erase(it);
+            return p;
+        }
+    }
+    void* p = nullptr;
+    if (cudaHostAlloc(&p, bytes, cudaHostAllocMapped) != cudaSuccess) { cudaGetLastError(); return nullptr; }
+    return p;
+}
+void pinned_put(effsc_ctx* c, void* p, size_t bytes) {
+    if (!p) return;
+    std::lock_guard<std::mutex> g(c->pin_mu);
+    if (c->pin_free.size() < 64) c->pin_free.emplace(bytes, p);
+    else cudaFreeHost(p);
+}
+}  // namespace
 
 // ===========================================================================
 // prover state
@@ -271,6 +301,7 @@ struct effsc_prover {
     // effsc_prove outputs: pinned staging (wire | challenges | transcript |
     // first entries of the tables) and the device copy of the first entries
     u64* h_out = nullptr;
+    size_t h_out_bytes = 0;
     u64* d_first = nullptr;
 };
 
@@ -953,7 +984,8 @@ int prover_common_init(effsc_prover* P) {
     CK(cudaMallocAsync((void**)&P->partials, (size_t)max_grid() * 12 * sizeof(u64), s));
     CK(cudaMallocAsync((void**)&P->counter, 2 * sizeof(u32), s));
     CK(cudaMemsetAsync(P->counter, 0, 2 * sizeof(u32), s));
-    CK(cudaHostAlloc((void**)&P->h_res, 16 * sizeof(u64), cudaHostAllocMapped));
+    P->h_res = (u64*)pinned_get(P->ctx, 16 * sizeof(u64));
+    if (!P->h_res) return fail(EFFSC_OOM, "pinned result block");
     CK(cudaHostGetDevicePointer((void**)&P->d_res, P->h_res, 0));
     memset(P->h_res, 0, 16 * sizeof(u64));
     // word 15 of the mapped result block: kernel status (0 = ok)
@@ -1077,8 +1109,13 @@ void release_prover(effsc_prover* P) {
         if (P->gexec) cudaGraphExecDestroy(P->gexec);
         cudaStreamSynchronize(s);
     }
-    if (P->h_res) cudaFreeHost(P->h_res);
-    if (P->h_out) cudaFreeHost(P->h_out);
+    if (P->ctx) {
+        pinned_put(P->ctx, P->h_res, 16 * sizeof(u64));
+        pinned_put(P->ctx, P->h_out, P->h_out_bytes);
+    } else {
+        if (P->h_res) cudaFreeHost(P->h_res);
+        if (P->h_out) cudaFreeHost(P->h_out);
+    }
     delete P;
 }
 
@@ -1198,6 +1235,8 @@ int effsc_ctx_destroy(effsc_ctx* c) {
     if (!c) return EFFSC_OK;
     cudaSetDevice(c->device);
     cudaStreamSynchronize(c->stream);
+    for (auto& kv : c->pin_free) cudaFreeHost(kv.second);
+    c->pin_free.clear();
     cudaStreamDestroy(c->own);
     delete c;
     return EFFSC_OK;
@@ -1564,8 +1603,12 @@ int effsc_prove(effsc_prover* P, size_t num_rounds, effsc_transcript* T, const u
         size_t cap = std::max<size_t>(num_rounds, 1);
         CK(cudaMallocAsync((void**)&P->d_wire, cap * 9 * sizeof(u64), s));
         CK(cudaMallocAsync((void**)&P->d_chals, cap * 3 * sizeof(u64), s));
-        if (P->h_out) { CK(cudaStreamSynchronize(s)); cudaFreeHost(P->h_out); P->h_out = nullptr; }
-        CK(cudaHostAlloc((void**)&P->h_out, (cap * 12 + TX_OUT_WORDS + 12) * sizeof(u64), cudaHostAllocDefault));
+        if (P->h_out) { CK(cudaStreamSynchronize(s)); pinned_put(P->ctx, P->h_out, P->h_out_bytes); P->h_out = nullptr; }
+        // sized in steps of 64 rounds so that provers of similar size share blocks
+        const size_t capr = (cap + 63) / 64 * 64;
+        P->h_out_bytes = (capr * 12 + TX_OUT_WORDS + 12) * sizeof(u64);
+        P->h_out = (u64*)pinned_get(P->ctx, P->h_out_bytes);
+        if (!P->h_out) return fail(EFFSC_OOM, "pinned output block");
         if (!P->d_first) CK(cudaMallocAsync((void**)&P->d_first, 12 * sizeof(u64), s));
         P->rounds_cap = cap;
         if (P->gexec) { cudaGraphExecDestroy(P->gexec); P->gexec = nullptr; }
