@@ -457,6 +457,29 @@ def sumcheck_verify(claimed_sum, degree, num_rounds, transcript, round_polys, ho
     return ch, fc
 
 
+def sumcheck_verify_batch(claimed_sums, degree, round_polys, transcripts, hook=b"", field=FP3, ctx=None):
+    """sumcheck_verify (src/verifier.rs:61-139) for many proofs on the device.
+    round_polys: one array per proof of shape (rounds, max(degree, 1), field)
+    or (rounds, degree, field); transcripts: one per proof at its starting
+    state.  Returns (final_claims (n, field), challenges per proof)."""
+    ctx = ctx or Context.default()
+    n = len(round_polys)
+    nw = max(int(degree), 1)
+    rounds = [int(np.asarray(rp).shape[0]) for rp in round_polys]
+    flat = np.ascontiguousarray(np.concatenate(
+        [np.asarray(rp, dtype=np.uint64).reshape(-1) for rp in round_polys]) if n and sum(rounds)
+        else np.zeros(1, dtype=np.uint64))
+    cs = np.ascontiguousarray(np.asarray(claimed_sums, dtype=np.uint64).reshape(n, field))
+    fin = np.zeros((n, field), dtype=np.uint64)
+    ch = np.zeros((max(1, sum(rounds)), field), dtype=np.uint64)
+    hb, hn = _bytes(hook)
+    check(load().effsc_verify_batch(ctx.h, field, n, _p(cs), int(degree), (ctypes.c_uint32 * max(n, 1))(*rounds),
+                                    (vp * max(n, 1))(*[t.h for t in transcripts]), hb, hn, _p(flat), _p(ch),
+                                    _p(fin)))
+    offs = np.concatenate([[0], np.cumsum(rounds)])
+    return fin, [ch[offs[i]:offs[i + 1]] for i in range(n)]
+
+
 def fold(values, weight, field=FP3, repr=CANONICAL, ctx=None):
     """effsc::fold (src/fold.rs:14): half-split fold with implicit zero padding."""
     ctx = ctx or Context.default()

@@ -263,6 +263,20 @@ int effsc_diag_mulmod_rate(effsc_ctx* ctx, double* mulmod_per_s, double* fp3_mul
  * usable either way. */
 int effsc_diag_bounded_wait(effsc_ctx* ctx, uint64_t limit_ns, int arrive, uint32_t* status);
 
+/* sumcheck_verify (src/verifier.rs:61-139) for n proofs at once on the
+ * device (no reference counterpart for the batch; the serving loop's
+ * self-check): proof i has num_rounds[i] rounds of `degree` (0..3) wire
+ * elements each, rows concatenated in proof order (round_polys: max(degree,
+ * 1) elements per row, `field` canonical words per element), its claimed sum
+ * and the transcript state it starts from; the same hook bytes are absorbed
+ * every round.  Writes each proof's final claim (and, if challenges is not
+ * NULL, the recomputed challenges per row).  The caller compares final_claim
+ * with the evaluation it expects (for proofs of this library: the proof's
+ * final value).  The transcripts are not modified. */
+int effsc_verify_batch(effsc_ctx* ctx, int field, size_t n, const uint64_t* claimed_sums, int degree,
+                       const uint32_t* num_rounds, const effsc_transcript* const* transcripts, const uint8_t* hook,
+                       size_t hook_len, const uint64_t* round_polys, uint64_t* challenges, uint64_t* final_claims);
+
 /* ---- batches: many independent provers, one launch per round -------------
  * No reference counterpart (the crate proves one instance per call).  A batch
  * holds n_inst InnerProductProver (kind EFFSC_IP, tables a and b) or
