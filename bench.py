@@ -834,7 +834,66 @@ def run_configs(args, E, L, ctx, stream, rank):
         "device_table_bytes_if_uploaded": 2 * N * 8 + 2 * 3 * (N // 4) * 8,
         "bit_exact_vs_oracle": ok_h}
     del hp, ah, bh
+    res["protogalaxy_fold"] = run_pg_fold(E, L, ctx, stream, check)
     return res
+
+
+def run_pg_fold(E, L, ctx, stream, check, steps=20):
+    """protogalaxy::fold (effsc_protogalaxy_fold) on 2^22 polynomials of
+    degree 7 over Fp (256 MiB) and 2^20 over Fp3 (192 MiB), all levels,
+    coefficients resident in HBM (generated on the device); the call's own
+    time (pairs upload, the passes, result read-back) by CUDA events, and the
+    oracle on the same input for parity and the CPU time."""
+    import numpy as np
+    import torch
+    from effsc_gpu import _lib
+    out = {}
+    for field, logn in ((1, 22), (3, 20)):
+        n, width = 1 << logn, 8
+        words = n * width * field
+        buf = torch.empty(words, dtype=torch.int64, device="cuda")
+        _lib.check(L.effsc_gen_uniform(ctx.h, E.table_seed(0x9A1F_2026, field), words,
+                                       _lib.ctypes.cast(_lib.ctypes.c_void_p(buf.data_ptr()), _lib.u64p), None))
+        pairs = [tuple(E.gen_uniform(E.table_seed(0x9A1F_2026, 100 + 2 * k + h), field, ctx=ctx) for h in range(2))
+                 for k in range(logn)]
+
+        def fold():
+            return E.protogalaxy_fold_raw(pairs, buf.data_ptr(), n, width, field=field, ctx=ctx)
+
+        for _ in range(3):
+            got = fold()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t0 = time.perf_counter()
+        e0.record(stream)
+        for _ in range(steps):
+            got = fold()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        wall_ms = (time.perf_counter() - t0) * 1e3 / steps
+        ms = e0.elapsed_time(e1) / steps
+        E.launch_count_reset()
+        fold()
+        launches = E.launch_count()
+        in_bytes = words * 8
+        ok, cpu_s = None, None
+        if check:
+            from oracle import oracle as O
+            host = buf.cpu().numpy().view(np.uint64).reshape((n, width) if field == 1 else (n, width, 3))
+            t0 = time.perf_counter()
+            want = O.protogalaxy_fold(pairs, host)
+            cpu_s = time.perf_counter() - t0
+            ok = bool(np.array_equal(np.asarray(got).reshape(-1, field), want[:, :field]) and not want[:, field:].any())
+            assert ok, "protogalaxy fold differs from the oracle"
+        out["%s_n2^%d_deg%d" % ("fp" if field == 1 else "fp3", logn, width - 1)] = {
+            "workload": "protogalaxy::fold of 2^%d seeded uniform %s polynomials of degree %d (AoS, %d MiB), %d levels "
+                        "with seeded (a, b), result of degree %d" % (logn, "Fp" if field == 1 else "Fp3", width - 1,
+                                                                     in_bytes >> 20, logn, width - 1 + logn),
+            "ms_per_fold": ms, "wall_ms_per_fold": wall_ms, "coefficients_per_s": n * width / (ms * 1e-3),
+            "input_bytes": in_bytes, "hbm_gbs": in_bytes / (ms * 1e-3) / 1e9, "launches_per_fold": launches,
+            "cpu_oracle_s": cpu_s, "cpu_cores": os.cpu_count(), "bit_exact_vs_oracle": ok}
+        del buf
+    return out
 
 
 # ---------------------------------------------------------------------------

@@ -11,5 +11,6 @@ from .api import (  # noqa: F401
     SumcheckProof, Transcript, build_eq_table, fold, gen_uniform, inner_product_sumcheck,
     inner_product_sumcheck_partial, launch_count, launch_count_reset, multilinear_sumcheck,
     multilinear_sumcheck_partial, noop_hook, sumcheck, sumcheck_verify, sumcheck_verify_batch, table_seed,
+    protogalaxy_fold, protogalaxy_fold_raw,
     FileStream, MemoryStream, multivariate_claim, multivariate_product_claim, reorder_vec_msb,
 )

@@ -457,6 +457,45 @@ def sumcheck_verify(claimed_sum, degree, num_rounds, transcript, round_polys, ho
     return ch, fc
 
 
+def protogalaxy_fold(coeffs, polys, field=FP, ctx=None):
+    """protogalaxy::fold (src/folding.rs:14-75) on the device.  coeffs: the
+    (a, b) pairs, one per level; polys: a list of coefficient arrays
+    (ascending degree; `field` words per coefficient) or one zero-padded
+    array of shape (n, width) for Fp, (n, width, 3) for Fp3 (for device
+    memory see `protogalaxy_fold_raw`).  Returns the coefficients of the
+    result, trailing zeros trimmed, shape (len,) for Fp and (len, 3) for
+    Fp3."""
+    ctx = ctx or Context.default()
+    pairs = [(_elem(a, field), _elem(b, field)) for a, b in coeffs]
+    if isinstance(polys, np.ndarray) and polys.ndim == (2 if field == 1 else 3):
+        n, width = polys.shape[0], polys.shape[1]
+        buf = np.ascontiguousarray(polys.astype(np.uint64, copy=False))
+    else:
+        rows = [np.asarray(p, dtype=np.uint64).reshape(-1, field) for p in polys]
+        n = len(rows)
+        width = max([r.shape[0] for r in rows] + [0])
+        buf = np.zeros((max(n, 1), max(width, 1) * field), dtype=np.uint64)
+        for i, r in enumerate(rows):
+            buf[i, :r.shape[0] * field] = r.reshape(-1)
+    return protogalaxy_fold_raw(pairs, buf.ctypes.data, n, width, field, ctx)
+
+
+def protogalaxy_fold_raw(pairs, polys_ptr, n, width, field=FP, ctx=None):
+    """The same on a raw pointer to n x width coefficients (device, pinned or
+    host memory); pairs as (a, b) tuples of `field`-word arrays."""
+    ctx = ctx or Context.default()
+    pr = np.zeros((max(len(pairs), 1), 2, field), dtype=np.uint64)
+    for k, (a, b) in enumerate(pairs):
+        pr[k, 0], pr[k, 1] = _elem(a, field), _elem(b, field)
+    out = np.zeros((max(width + len(pairs), 1), field), dtype=np.uint64)
+    n_out = ctypes.c_size_t(0)
+    check(load().effsc_protogalaxy_fold(ctx.h, field, _p(pr), len(pairs),
+                                        ctypes.cast(polys_ptr, u64p) if polys_ptr else None, n, width, _p(out),
+                                        ctypes.byref(n_out)))
+    res = out[: n_out.value]
+    return res.reshape(-1) if field == 1 else res.copy()
+
+
 def sumcheck_verify_batch(claimed_sums, degree, round_polys, transcripts, hook=b"", field=FP3, ctx=None):
     """sumcheck_verify (src/verifier.rs:61-139) for many proofs on the device.
     round_polys: one array per proof of shape (rounds, max(degree, 1), field)

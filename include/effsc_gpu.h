@@ -277,6 +277,24 @@ int effsc_verify_batch(effsc_ctx* ctx, int field, size_t n, const uint64_t* clai
                        const uint32_t* num_rounds, const effsc_transcript* const* transcripts, const uint8_t* hook,
                        size_t hook_len, const uint64_t* round_polys, uint64_t* challenges, uint64_t* final_claims);
 
+/* protogalaxy::fold (src/folding.rs:14-75): folds n_polys univariate
+ * polynomials with n_levels pairs (a, b), level k replacing neighbours
+ * p[2i], p[2i+1] by p[2i] + (a_k + b_k X)(p[2i+1] - p[2i]).  Release-build
+ * semantics: an odd last polynomial is dropped at its level and levels after
+ * a single polynomial remains change nothing (the reference debug-asserts
+ * n_polys == 2^n_levels).
+ *   pairs:  n_levels x (a, b), `field` canonical words per element.
+ *   polys:  n_polys rows of `width` coefficients (ascending degree, zero-
+ *           padded, canonical), `field` words each; device, pinned or host
+ *           memory.
+ *   out:    host, capacity max(width + n_levels, 1) elements; *out_len = the
+ *           number of coefficients of the result with trailing zeros trimmed:
+ *           0 for n_polys = 0, the input's own trimmed length for
+ *           n_polys = 1, at least 1 otherwise (to_dense_poly,
+ *           src/poly_ops.rs:159-166). */
+int effsc_protogalaxy_fold(effsc_ctx* ctx, int field, const uint64_t* pairs, size_t n_levels, const uint64_t* polys,
+                           size_t n_polys, size_t width, uint64_t* out, size_t* out_len);
+
 /* ---- batches: many independent provers, one launch per round -------------
  * No reference counterpart (the crate proves one instance per call).  A batch
  * holds n_inst InnerProductProver (kind EFFSC_IP, tables a and b) or

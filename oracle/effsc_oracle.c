@@ -84,6 +84,7 @@ static inline or_f f_mul(or_f a, or_f b) {
     r.c[2] = or_fp_add(or_fp_add(or_fp_mul(a0, b2), or_fp_mul(a1, b1)), or_fp_mul(a2, b0));
     return r;
 }
+static inline int f_eq(or_f a, or_f b) { return a.c[0] == b.c[0] && a.c[1] == b.c[1] && a.c[2] == b.c[2]; }
 static inline or_f f_from_u64(uint64_t x) { or_f r = {{x % OR_P, 0, 0}}; return r; }
 static inline or_f f_load(const uint64_t* p) { or_f r = {{p[0], p[1], p[2]}}; return r; }
 static inline void f_store(uint64_t* p, or_f a) { p[0] = a.c[0]; p[1] = a.c[1]; p[2] = a.c[2]; }
@@ -825,6 +826,63 @@ void or_mle_eval_msb(const uint64_t* table, size_t len, const uint64_t* point, s
     }
     f_store(out, n ? cur[0] : F_ZERO);
     free(cur);
+}
+
+/* protogalaxy::fold (src/folding.rs:14-75) as a release build runs it:
+ * level k pairs polynomial 2i with 2i+1 (an odd last one is dropped) into
+ * p[2i] + (a_k + b_k X)(p[2i+1] - p[2i]), each level raising the degree
+ * bound by one; levels after a single polynomial remains change nothing.
+ * polys: n rows of `width` coefficients (ncomp = 1 or 3 words each,
+ * ascending degree, zero-padded); pairs: levels x (a, b), 3 words each.  out: width + levels coefficients;
+ * *out_len = the length of the result with trailing zeros trimmed -- at
+ * least 1 for n >= 2 (to_dense_poly, src/poly_ops.rs:159-166), 0 for the
+ * zero polynomial at n = 0, the input's own trimmed length at n = 1. */
+void or_pg_fold(const uint64_t* pairs, size_t levels, const uint64_t* polys, size_t n, size_t width, int ncomp,
+                uint64_t* out, size_t* out_len) {
+    const size_t slot = width + levels;
+    size_t len = 0;
+    for (size_t j = 0; j < slot; j++) f_store(out + 3 * j, F_ZERO);
+    if (n == 0) { *out_len = 0; return; }
+    or_f* buf = (or_f*)calloc(n * (slot ? slot : 1), sizeof(or_f));
+    for (size_t i = 0; i < n; i++)
+        for (size_t j = 0; j < width; j++) {
+            const uint64_t* src = polys + (size_t)ncomp * (i * width + j);
+            or_f x = F_ZERO;
+            for (int c = 0; c < ncomp; c++) x.c[c] = src[c];
+            buf[i * slot + j] = x;
+        }
+    size_t count = n, w = width;
+    if (n >= 2) {
+        for (size_t k = 0; k < levels && count >= 2; k++) {
+            const or_f a = f_load(pairs + 6 * k), b = f_load(pairs + 6 * k + 3);
+            const size_t half = count / 2;
+            or_f* nxt = (or_f*)calloc(half * slot, sizeof(or_f));
+            #pragma omp parallel for schedule(static) if (half * w > PAR_MIN)
+            for (size_t i = 0; i < half; i++) {
+                const or_f* p0 = buf + 2 * i * slot;
+                const or_f* p1 = buf + (2 * i + 1) * slot;
+                or_f prev = F_ZERO;
+                for (size_t j = 0; j <= w; j++) {
+                    const or_f d = j < w ? f_sub(p1[j], p0[j]) : F_ZERO;
+                    const or_f base = j < w ? p0[j] : F_ZERO;
+                    nxt[i * slot + j] = f_add(base, f_add(f_mul(a, d), f_mul(b, prev)));
+                    prev = d;
+                }
+            }
+            free(buf);
+            buf = nxt;
+            count = half;
+            w++;
+        }
+        len = w;
+        while (len > 1 && f_eq(buf[len - 1], F_ZERO)) len--;
+    } else {
+        len = width;
+        while (len > 0 && f_eq(buf[len - 1], F_ZERO)) len--;
+    }
+    for (size_t j = 0; j < len; j++) f_store(out + 3 * j, buf[j]);
+    *out_len = len;
+    free(buf);
 }
 
 void or_set_threads(int n) {

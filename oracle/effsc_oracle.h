@@ -123,6 +123,13 @@ int or_verify(const uint64_t* claimed_sum, size_t degree, size_t num_rounds,
 void or_build_eq_table(const uint64_t* w, size_t v, uint64_t* out /* 3 * 2^v */);
 void or_mle_eval_msb(const uint64_t* table, size_t len, const uint64_t* point, size_t v, uint64_t* out);
 
+/* protogalaxy::fold (src/folding.rs:14-75), release-build semantics: n
+ * polynomials of `width` coefficients (ncomp words each, zero-padded), `levels`
+ * pairs (a, b); out holds width + levels coefficients, *out_len the trimmed
+ * length (>= 1 for n >= 2, 0 for n = 0). */
+void or_pg_fold(const uint64_t* pairs, size_t levels, const uint64_t* polys, size_t n, size_t width, int ncomp,
+                uint64_t* out, size_t* out_len);
+
 void or_set_threads(int n);
 int  or_get_threads(void);
 

@@ -85,6 +85,8 @@ def lib():
                                 ctypes.c_size_t, _u64p, _u64p, _u64p]
         L.or_build_eq_table.argtypes = [_u64p, ctypes.c_size_t, _u64p]
         L.or_mle_eval_msb.argtypes = [_u64p, ctypes.c_size_t, _u64p, ctypes.c_size_t, _u64p]
+        L.or_pg_fold.argtypes = [_u64p, ctypes.c_size_t, _u64p, ctypes.c_size_t, ctypes.c_size_t, ctypes.c_int,
+                                 _u64p, ctypes.POINTER(ctypes.c_size_t)]
         L.or_set_threads.argtypes = [ctypes.c_int]
         L.or_get_threads.restype = ctypes.c_int
         _lib = L
@@ -307,6 +309,35 @@ def mle_eval_msb(table, point):
     out = np.zeros(3, dtype=np.uint64)
     lib().or_mle_eval_msb(_p(t), t.shape[0], _p(pt), pt.shape[0], _p(out))
     return out
+
+
+def protogalaxy_fold(pairs, polys):
+    """protogalaxy::fold (reference src/folding.rs:14-75), release-build
+    semantics.  pairs: (a, b) per level, field elements (1 or 3 words);
+    polys: a list of coefficient arrays (ascending degree; 1 or 3 words per
+    coefficient), or one zero-padded array of shape (n, width) (base field)
+    or (n, width, 3).  Returns the trimmed coefficients as an (len, 3) array."""
+    pr = np.zeros((max(len(pairs), 1), 2, 3), dtype=np.uint64)
+    for k, (a, b) in enumerate(pairs):
+        pr[k, 0], pr[k, 1] = as_f(a), as_f(b)
+    if isinstance(polys, np.ndarray) and polys.ndim in (2, 3):
+        buf = np.ascontiguousarray(polys, dtype=np.uint64)
+        n, width = buf.shape[0], buf.shape[1]
+        ncomp = 1 if buf.ndim == 2 else 3
+    else:
+        rows = [np.asarray(p, dtype=np.uint64).reshape(len(p), -1) if len(p) else np.zeros((0, 3), np.uint64)
+                for p in polys]
+        n = len(rows)
+        width = max([r.shape[0] for r in rows] + [0])
+        buf = np.zeros((max(n, 1), width, 3), dtype=np.uint64)
+        for i, r in enumerate(rows):
+            buf[i, :r.shape[0], :r.shape[1]] = r
+        ncomp = 3
+    out = np.zeros((width + len(pairs) + 1, 3), dtype=np.uint64)
+    n_out = ctypes.c_size_t(0)
+    lib().or_pg_fold(_p(pr), len(pairs), _p(buf) if buf.size else None, n, width, ncomp, _p(out),
+                     ctypes.byref(n_out))
+    return out[: n_out.value].copy()
 
 
 def fp_mul(a, b):

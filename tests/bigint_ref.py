@@ -321,3 +321,41 @@ class RefGkr:
         A, M, B, C = self.t
         return self.term(A[0], M[0], B[0], C[0]) if len(A) == 1 else ZERO
 
+
+
+def poly_trim(c):
+    c = list(c)
+    while c and c[-1] == ZERO:
+        c.pop()
+    return c
+
+
+def poly_add(p, q):
+    n = max(len(p), len(q))
+    return poly_trim([add(p[i] if i < len(p) else ZERO, q[i] if i < len(q) else ZERO) for i in range(n)])
+
+
+def poly_sub(p, q):
+    n = max(len(p), len(q))
+    return poly_trim([sub(p[i] if i < len(p) else ZERO, q[i] if i < len(q) else ZERO) for i in range(n)])
+
+
+def poly_mul(p, q):
+    if not p or not q:
+        return []
+    out = [ZERO] * (len(p) + len(q) - 1)
+    for i, x in enumerate(p):
+        for j, y in enumerate(q):
+            out[i + j] = add(out[i + j], mul(x, y))
+    return poly_trim(out)
+
+
+def protogalaxy_fold_naive(pairs, polys):
+    """The naive fold of src/folding.rs:124-137 (tests): per level, each pair
+    of neighbours becomes p0 + (a + b X) (p1 - p0), with normalised dense
+    polynomials (trailing zeros dropped, zero = [])."""
+    ps = [poly_trim(p) for p in polys]
+    for a, b in pairs:
+        ps = [poly_add(ps[2 * i], poly_mul(poly_trim([a, b]), poly_sub(ps[2 * i + 1], ps[2 * i])))
+              for i in range(len(ps) // 2)]
+    return ps[0]

@@ -448,3 +448,53 @@ def test_gkr_zero_gates_and_add_only():
     _, fc = O.verify(s, 2, 2 * k, O.Transcript(3, label=b"a"), rp)
     assert (fc == fv).all()
 
+
+
+# ---- protogalaxy::fold (src/folding.rs:14-75) ----------------------------------
+def test_pg_fold_two_polys():
+    """src/folding.rs:82-98: p0 = 1, p1 = X, (a, b) = (3, 5) gives
+    (1 - a) + (a - b) X + b X^2."""
+    r = O.protogalaxy_fold([(3, 5)], [[1], [0, 1]])
+    assert [int(x) for x in r[:, 0]] == [(1 - 3) % O.P, (3 - 5) % O.P, 5]
+    assert not r[:, 1:].any()
+
+
+def test_pg_fold_four_polys():
+    """src/folding.rs:100-114: constants 1..4 with (1, 0) at both levels
+    select the last one."""
+    r = O.protogalaxy_fold([(1, 0)] * 2, [[1], [2], [3], [4]])
+    assert r.shape[0] == 1 and int(r[0, 0]) == 4
+
+
+@pytest.mark.parametrize("n,deg,ext", [(8, 2, False), (16, 5, True), (32, 0, False), (2, 3, True)])
+def test_pg_fold_matches_naive(n, deg, ext):
+    """src/folding.rs:116-162: random polynomials of degree `deg`, log2 n
+    levels, against the naive per-level polynomial arithmetic."""
+    rng = random.Random(n * 31 + deg)
+    el = (lambda: (rng.randrange(R.P), rng.randrange(R.P), rng.randrange(R.P))) if ext else \
+        (lambda: (rng.randrange(R.P), 0, 0))
+    polys = [[el() for _ in range(deg + 1)] for _ in range(n)]
+    pairs = [(el(), el()) for _ in range(n.bit_length() - 1)]
+    got = O.protogalaxy_fold(pairs, [np.array(p, dtype=np.uint64) for p in polys])
+    want = R.protogalaxy_fold_naive(pairs, polys)
+    assert [tuple(int(x) for x in row) for row in got] == want
+
+
+def test_pg_fold_edges():
+    P = O.P
+    assert O.protogalaxy_fold([], []).shape[0] == 0                       # no polynomials: zero
+    assert O.protogalaxy_fold([(1, 2)], [[5, 7, 0]]).tolist() == [[5, 0, 0], [7, 0, 0]]   # one: itself
+    assert O.protogalaxy_fold([(1, 2)], [[0, 0]]).shape[0] == 0           # one zero polynomial
+    assert O.protogalaxy_fold([(3, 4)], [[1], [1]]).tolist() == [[1, 0, 0]]  # zero difference: [p0], >= 1 term
+    assert O.protogalaxy_fold([(3, 4)], [[], []]).tolist() == [[0, 0, 0]]
+    # odd count: the last polynomial is dropped at the level it is left over
+    a = O.protogalaxy_fold([(3, 4)], [[1], [2], [9]])
+    b = O.protogalaxy_fold([(3, 4)], [[1], [2]])
+    assert a.tolist() == b.tolist()
+    # more levels than log2 n: the extra levels change nothing
+    c = O.protogalaxy_fold([(3, 4), (5, 6), (7, 8)], [[1], [2]])
+    assert c.tolist() == b.tolist()
+    # fewer levels than log2 n: the result is the first of the remaining polynomials
+    d = O.protogalaxy_fold([(3, 4)], [[1], [2], [10], [20]])
+    assert d.tolist() == b.tolist()
+    assert int(b[0, 0]) == (1 + 3 * (2 - 1)) % P and int(b[1, 0]) == 4
