@@ -60,6 +60,8 @@ def parse():
                     help="serving leg: this many requests, 70%% IP / 30%% ML, num_vars uniform on 14..=26 (0 = skip)")
     ap.add_argument("--serve-slots", type=int, default=128)
     ap.add_argument("--serve-budget-gb", type=float, default=150.0)
+    ap.add_argument("--only", choices=["protogalaxy_fold"],
+                    help="run one secondary workload alone and print its record (for profiling)")
     return ap.parse_args()
 
 
@@ -979,10 +981,24 @@ def run_serving(args, E, ctx):
 
 def main():
     args = parse()
-    if args.impl == "reference":
+    if args.only:
+        run_only(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_ours(args)
+
+
+def run_only(args):
+    import torch
+    import effsc_gpu as E
+    L = E.load()
+    ctx = E.Context(0)
+    stream = torch.cuda.current_stream()
+    ctx.set_stream(stream.cuda_stream)
+    if args.only == "protogalaxy_fold":
+        rec = run_pg_fold(E, L, ctx, stream, not args.no_cpu_baseline, steps=max(args.steps, 1))
+    print(json.dumps({"only": args.only, "record": rec}))
 
 
 if __name__ == "__main__":

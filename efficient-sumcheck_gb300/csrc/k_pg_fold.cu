@@ -31,7 +31,8 @@ const u64* effsc_internal_device_view(int device, const uint64_t* ptr, bool* is_
 namespace effsc {
 
 constexpr int PG_TPB = 256;
-constexpr size_t PG_SMEM = 48 * 1024;   // per block: four blocks per SM
+constexpr size_t PG_SMEM = 48 * 1024;        // wide grids: four blocks per SM
+constexpr size_t PG_SMEM_BIG = 200 * 1024;   // narrow grids: fewer passes
 constexpr u32 PG_MAX_G = 10;
 
 template <bool E>
@@ -65,44 +66,142 @@ __device__ __forceinline__ F3 pg_coef(const F3& p0, const F3& d, const F3& dm1, 
     return r;
 }
 
-// One block folds g levels of 2^g consecutive rows of width w.  Shared
-// memory: A (2^g rows) and B (2^(g-1) rows), row stride w + g coefficients.
 template <bool E>
-__global__ void __launch_bounds__(PG_TPB) k_pg_group(const u64* __restrict__ in, u32 w, u32 g,
+__device__ __forceinline__ Mul3 pg_mul3(const u64* q) {
+    Mul3 m;
+    m.m0 = q[0];
+    m.m1 = E ? q[1] : 0;
+    m.m2 = E ? q[2] : 0;
+    m.w1 = E ? q[3] : 0;
+    m.w2 = E ? q[4] : 0;
+    return m;
+}
+
+// One block folds g levels of R = 2^g consecutive rows of width w.
+// Shared-memory layout: rows are kept as pairs, pair k of a level at k * P
+// (P = 2 S + 1 coefficients, S >= w + g the widest row), its first row at
+// +0 and its second at +S; the odd pair stride spreads the rows that
+// neighbouring threads read over all banks.  Buffer A holds the R rows of
+// level 0 (R/2 pairs), B the R/2 rows of level 1; the levels then alternate.
+// The group arrives by 8-byte asynchronous copies (cp.async, no register
+// staging).  Each level gives every row pair TPB/cnt threads (or every
+// thread whole pairs when cnt >= TPB), each computing a run of consecutive
+// coefficients, so d[j-1] carries over in a register.
+__device__ __forceinline__ void pg_cp8(u64* dst, const u64* src) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(d), "l"(src) : "memory");
+}
+
+template <bool E>
+__global__ void __launch_bounds__(PG_TPB) k_pg_group(const u64* __restrict__ in, u32 w, u32 g, u32 S,
                                                      const u64* __restrict__ pairs, u64* __restrict__ out) {
     extern __shared__ u64 sm[];
     constexpr u32 EW = E ? 3 : 1;
-    const u32 S = w + g, R = 1u << g;
+    const u32 R = 1u << g, P = 2 * S + 1;
     u64* A = sm;
-    u64* B = sm + (size_t)R * S * EW;
-    const u32 row_words = w * EW;
-    const u64* src = in + (size_t)blockIdx.x * R * row_words;
-    for (u32 t = threadIdx.x; t < R * row_words; t += PG_TPB) {
-        const u32 row = t / row_words, rem = t - row * row_words;
-        A[row * S * EW + rem] = src[t];
+    u64* B = sm + (size_t)(R / 2) * P * EW;
+    const u32 row_words = w * EW, total = R * row_words;
+    const u64* src = in + (size_t)blockIdx.x * total;
+    {
+        u32 row = threadIdx.x / row_words, col = threadIdx.x - row * row_words;
+        const u32 step_r = PG_TPB / row_words, step_c = PG_TPB - step_r * row_words;
+        for (u32 t = threadIdx.x; t < total; t += PG_TPB) {
+            pg_cp8(A + ((row >> 1) * P + (row & 1) * S) * EW + col, src + t);
+            row += step_r;
+            col += step_c;
+            if (col >= row_words) { col -= row_words; row++; }
+        }
+        asm volatile("cp.async.wait_all;" ::: "memory");
     }
     __syncthreads();
     for (u32 l = 0; l < g; l++) {
         const u64* s = (l & 1) ? B : A;
         u64* d = (l & 1) ? A : B;
-        const u32 cnt = R >> (l + 1), wl = w + l, wo = wl + 1;
-        const Mul3 ma = mul3_prepare<E>(f3_make(pairs[6 * l], pairs[6 * l + 1], pairs[6 * l + 2]));
-        const Mul3 mb = mul3_prepare<E>(f3_make(pairs[6 * l + 3], pairs[6 * l + 4], pairs[6 * l + 5]));
-        for (u32 idx = threadIdx.x; idx < cnt * wo; idx += PG_TPB) {
-            const u32 i = idx / wo, j = idx - i * wo;
-            const u64* p0 = s + (size_t)(2 * i) * S * EW;
+        const u32 lg_cnt = g - l - 1, cnt = 1u << lg_cnt, wl = w + l, wo = wl + 1;
+        const Mul3 ma = pg_mul3<E>(pairs + 10 * l), mb = pg_mul3<E>(pairs + 10 * l + 5);
+        // threads per pair (a power of two) and the run each computes
+        const u32 lg_tpp = cnt >= PG_TPB ? 0 : __ffs(PG_TPB) - 1 - lg_cnt;
+        const u32 tpp = 1u << lg_tpp, run = (wo + tpp - 1) >> lg_tpp;
+        const u32 part = threadIdx.x & (tpp - 1);
+        const u32 j0 = part * run, j1 = min(j0 + run, wo);
+        for (u32 i = threadIdx.x >> lg_tpp; i < cnt; i += PG_TPB >> lg_tpp) {
+            if (j0 >= j1) break;
+            const u64* p0 = s + (size_t)i * P * EW;
             const u64* p1 = p0 + (size_t)S * EW;
-            const F3 z = f3_zero();
-            const F3 b0 = j < wl ? pg_load<E>(p0, j) : z;
-            const F3 dj = j < wl ? f3_sub<E>(pg_load<E>(p1, j), b0) : z;
-            const F3 dm = j > 0 ? f3_sub<E>(pg_load<E>(p1, j - 1), pg_load<E>(p0, j - 1)) : z;
-            pg_store<E>(d + (size_t)i * S * EW, j, pg_coef<E>(b0, dj, dm, ma, mb));
+            u64* o = d + ((size_t)(i >> 1) * P + (i & 1) * S) * EW;
+            F3 dm = j0 ? f3_sub<E>(pg_load<E>(p1, j0 - 1), pg_load<E>(p0, j0 - 1)) : f3_zero();
+            for (u32 j = j0; j < j1; j++) {
+                F3 x0 = f3_zero(), dj = f3_zero();
+                if (j < wl) {
+                    x0 = pg_load<E>(p0, j);
+                    dj = f3_sub<E>(pg_load<E>(p1, j), x0);
+                }
+                pg_store<E>(o, j, pg_coef<E>(x0, dj, dm, ma, mb));
+                dm = dj;
+            }
         }
         __syncthreads();
     }
     const u64* res = (g & 1) ? B : A;
-    u64* dst = out + (size_t)blockIdx.x * S * EW;
-    for (u32 t = threadIdx.x; t < S * EW; t += PG_TPB) dst[t] = res[t];
+    u64* dst = out + (size_t)blockIdx.x * (w + g) * EW;
+    for (u32 t = threadIdx.x; t < (w + g) * EW; t += PG_TPB) dst[t] = res[t];
+}
+
+// Warp subtrees for the wide first passes: each warp folds gw levels of its
+// own R = 2^gw consecutive rows with no block barrier.  Rows are dense in
+// shared memory (row i of a level at i * width), and a level's outputs are
+// spread over the 32 lanes in order (output k = coefficient k mod wo of row
+// k / wo), so every lane has work until the last levels and neighbouring
+// lanes read neighbouring words.  Per warp: A holds the R input rows, B the
+// R/2 rows of level 1; the levels then alternate.
+template <bool E>
+__global__ void __launch_bounds__(PG_TPB) k_pg_warp(const u64* __restrict__ in, size_t trees, u32 w, u32 gw,
+                                                    const u64* __restrict__ pairs, u64* __restrict__ out) {
+    extern __shared__ u64 sm[];
+    constexpr u32 EW = E ? 3 : 1;
+    const u32 lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const size_t tree = (size_t)blockIdx.x * (PG_TPB / 32) + wid;
+    if (tree >= trees) return;
+    const u32 R = 1u << gw, a_words = R * w * EW, b_words = (R / 2) * (w + 1) * EW;
+    u64* A = sm + (size_t)wid * (a_words + b_words);
+    u64* B = A + a_words;
+    const u64* src = in + tree * a_words;
+    for (u32 t = lane; t < a_words; t += 32) pg_cp8(A + t, src + t);
+    asm volatile("cp.async.wait_all;" ::: "memory");
+    __syncwarp();
+    u32 wl = w;
+    for (u32 l = 0; l < gw; l++) {
+        const u64* s = (l & 1) ? B : A;
+        u64* d = (l & 1) ? A : B;
+        const u32 wo = wl + 1, total = (R >> (l + 1)) * wo, pair_words = 2 * wl * EW;
+        const Mul3 ma = pg_mul3<E>(pairs + 10 * l), mb = pg_mul3<E>(pairs + 10 * l + 5);
+        // lane -> (row pair, coefficient) and the step of 32 outputs, by
+        // subtraction (wo >= 2, so at most 16 rounds)
+        u32 q32 = 0, r32 = 32, i = 0, j = lane;
+        while (r32 >= wo) { r32 -= wo; q32++; }
+        while (j >= wo) { j -= wo; i++; }
+        u32 row = i * pair_words;                 // word offset of the pair's first row
+        const u32 row_step = q32 * pair_words;
+        for (u32 k = lane; k < total; k += 32) {
+            const u64* p0 = s + row;
+            const u64* p1 = p0 + wl * EW;
+            F3 x0 = f3_zero(), dj = f3_zero(), dm = f3_zero();
+            if (j < wl) {
+                x0 = pg_load<E>(p0, j);
+                dj = f3_sub<E>(pg_load<E>(p1, j), x0);
+            }
+            if (j) dm = f3_sub<E>(pg_load<E>(p1, j - 1), pg_load<E>(p0, j - 1));
+            pg_store<E>(d, k, pg_coef<E>(x0, dj, dm, ma, mb));
+            row += row_step;
+            j += r32;
+            if (j >= wo) { j -= wo; row += pair_words; }
+        }
+        __syncwarp();
+        wl = wo;
+    }
+    const u64* res = (gw & 1) ? B : A;
+    u64* dst = out + tree * (size_t)wl * EW;
+    for (u32 t = lane; t < wl * EW; t += 32) dst[t] = res[t];
 }
 
 // One level on global memory: cnt output rows of width w + 1 from 2 cnt
@@ -110,8 +209,7 @@ __global__ void __launch_bounds__(PG_TPB) k_pg_group(const u64* __restrict__ in,
 template <bool E>
 __global__ void __launch_bounds__(PG_TPB) k_pg_level(const u64* __restrict__ in, size_t cnt, u32 w,
                                                      const u64* __restrict__ pair, u64* __restrict__ out) {
-    const Mul3 ma = mul3_prepare<E>(f3_make(pair[0], pair[1], pair[2]));
-    const Mul3 mb = mul3_prepare<E>(f3_make(pair[3], pair[4], pair[5]));
+    const Mul3 ma = pg_mul3<E>(pair), mb = pg_mul3<E>(pair + 5);
     const u32 wo = w + 1;
     for (size_t idx = (size_t)blockIdx.x * PG_TPB + threadIdx.x; idx < cnt * wo; idx += (size_t)gridDim.x * PG_TPB) {
         const size_t i = idx / wo;
@@ -126,12 +224,36 @@ __global__ void __launch_bounds__(PG_TPB) k_pg_level(const u64* __restrict__ in,
     }
 }
 
-size_t pg_group_smem(u32 w, u32 g, u32 ew) { return (size_t)3 * (1u << (g - 1)) * (w + g) * ew * 8; }
+constexpr u64 PG_P = 0xFFFFFFFF00000001ULL;
+inline u64 pg_hmul(u64 a, u64 b) { return (u64)(((unsigned __int128)a * b) % PG_P); }
 
-// Levels one shared-memory pass folds for `count` rows of width w (0: none fit).
-u32 pg_plan_levels(size_t count, u32 w, u32 ew) {
+size_t pg_warp_smem(u32 w, u32 gw, u32 ew) {
+    const size_t R = (size_t)1 << gw;
+    return (R * w + (R / 2) * (w + 1)) * ew * 8;
+}
+constexpr size_t PG_WARP_SMEM = 12 * 1024;   // per warp
+constexpr u32 PG_WARP_MAX_G = 6;
+// Levels a warp-subtree pass folds: at least 3 (or all that are left),
+// else 0 and the block kernel takes the pass.
+u32 pg_plan_warp(size_t count, u32 w, u32 ew) {
     u32 g = 0;
-    while (g < PG_MAX_G && ((size_t)2 << g) <= count && pg_group_smem(w, g + 1, ew) <= PG_SMEM) g++;
+    while (g < PG_WARP_MAX_G && ((size_t)2 << g) <= count && pg_warp_smem(w, g + 1, ew) <= PG_WARP_SMEM) g++;
+    return (g >= 3 || (g && (count >> g) == 1)) ? g : 0;
+}
+
+// Row width bound of a group (odd, so that the pair stride 2 S + 1 is odd
+// as well as the row offset S within a pair).
+u32 pg_stride(u32 w, u32 g) { return (w + g) | 1u; }
+size_t pg_group_smem(u32 w, u32 g, u32 ew) {
+    const size_t R = (size_t)1 << g, pairs_a = R / 2, pairs_b = R >= 4 ? R / 4 : 1;
+    return (pairs_a + pairs_b) * (2 * pg_stride(w, g) + 1) * ew * 8;
+}
+
+// Levels one shared-memory pass folds for `count` rows of width w (0: none
+// fit in `budget` bytes).
+u32 pg_plan_levels(size_t count, u32 w, u32 ew, size_t budget) {
+    u32 g = 0;
+    while (g < PG_MAX_G && ((size_t)2 << g) <= count && pg_group_smem(w, g + 1, ew) <= budget) g++;
     return g;
 }
 
@@ -164,16 +286,24 @@ extern "C" int effsc_protogalaxy_fold(effsc_ctx* ctx, int field, const uint64_t*
         while (K < n_levels && ((size_t)2 << K) <= n_polys) K++;
     const size_t count0 = (size_t)1 << K;
     const size_t final_w = width + K;
-    std::vector<u64> res(std::max<size_t>(final_w, 1) * ew, 0), pr(std::max<size_t>(K, 1) * 6, 0);
+    // (a, b) per level as prepared multipliers (m0, m1, m2, W m1, W m2)
+    std::vector<u64> res(std::max<size_t>(final_w, 1) * ew, 0), pr(std::max<size_t>(K, 1) * 10, 0);
     for (u32 k = 0; k < K; k++)
-        for (int h = 0; h < 2; h++)
-            for (u32 c = 0; c < ew; c++) pr[6 * k + 3 * h + c] = pairs[(2 * k + h) * ew + c] % 0xFFFFFFFF00000001ULL;
+        for (int h = 0; h < 2; h++) {
+            u64* q = &pr[10 * k + 5 * h];
+            for (u32 c = 0; c < ew; c++) q[c] = pairs[(2 * k + h) * ew + c] % PG_P;
+            q[3] = pg_hmul(GL_W, q[1]);
+            q[4] = pg_hmul(GL_W, q[2]);
+        }
     int rc = EFFSC_OK;
     u64 *d_pairs = nullptr, *d_in = nullptr, *bufs[2] = {nullptr, nullptr};
     const u64* cur = nullptr;
     if (width) {
+        // device memory is read in place; host memory (pinned or pageable)
+        // is copied first, so the passes only ever read device memory
         bool is_host = false;
         cur = effsc_internal_device_view(dev, polys, &is_host);
+        if (is_host) cur = nullptr;
         if (!cur) {
             const size_t bytes = count0 * width * ew * 8;
             PCK(cudaMallocAsync((void**)&d_in, bytes, s));
@@ -188,8 +318,40 @@ extern "C" int effsc_protogalaxy_fold(effsc_ctx* ctx, int field, const uint64_t*
         u32 w = (u32)width, lvl = 0;
         int which = 0;
         size_t cap[2] = {0, 0};
+        static bool attr_set = false;
+        if (!attr_set) {
+            PCK(cudaFuncSetAttribute(k_pg_group<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)PG_SMEM_BIG));
+            PCK(cudaFuncSetAttribute(k_pg_group<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)PG_SMEM_BIG));
+            PCK(cudaFuncSetAttribute(k_pg_warp<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(8 * PG_WARP_SMEM)));
+            PCK(cudaFuncSetAttribute(k_pg_warp<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(8 * PG_WARP_SMEM)));
+            attr_set = true;
+        }
         while (count > 1) {
-            u32 g = pg_plan_levels(count, w, ew);
+            const u32 gw = pg_plan_warp(count, w, ew);
+            if (gw) {
+                const size_t trees = count >> gw, need = trees * (w + gw) * ew * 8;
+                if (need > cap[which]) {
+                    if (bufs[which]) cudaFreeAsync(bufs[which], s);
+                    bufs[which] = nullptr;
+                    cap[which] = 0;
+                    PCK(cudaMallocAsync((void**)&bufs[which], need, s));
+                    cap[which] = need;
+                }
+                const size_t smem = (PG_TPB / 32) * pg_warp_smem(w, gw, ew);
+                const unsigned grid = (unsigned)((trees + PG_TPB / 32 - 1) / (PG_TPB / 32));
+                if (ew == 3) k_pg_warp<true><<<grid, PG_TPB, smem, s>>>(cur, trees, w, gw, d_pairs + 10 * lvl, bufs[which]);
+                else k_pg_warp<false><<<grid, PG_TPB, smem, s>>>(cur, trees, w, gw, d_pairs + 10 * lvl, bufs[which]);
+                effsc_internal_add_launches(1);
+                PCK(cudaGetLastError());
+                cur = bufs[which];
+                which ^= 1;
+                count = trees;
+                w += gw;
+                lvl += gw;
+                continue;
+            }
+            u32 g = pg_plan_levels(count, w, ew, PG_SMEM);
+            if (!g || (count >> g) < 4 * 152) g = std::max(g, pg_plan_levels(count, w, ew, PG_SMEM_BIG));
             const size_t out_rows = g ? count >> g : count >> 1;
             const u32 out_w = w + (g ? g : 1);
             const size_t need = out_rows * out_w * ew * 8;
@@ -202,14 +364,15 @@ extern "C" int effsc_protogalaxy_fold(effsc_ctx* ctx, int field, const uint64_t*
             }
             if (g) {
                 const size_t smem = pg_group_smem(w, g, ew);
-                if (ew == 3) k_pg_group<true><<<(unsigned)out_rows, PG_TPB, smem, s>>>(cur, w, g, d_pairs + 6 * lvl, bufs[which]);
-                else k_pg_group<false><<<(unsigned)out_rows, PG_TPB, smem, s>>>(cur, w, g, d_pairs + 6 * lvl, bufs[which]);
+                const u32 S = pg_stride(w, g);
+                if (ew == 3) k_pg_group<true><<<(unsigned)out_rows, PG_TPB, smem, s>>>(cur, w, g, S, d_pairs + 10 * lvl, bufs[which]);
+                else k_pg_group<false><<<(unsigned)out_rows, PG_TPB, smem, s>>>(cur, w, g, S, d_pairs + 10 * lvl, bufs[which]);
                 lvl += g;
             } else {
                 const size_t items = out_rows * (w + 1);
                 const unsigned grid = (unsigned)std::min<size_t>((items + PG_TPB - 1) / PG_TPB, 152 * 16);
-                if (ew == 3) k_pg_level<true><<<grid, PG_TPB, 0, s>>>(cur, out_rows, w, d_pairs + 6 * lvl, bufs[which]);
-                else k_pg_level<false><<<grid, PG_TPB, 0, s>>>(cur, out_rows, w, d_pairs + 6 * lvl, bufs[which]);
+                if (ew == 3) k_pg_level<true><<<grid, PG_TPB, 0, s>>>(cur, out_rows, w, d_pairs + 10 * lvl, bufs[which]);
+                else k_pg_level<false><<<grid, PG_TPB, 0, s>>>(cur, out_rows, w, d_pairs + 10 * lvl, bufs[which]);
                 lvl += 1;
             }
             effsc_internal_add_launches(1);

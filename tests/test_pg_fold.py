@@ -2,7 +2,8 @@
 (effsc_protogalaxy_fold) against the oracle: the reference's own cases
 (two polynomials, four constants, random against the naive fold), both
 fields, sizes that take one, two and three shared-memory passes, polynomials
-too wide for a shared-memory group (per-level kernel), ragged counts and
+too wide for a shared-memory group (per-level kernel), sizes wide enough for
+the warp-subtree first pass, ragged counts and
 level counts, trailing zeros, and inputs in device and pinned memory."""
 import random
 
@@ -69,7 +70,8 @@ def R_pad(c):
 
 @pytest.mark.parametrize("field", [1, 3])
 @pytest.mark.parametrize("n,width", [(2, 1), (4, 8), (64, 8), (1024, 8), (1 << 14, 4), (1 << 12, 30),
-                                     (1 << 11, 100), (16, 700), (8, 2100), (1 << 16, 1)])
+                                     (1 << 11, 100), (16, 700), (8, 2100), (4, 7000), (1 << 16, 1),
+                                     (1 << 18, 2), (1 << 18, 8)])
 def test_sizes_match_oracle(E, field, n, width):
     rng = random.Random(n * 7 + width + field)
     levels = n.bit_length() - 1
