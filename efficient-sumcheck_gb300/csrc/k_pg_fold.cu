@@ -19,6 +19,7 @@
 #include "round_common.cuh"
 
 #include <algorithm>
+#include <atomic>
 #include <vector>
 
 using namespace effsc;
@@ -27,6 +28,8 @@ int effsc_internal_ctx_device(const effsc_ctx* c);
 cudaStream_t effsc_internal_ctx_stream(const effsc_ctx* c);
 uint64_t effsc_internal_add_launches(uint64_t k);
 const u64* effsc_internal_device_view(int device, const uint64_t* ptr, bool* is_host);
+void* effsc_internal_pinned_get(effsc_ctx* c, size_t bytes);
+void effsc_internal_pinned_put(effsc_ctx* c, void* p, size_t bytes);
 
 namespace effsc {
 
@@ -34,6 +37,12 @@ constexpr int PG_TPB = 256;
 constexpr size_t PG_SMEM = 48 * 1024;        // wide grids: four blocks per SM
 constexpr size_t PG_SMEM_BIG = 200 * 1024;   // narrow grids: fewer passes
 constexpr u32 PG_MAX_G = 10;
+
+// The (a, b) multipliers of the levels one pass folds, prepared on the host
+// as (m0, m1, m2, W m1, W m2) each and passed by value (no upload).
+struct PgMul {
+    u64 q[PG_MAX_G * 10];
+};
 
 template <bool E>
 __device__ __forceinline__ F3 pg_load(const u64* p, size_t e) {
@@ -94,9 +103,10 @@ __device__ __forceinline__ void pg_cp8(u64* dst, const u64* src) {
 
 template <bool E>
 __global__ void __launch_bounds__(PG_TPB) k_pg_group(const u64* __restrict__ in, u32 w, u32 g, u32 S,
-                                                     const u64* __restrict__ pairs, u64* __restrict__ out) {
+                                                     const PgMul mul, u64* __restrict__ out) {
     extern __shared__ u64 sm[];
     constexpr u32 EW = E ? 3 : 1;
+    const u64* pairs = mul.q;
     const u32 R = 1u << g, P = 2 * S + 1;
     u64* A = sm;
     u64* B = sm + (size_t)(R / 2) * P * EW;
@@ -156,9 +166,10 @@ __global__ void __launch_bounds__(PG_TPB) k_pg_group(const u64* __restrict__ in,
 // R/2 rows of level 1; the levels then alternate.
 template <bool E>
 __global__ void __launch_bounds__(PG_TPB) k_pg_warp(const u64* __restrict__ in, size_t trees, u32 w, u32 gw,
-                                                    const u64* __restrict__ pairs, u64* __restrict__ out) {
+                                                    const PgMul mul, u64* __restrict__ out) {
     extern __shared__ u64 sm[];
     constexpr u32 EW = E ? 3 : 1;
+    const u64* pairs = mul.q;
     const u32 lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const size_t tree = (size_t)blockIdx.x * (PG_TPB / 32) + wid;
     if (tree >= trees) return;
@@ -208,7 +219,8 @@ __global__ void __launch_bounds__(PG_TPB) k_pg_warp(const u64* __restrict__ in, 
 // input rows of width w.
 template <bool E>
 __global__ void __launch_bounds__(PG_TPB) k_pg_level(const u64* __restrict__ in, size_t cnt, u32 w,
-                                                     const u64* __restrict__ pair, u64* __restrict__ out) {
+                                                     const PgMul mul, u64* __restrict__ out) {
+    const u64* pair = mul.q;
     const Mul3 ma = pg_mul3<E>(pair), mb = pg_mul3<E>(pair + 5);
     const u32 wo = w + 1;
     for (size_t idx = (size_t)blockIdx.x * PG_TPB + threadIdx.x; idx < cnt * wo; idx += (size_t)gridDim.x * PG_TPB) {
@@ -287,7 +299,7 @@ extern "C" int effsc_protogalaxy_fold(effsc_ctx* ctx, int field, const uint64_t*
     const size_t count0 = (size_t)1 << K;
     const size_t final_w = width + K;
     // (a, b) per level as prepared multipliers (m0, m1, m2, W m1, W m2)
-    std::vector<u64> res(std::max<size_t>(final_w, 1) * ew, 0), pr(std::max<size_t>(K, 1) * 10, 0);
+    std::vector<u64> pr(std::max<size_t>(K, 1) * 10, 0);
     for (u32 k = 0; k < K; k++)
         for (int h = 0; h < 2; h++) {
             u64* q = &pr[10 * k + 5 * h];
@@ -295,8 +307,22 @@ extern "C" int effsc_protogalaxy_fold(effsc_ctx* ctx, int field, const uint64_t*
             q[3] = pg_hmul(GL_W, q[1]);
             q[4] = pg_hmul(GL_W, q[2]);
         }
+    auto muls = [&](u32 lvl, u32 g) {
+        PgMul m;
+        for (u32 t = 0; t < PG_MAX_G * 10; t++) m.q[t] = t < g * 10 ? pr[10 * lvl + t] : 0;
+        return m;
+    };
+    // the result comes back through a pinned block of the context's pool
+    size_t res_bytes = 4096;
+    while (res_bytes < std::max<size_t>(final_w, 1) * ew * 8) res_bytes <<= 1;
+    u64* res = (u64*)effsc_internal_pinned_get(ctx, res_bytes);
+    std::vector<u64> res_fallback;
+    if (!res) {
+        res_fallback.assign(res_bytes / 8, 0);
+        res = res_fallback.data();
+    }
     int rc = EFFSC_OK;
-    u64 *d_pairs = nullptr, *d_in = nullptr, *bufs[2] = {nullptr, nullptr};
+    u64 *d_in = nullptr, *bufs[2] = {nullptr, nullptr};
     const u64* cur = nullptr;
     if (width) {
         // device memory is read in place; host memory (pinned or pageable)
@@ -312,19 +338,18 @@ extern "C" int effsc_protogalaxy_fold(effsc_ctx* ctx, int field, const uint64_t*
         }
     }
     if (K && width) {
-        PCK(cudaMallocAsync((void**)&d_pairs, pr.size() * 8, s));
-        PCK(cudaMemcpyAsync(d_pairs, pr.data(), pr.size() * 8, cudaMemcpyHostToDevice, s));
         size_t count = count0;
         u32 w = (u32)width, lvl = 0;
         int which = 0;
         size_t cap[2] = {0, 0};
-        static bool attr_set = false;
-        if (!attr_set) {
+        static std::atomic<uint64_t> attr_done{0};    // one bit per device
+        const uint64_t bit = 1ull << (dev & 63);
+        if (!(attr_done.load() & bit)) {
             PCK(cudaFuncSetAttribute(k_pg_group<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)PG_SMEM_BIG));
             PCK(cudaFuncSetAttribute(k_pg_group<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)PG_SMEM_BIG));
             PCK(cudaFuncSetAttribute(k_pg_warp<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(8 * PG_WARP_SMEM)));
             PCK(cudaFuncSetAttribute(k_pg_warp<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(8 * PG_WARP_SMEM)));
-            attr_set = true;
+            attr_done.fetch_or(bit);
         }
         while (count > 1) {
             const u32 gw = pg_plan_warp(count, w, ew);
@@ -339,8 +364,8 @@ extern "C" int effsc_protogalaxy_fold(effsc_ctx* ctx, int field, const uint64_t*
                 }
                 const size_t smem = (PG_TPB / 32) * pg_warp_smem(w, gw, ew);
                 const unsigned grid = (unsigned)((trees + PG_TPB / 32 - 1) / (PG_TPB / 32));
-                if (ew == 3) k_pg_warp<true><<<grid, PG_TPB, smem, s>>>(cur, trees, w, gw, d_pairs + 10 * lvl, bufs[which]);
-                else k_pg_warp<false><<<grid, PG_TPB, smem, s>>>(cur, trees, w, gw, d_pairs + 10 * lvl, bufs[which]);
+                if (ew == 3) k_pg_warp<true><<<grid, PG_TPB, smem, s>>>(cur, trees, w, gw, muls(lvl, gw), bufs[which]);
+                else k_pg_warp<false><<<grid, PG_TPB, smem, s>>>(cur, trees, w, gw, muls(lvl, gw), bufs[which]);
                 effsc_internal_add_launches(1);
                 PCK(cudaGetLastError());
                 cur = bufs[which];
@@ -365,14 +390,14 @@ extern "C" int effsc_protogalaxy_fold(effsc_ctx* ctx, int field, const uint64_t*
             if (g) {
                 const size_t smem = pg_group_smem(w, g, ew);
                 const u32 S = pg_stride(w, g);
-                if (ew == 3) k_pg_group<true><<<(unsigned)out_rows, PG_TPB, smem, s>>>(cur, w, g, S, d_pairs + 10 * lvl, bufs[which]);
-                else k_pg_group<false><<<(unsigned)out_rows, PG_TPB, smem, s>>>(cur, w, g, S, d_pairs + 10 * lvl, bufs[which]);
+                if (ew == 3) k_pg_group<true><<<(unsigned)out_rows, PG_TPB, smem, s>>>(cur, w, g, S, muls(lvl, g), bufs[which]);
+                else k_pg_group<false><<<(unsigned)out_rows, PG_TPB, smem, s>>>(cur, w, g, S, muls(lvl, g), bufs[which]);
                 lvl += g;
             } else {
                 const size_t items = out_rows * (w + 1);
                 const unsigned grid = (unsigned)std::min<size_t>((items + PG_TPB - 1) / PG_TPB, 152 * 16);
-                if (ew == 3) k_pg_level<true><<<grid, PG_TPB, 0, s>>>(cur, out_rows, w, d_pairs + 10 * lvl, bufs[which]);
-                else k_pg_level<false><<<grid, PG_TPB, 0, s>>>(cur, out_rows, w, d_pairs + 10 * lvl, bufs[which]);
+                if (ew == 3) k_pg_level<true><<<grid, PG_TPB, 0, s>>>(cur, out_rows, w, muls(lvl, 1), bufs[which]);
+                else k_pg_level<false><<<grid, PG_TPB, 0, s>>>(cur, out_rows, w, muls(lvl, 1), bufs[which]);
                 lvl += 1;
             }
             effsc_internal_add_launches(1);
@@ -383,10 +408,10 @@ extern "C" int effsc_protogalaxy_fold(effsc_ctx* ctx, int field, const uint64_t*
             w = out_w;
         }
     }
-    if (final_w && width) PCK(cudaMemcpyAsync(res.data(), cur, final_w * ew * 8, cudaMemcpyDefault, s));
+    if (final_w && width) PCK(cudaMemcpyAsync(res, cur, final_w * ew * 8, cudaMemcpyDefault, s));
     PCK(cudaStreamSynchronize(s));
     {
-        size_t len = final_w;
+        size_t len = width ? final_w : 0;
         auto zero = [&](size_t e) {
             for (u32 c = 0; c < ew; c++)
                 if (res[e * ew + c]) return false;
@@ -396,11 +421,12 @@ extern "C" int effsc_protogalaxy_fold(effsc_ctx* ctx, int field, const uint64_t*
         while (len > keep && zero(len - 1)) len--;
         if (n_polys >= 2 && len == 0) len = 1;       // width 0: the zero polynomial as one term
         for (size_t e = 0; e < len; e++)
-            for (u32 c = 0; c < ew; c++) out[e * ew + c] = e < final_w ? res[e * ew + c] : 0;
+            for (u32 c = 0; c < ew; c++) out[e * ew + c] = (width && e < final_w) ? res[e * ew + c] : 0;
         *out_len = len;
     }
 done:
-    for (void* p : {(void*)d_pairs, (void*)d_in, (void*)bufs[0], (void*)bufs[1]})
+    for (void* p : {(void*)d_in, (void*)bufs[0], (void*)bufs[1]})
         if (p) cudaFreeAsync(p, s);
+    if (res_fallback.empty()) effsc_internal_pinned_put(ctx, res, res_bytes);
     return rc;
 }

@@ -1150,6 +1150,8 @@ const u64* effsc_internal_device_view(int device, const uint64_t* ptr, bool* is_
     cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, device);
     return pageable ? (const u64*)ptr : nullptr;
 }
+void* effsc_internal_pinned_get(effsc_ctx* c, size_t bytes) { return pinned_get(c, bytes); }
+void effsc_internal_pinned_put(effsc_ctx* c, void* p, size_t bytes) { pinned_put(c, p, bytes); }
 int effsc_internal_ctx_device(const effsc_ctx* c) { return c->device; }
 cudaStream_t effsc_internal_ctx_stream(const effsc_ctx* c) { return c->stream; }
 uint64_t effsc_internal_add_launches(uint64_t k) { g_launches += k; return g_launches; }
