@@ -48,23 +48,33 @@ __device__ __forceinline__ u64 rotl64d(u64 x, int r) {
 }
 
 // One Keccak-f[1600] permutation; lane i (< 25) holds lane A[i], i = x + 5y.
+// The round is bound by shuffle latency and count (one warp, nothing to
+// overlap with), so each step uses as few as it can: theta's column parities
+// by a tree over the rows (y, y+1; then +2 rows; then row 4: three 64-bit
+// shuffles, the parity of column x lands in lane x), then C[x-1] and C[x+1];
+// pi and chi take B[x, y], B[x+1, y] and B[x+2, y] straight from the lanes
+// that rho-rotate into them.  Eight 64-bit shuffles per round.
 static __device__ __noinline__ void keccak_f_warp(u64& a, int lane) {
     const int i = lane < 25 ? lane : 0;
     const int x = i % 5, y = i / 5;
     const int my_rot = c_keccak_rot[i];
-    // pi: B[X, Y] = rho(A[x, y]) with X = y, Y = 2x + 3y;  source of lane (X,Y)
-    // is x = (X + 3Y) mod 5, y = X.
-    const int pi_src = ((x + 3 * y) % 5) + 5 * x;
-    const int chi1 = (x + 1) % 5 + 5 * y, chi2 = (x + 2) % 5 + 5 * y;
-    const int xm1 = (x + 4) % 5, xp1 = (x + 1) % 5;
+    // pi: B[X, Y] = rho(A[x, y]) with X = y, Y = 2x + 3y; the source of lane
+    // (X, Y) is x = (X + 3Y) mod 5, y = X.
+    const int xp1 = (x + 1) % 5, xp2 = (x + 2) % 5, xm1 = (x + 4) % 5;
+    const int src0 = ((x + 3 * y) % 5) + 5 * x;
+    const int src1 = ((xp1 + 3 * y) % 5) + 5 * xp1;
+    const int src2 = ((xp2 + 3 * y) % 5) + 5 * xp2;
+    const int l5 = min(i + 5, 31), l10 = min(i + 10, 31), l20 = min(i + 20, 31);
 #pragma unroll 1
     for (int round = 0; round < 24; round++) {
-        u64 c = shfl64(a, x) ^ shfl64(a, x + 5) ^ shfl64(a, x + 10) ^ shfl64(a, x + 15) ^ shfl64(a, x + 20);
-        u64 cm = shfl64(c, xm1), cp = shfl64(c, xp1);
+        u64 v = a ^ shfl64(a, l5);           // rows y, y+1
+        const u64 a20 = shfl64(a, l20);      // row y+4 (used by lanes 0..4)
+        v ^= shfl64(v, l10);                 // rows y..y+3
+        v ^= a20;                            // lanes 0..4: C[x]
+        const u64 cm = shfl64(v, xm1), cp = shfl64(v, xp1);
         a ^= cm ^ rotl64d(cp, 1);
-        u64 r = rotl64d(a, my_rot);
-        u64 b = shfl64(r, pi_src);
-        u64 b1 = shfl64(b, chi1), b2 = shfl64(b, chi2);
+        const u64 r = rotl64d(a, my_rot);
+        const u64 b = shfl64(r, src0), b1 = shfl64(r, src1), b2 = shfl64(r, src2);
         a = b ^ (~b1 & b2);
         if (lane == 0) a ^= c_keccak_rc[round];
     }

@@ -164,6 +164,7 @@ bool diag_mulmod_rate(cudaStream_t s, double* mulmod_per_s, double* fp3_mul_per_
 // One thread waits on an mbarrier with the round kernels' bounded wait;
 // `arrive`: complete the phase first.  *status = 0 or EFFSC_STATUS_TIMEOUT.
 void launch_diag_bounded_wait(u64 limit_ns, int arrive, u32* status, cudaStream_t s);
+void launch_diag_transcript(u32 iters, u64* out, cudaStream_t s);
 int max_grid(void);
 void kernels_init(int device);
 

@@ -1213,6 +1213,24 @@ int effsc_diag_mulmod_rate(effsc_ctx* ctx, double* mulmod_per_s, double* fp3_mul
     return EFFSC_OK;
 }
 
+int effsc_diag_transcript_latency(effsc_ctx* ctx, double* ns_per_permutation, double* ns_per_round_step) {
+    if (!ctx) return fail(EFFSC_INVALID_ARG, "ctx is NULL");
+    CK(cudaSetDevice(ctx->device));
+    u64* d = nullptr;
+    u64 h[3] = {0, 0, 0};
+    CK(cudaMallocAsync((void**)&d, sizeof h, ctx->stream));
+    launch_diag_transcript(2, d, ctx->stream);        // warm-up
+    launch_diag_transcript(1000, d, ctx->stream);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpyAsync(h, d, sizeof h, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    cudaFreeAsync(d, ctx->stream);
+    if (e != cudaSuccess) return fail(EFFSC_CUDA_ERROR, "transcript probe: %s", cudaGetErrorString(e));
+    if (ns_per_permutation) *ns_per_permutation = (double)h[0];
+    if (ns_per_round_step) *ns_per_round_step = (double)h[1];
+    return EFFSC_OK;
+}
+
 int effsc_ctx_create(int device, effsc_ctx** out) {
     if (!out) return fail(EFFSC_INVALID_ARG, "out is NULL");
     int n = 0;

@@ -63,6 +63,7 @@ SIGNATURES = {
     "effsc_reorder_msb": (ci, [vp, u64p, sz, ci, u64p]),
     "effsc_stream_claim": (ci, [vp, ci, ci, ctypes.POINTER(u64p), sz, ci, u64p]),
     "effsc_protogalaxy_fold": (ci, [vp, ci, u64p, sz, u64p, sz, sz, u64p, ctypes.POINTER(sz)]),
+    "effsc_diag_transcript_latency": (ci, [vp, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]),
     "effsc_verify_batch": (ci, [vp, ci, sz, u64p, ci, ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(vp), u8p, sz,
                                 u64p, u64p, u64p]),
     "effsc_gkr_create": (ci, [vp, ci, ci, u64p, u64p, u64p, sz, ci, ctypes.POINTER(vp)]),

@@ -255,6 +255,12 @@ uint64_t effsc_table_seed(uint64_t seed, uint64_t table);
  * thread of a full grid; the denominator of the integer-multiply roofline. */
 int effsc_diag_mulmod_rate(effsc_ctx* ctx, double* mulmod_per_s, double* fp3_mul_per_s);
 
+/* Transcript latency probe (no reference counterpart): one warp runs 1000
+ * Keccak-f[1600] permutations, then 1000 round steps (send one Fp3 element,
+ * squeeze one challenge); ns per permutation and per step, from the device's
+ * global timer.  The per-round floor of every round of a proof. */
+int effsc_diag_transcript_latency(effsc_ctx* ctx, double* ns_per_permutation, double* ns_per_round_step);
+
 /* Self-test of the bounded wait that the TMA-staged round kernel uses on its
  * own mbarriers (no reference counterpart): one thread waits on a barrier
  * that nothing completes (arrive = 0) or that it completed itself (arrive =

@@ -261,3 +261,12 @@ def test_kernels_launch(E):
     p.set_tail(None)     # all 12 rounds in the one-block tail kernel, the final folds, the read-back gather
     p.prove(12, E.Transcript.keccak(3, b"k"), use_graph=False)
     assert 1 <= E.launch_count() <= 4
+
+
+def test_transcript_latency_probe(E):
+    """effsc_diag_transcript_latency: a round step (send + challenge) costs
+    at least one permutation and stays within a few microseconds."""
+    import ctypes
+    perm, step = ctypes.c_double(), ctypes.c_double()
+    assert E.load().effsc_diag_transcript_latency(E.Context.default().h, ctypes.byref(perm), ctypes.byref(step)) == 0
+    assert 0 < perm.value <= step.value < 50_000
