@@ -2,6 +2,8 @@
 // provers (template instantiations and their launch dispatch).
 #include "round_common.cuh"
 
+#include <atomic>
+
 namespace effsc {
 
 #define EVAL(POL, SEM, M) \
@@ -37,11 +39,16 @@ template <int POL, u32 M, bool ECH>
 static bool launch_tma_inst(const RoundArgs& a, u32 ntiles, int grid, cudaStream_t s) {
     constexpr int NT = Policy<POL, 0>::NT;
     constexpr int SM_BYTES = TmaLayout<M, NT>::smem_bytes();
-    static bool configured = false;
-    if (!configured) {
+    // the shared-memory limit is a per-device function attribute: set once
+    // per device (one bit each), safe when threads race to set it
+    static std::atomic<uint64_t> configured{0};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return false;
+    const uint64_t bit = 1ull << (dev & 63);
+    if (!(configured.load() & bit)) {
         if (cudaFuncSetAttribute(k_fused_tma<POL, M, ECH>, cudaFuncAttributeMaxDynamicSharedMemorySize, SM_BYTES) != cudaSuccess)
             return false;
-        configured = true;
+        configured.fetch_or(bit);
     }
     k_fused_tma<POL, M, ECH><<<grid, TPB, SM_BYTES, s>>>(a, ntiles);
     return true;
