@@ -35,7 +35,7 @@ bool launch_fused_mlip(int pol, int sem, u32 mask, bool ech, const RoundArgs& a,
     }
 }
 
-template <int POL, u32 M, bool ECH>
+template <int POL, int SEM, u32 M, bool ECH>
 static bool launch_tma_inst(const RoundArgs& a, u32 ntiles, int grid, cudaStream_t s) {
     constexpr int NT = Policy<POL, 0>::NT;
     constexpr int SM_BYTES = TmaLayout<M, NT>::smem_bytes();
@@ -46,20 +46,23 @@ static bool launch_tma_inst(const RoundArgs& a, u32 ntiles, int grid, cudaStream
     if (cudaGetDevice(&dev) != cudaSuccess) return false;
     const uint64_t bit = 1ull << (dev & 63);
     if (!(configured.load() & bit)) {
-        if (cudaFuncSetAttribute(k_fused_tma<POL, M, ECH>, cudaFuncAttributeMaxDynamicSharedMemorySize, SM_BYTES) != cudaSuccess)
+        if (cudaFuncSetAttribute(k_fused_tma<POL, SEM, M, ECH>, cudaFuncAttributeMaxDynamicSharedMemorySize, SM_BYTES) != cudaSuccess)
             return false;
         configured.fetch_or(bit);
     }
-    k_fused_tma<POL, M, ECH><<<grid, TPB, SM_BYTES, s>>>(a, ntiles);
+    k_fused_tma<POL, SEM, M, ECH><<<grid, TPB, SM_BYTES, s>>>(a, ntiles);
     return true;
 }
 
-bool launch_fused_tma(int pol, u32 mask, bool ech, const RoundArgs& a, u32 ntiles, int grid, cudaStream_t s) {
-    int key = pol * 64 + (int)mask * 2 + (ech ? 1 : 0);
+bool launch_fused_tma(int pol, int sem, u32 mask, bool ech, const RoundArgs& a, u32 ntiles, int grid, cudaStream_t s) {
+    int key = pol * 64 + (sem == SEM_LSB ? 32 : 0) + (int)mask * 2 + (ech ? 1 : 0);
     switch (key) {
-        case POL_IP * 64 + 0 * 2 + 0: return launch_tma_inst<POL_IP, 0, false>(a, ntiles, grid, s);
-        case POL_IP * 64 + 0 * 2 + 1: return launch_tma_inst<POL_IP, 0, true>(a, ntiles, grid, s);
-        case POL_IP * 64 + 3 * 2 + 1: return launch_tma_inst<POL_IP, 3, true>(a, ntiles, grid, s);
+        case POL_IP * 64 + 0 * 2 + 0: return launch_tma_inst<POL_IP, SEM_MSB_PAD, 0, false>(a, ntiles, grid, s);
+        case POL_IP * 64 + 0 * 2 + 1: return launch_tma_inst<POL_IP, SEM_MSB_PAD, 0, true>(a, ntiles, grid, s);
+        case POL_IP * 64 + 3 * 2 + 1: return launch_tma_inst<POL_IP, SEM_MSB_PAD, 3, true>(a, ntiles, grid, s);
+        case POL_IP * 64 + 32 + 0 * 2 + 0: return launch_tma_inst<POL_IP, SEM_LSB, 0, false>(a, ntiles, grid, s);
+        case POL_IP * 64 + 32 + 0 * 2 + 1: return launch_tma_inst<POL_IP, SEM_LSB, 0, true>(a, ntiles, grid, s);
+        case POL_IP * 64 + 32 + 3 * 2 + 1: return launch_tma_inst<POL_IP, SEM_LSB, 3, true>(a, ntiles, grid, s);
         default: return false;
     }
 }

@@ -133,7 +133,7 @@ bool launch_fused(int pol, int sem, u32 mask, bool ech, const RoundArgs& a, int 
 bool launch_eqf_left(bool fused, u32 mask, bool ech, const RoundArgs& a, int grid, cudaStream_t s);
 // TMA-staged fused MSB round: tiles of KERNEL_TPB quadruples; returns false
 // if no kernel is instantiated for the combination.
-bool launch_fused_tma(int pol, u32 mask, bool ech, const RoundArgs& a, u32 ntiles, int grid, cudaStream_t s);
+bool launch_fused_tma(int pol, int sem, u32 mask, bool ech, const RoundArgs& a, u32 ntiles, int grid, cudaStream_t s);
 int fused_tma_blocks_per_sm(void);
 // GkrProver round: t[0] = add, t[1] = mult (both Fp3 when ea), t[2] = W_b,
 // t[3] = W_c (Fp3 when ew; the compact witness tables of 2^(k - bound b

@@ -545,9 +545,10 @@ __global__ void __launch_bounds__(TPB, 1) k_fused_wide(RoundArgs a) {
 }
 
 // ---------------------------------------------------------------------------
-// TMA-staged fused round (MSB, L a power of two, Q = L/4 a multiple of TQ).
-// Each block owns tiles tile = blockIdx.x + i * gridDim.x of TQ quadruples.
-// Thread 0 streams a tile's 4 quarters x components x tables into one shared
+// TMA-staged fused round (MSB or LSB, L a power of two, Q = L/4 a multiple
+// of TQ).  Each block owns tiles tile = blockIdx.x + i * gridDim.x of TQ
+// quadruples.  Thread 0 streams a tile's 4 quarters (MSB) or its 4 TQ
+// consecutive entries (LSB) x components x tables into one shared
 // memory stage with cp.async.bulk (one bulk copy per contiguous chunk), the
 // stage's mbarrier counting the bytes; TMA_S stages are kept in flight while
 // every thread folds and evaluates the quadruple it owns from shared memory
@@ -597,6 +598,12 @@ struct TmaLayout {
         for (int u = 0; u < t; u++) o += 4 * nc(u);
         return (o + q * nc(t) + c) * TQ;
     }
+    // LSB: the tile's 4 TQ consecutive entries of (table t, component c)
+    __host__ __device__ static constexpr int offl(int t, int c) {
+        int o = 0;
+        for (int u = 0; u < t; u++) o += 4 * nc(u);
+        return (o + 4 * c) * TQ;
+    }
     __host__ __device__ static constexpr int words() {
         int o = 0;
         for (int u = 0; u < NT; u++) o += 4 * nc(u);
@@ -606,7 +613,7 @@ struct TmaLayout {
     __host__ __device__ static constexpr int smem_bytes() { return words() * 8 * stages(); }
 };
 
-template <int POL, u32 M, bool ECH>
+template <int POL, int SEM, u32 M, bool ECH>
 __global__ void __launch_bounds__(TPB, 2) k_fused_tma(RoundArgs a, u32 ntiles) {
     constexpr int NT = Policy<POL, 0>::NT;
     constexpr u32 FULL = (1u << NT) - 1;
@@ -626,13 +633,22 @@ __global__ void __launch_bounds__(TPB, 2) k_fused_tma(RoundArgs a, u32 ntiles) {
     auto issue = [&](u32 tile, int s) {
         mbar_expect_tx(&full_bar[s], (u32)(SW * 8));
         u64* dst = tma_smem + (size_t)s * SW;
+        if (SEM == SEM_LSB) {
+            // entries 4 TQ tile .. 4 TQ (tile + 1) - 1, one copy per component
 #pragma unroll
-        for (int t = 0; t < NT; t++)
-#pragma unroll
-            for (int q = 0; q < 4; q++)
+            for (int t = 0; t < NT; t++)
 #pragma unroll
                 for (int c = 0; c < LAY::nc(t); c++)
-                    tma_load_1d(dst + LAY::off(t, q, c), a.t[t].in[c] + q * Q + (u64)tile * TQ, TQ * 8, &full_bar[s]);
+                    tma_load_1d(dst + LAY::offl(t, c), a.t[t].in[c] + (u64)tile * 4 * TQ, 4 * TQ * 8, &full_bar[s]);
+        } else {
+#pragma unroll
+            for (int t = 0; t < NT; t++)
+#pragma unroll
+                for (int q = 0; q < 4; q++)
+#pragma unroll
+                    for (int c = 0; c < LAY::nc(t); c++)
+                        tma_load_1d(dst + LAY::off(t, q, c), a.t[t].in[c] + q * Q + (u64)tile * TQ, TQ * 8, &full_bar[s]);
+        }
     };
     if (threadIdx.x == 0) {
         for (int s = 0; s < S; s++) {
@@ -664,14 +680,31 @@ __global__ void __launch_bounds__(TPB, 2) k_fused_tma(RoundArgs a, u32 ntiles) {
 #pragma unroll
         for (int t = 0; t < NT; t++) {
             F3 x[4];
+            if (SEM == SEM_LSB) {
+                // entries 4i .. 4i+3 of the tile, two 16-byte loads per component
+                u64 w[3][4];
 #pragma unroll
-            for (int q = 0; q < 4; q++) {
-                x[q].c0 = st_[LAY::off(t, q, 0) + threadIdx.x];
-                if (LAY::nc(t) == 3) {
-                    x[q].c1 = st_[LAY::off(t, q, 1) + threadIdx.x];
-                    x[q].c2 = st_[LAY::off(t, q, 2) + threadIdx.x];
-                } else {
-                    x[q].c1 = x[q].c2 = 0;
+                for (int c = 0; c < 3; c++) {
+                    if (c < LAY::nc(t)) {
+                        const ulonglong2* p = (const ulonglong2*)(st_ + LAY::offl(t, c)) + 2 * threadIdx.x;
+                        const ulonglong2 v0 = p[0], v1 = p[1];
+                        w[c][0] = v0.x; w[c][1] = v0.y; w[c][2] = v1.x; w[c][3] = v1.y;
+                    } else {
+                        w[c][0] = w[c][1] = w[c][2] = w[c][3] = 0;
+                    }
+                }
+#pragma unroll
+                for (int q = 0; q < 4; q++) x[q] = f3_make(w[0][q], w[1][q], w[2][q]);
+            } else {
+#pragma unroll
+                for (int q = 0; q < 4; q++) {
+                    x[q].c0 = st_[LAY::off(t, q, 0) + threadIdx.x];
+                    if (LAY::nc(t) == 3) {
+                        x[q].c1 = st_[LAY::off(t, q, 1) + threadIdx.x];
+                        x[q].c2 = st_[LAY::off(t, q, 2) + threadIdx.x];
+                    } else {
+                        x[q].c1 = x[q].c2 = 0;
+                    }
                 }
             }
             if (t == NT - 1) {
@@ -691,10 +724,19 @@ __global__ void __launch_bounds__(TPB, 2) k_fused_tma(RoundArgs a, u32 ntiles) {
                     }
                 }
             }
-            if (ext_of<M>(t)) { lo[t] = f3_fold<true, true>(x[0], x[2], r); hi[t] = f3_fold<true, true>(x[1], x[3], r); }
-            else if (ECH) { lo[t] = f3_fold<false, true>(x[0], x[2], r); hi[t] = f3_fold<false, true>(x[1], x[3], r); }
-            else { lo[t] = f3_fold<false, false>(x[0], x[2], r); hi[t] = f3_fold<false, false>(x[1], x[3], r); }
-            if (ext_of<MO>(t)) { st<true>(a.t[t].out, k, lo[t]); st<true>(a.t[t].out, k + Q, hi[t]); }
+            // MSB pairs (k, k + 2Q) and (k + Q, k + 3Q); LSB pairs (4i, 4i+1) and (4i+2, 4i+3)
+            constexpr int PB = SEM == SEM_LSB ? 1 : 2, HA = SEM == SEM_LSB ? 2 : 1;
+            if (ext_of<M>(t)) { lo[t] = f3_fold<true, true>(x[0], x[PB], r); hi[t] = f3_fold<true, true>(x[HA], x[HA + PB], r); }
+            else if (ECH) { lo[t] = f3_fold<false, true>(x[0], x[PB], r); hi[t] = f3_fold<false, true>(x[HA], x[HA + PB], r); }
+            else { lo[t] = f3_fold<false, false>(x[0], x[PB], r); hi[t] = f3_fold<false, false>(x[HA], x[HA + PB], r); }
+            if (SEM == SEM_LSB) {
+                // folded entries 2k, 2k+1: one 16-byte store per component
+                ((ulonglong2*)a.t[t].out[0])[k] = make_ulonglong2(lo[t].c0, hi[t].c0);
+                if (ext_of<MO>(t)) {
+                    ((ulonglong2*)a.t[t].out[1])[k] = make_ulonglong2(lo[t].c1, hi[t].c1);
+                    ((ulonglong2*)a.t[t].out[2])[k] = make_ulonglong2(lo[t].c2, hi[t].c2);
+                }
+            } else if (ext_of<MO>(t)) { st<true>(a.t[t].out, k, lo[t]); st<true>(a.t[t].out, k + Q, hi[t]); }
             else { st<false>(a.t[t].out, k, lo[t]); st<false>(a.t[t].out, k + Q, hi[t]); }
         }
         acc.pair(lo, hi);

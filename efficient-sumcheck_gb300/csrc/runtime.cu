@@ -493,17 +493,21 @@ int round_std(effsc_prover* P, const Chal& ch, const TxIO& tx, bool dry) {
             uint64_t bytes = 0;
             for (int i = 0; i < nt; i++) bytes += L * wbytes(P->t[i].ext) + (L / 2) * wbytes(P->t[i].ext || ech);
             const char* nm = mask ? "fused_round_fp3" : (ech ? "fused_round_fp_to_fp3" : "fused_round_fp");
-            // large power-of-two MSB rounds: the TMA-staged kernel
+            // large power-of-two rounds: the TMA-staged kernel (LSB also
+            // stores the folded pairs with 16-byte stores)
             const u64 Q = L / 4;
-            bool tma = pol == POL_IP && sem == SEM_MSB_PAD && is_pow2(L) && Q >= TMA_MIN_QUADS && Q % KERNEL_TPB == 0;
+            bool tma = pol == POL_IP && (sem == SEM_MSB_PAD || sem == SEM_LSB) && is_pow2(L) && Q >= TMA_MIN_QUADS &&
+                       Q % KERNEL_TPB == 0;
             for (int i = 0; i < nt; i++) tma &= !P->t[i].bufs[P->t[i].cur].host;
             for (int i = 0; i < nt && tma; i++)
-                for (int c = 0; c < (P->t[i].ext ? 3 : 1); c++)
-                    tma &= ((uintptr_t)a.t[i].in[c] % 16) == 0;
+                for (int c = 0; c < 3; c++) {
+                    if (c < (P->t[i].ext ? 3 : 1)) tma &= ((uintptr_t)a.t[i].in[c] % 16) == 0;
+                    if (sem == SEM_LSB && a.t[i].out[c]) tma &= ((uintptr_t)a.t[i].out[c] % 16) == 0;
+                }
             if (tma) {
                 u32 ntiles = (u32)(Q / KERNEL_TPB);
                 int g = std::min<int>((int)ntiles, (max_grid() / 8) * fused_tma_blocks_per_sm());
-                if (!dry) TRY(timed_launch(P->ctx->stream, nm, bytes, [&] { return launch_fused_tma(pol, mask, ech, a, ntiles, g, P->ctx->stream); }));
+                if (!dry) TRY(timed_launch(P->ctx->stream, nm, bytes, [&] { return launch_fused_tma(pol, sem, mask, ech, a, ntiles, g, P->ctx->stream); }));
             } else {
                 if (!dry) TRY(timed_launch(P->ctx->stream, nm, bytes, [&] { return launch_fused(pol, sem, mask, ech, a, grid_for(L / 4), P->ctx->stream); }));
             }
