@@ -14,6 +14,11 @@
 // queued ahead of the GPU; the host never waits on a step unless it must
 // reuse that step's staging memory.
 //
+// Once a request's tables fit in one block's shared memory, its remaining
+// rounds run in one tail launch (a block per request, on a second stream so
+// they overlap the step) instead of one step each; its final fold joins the
+// first step after the tail has finished.
+//
 // Each request's arithmetic, reductions and transcript are exactly those of
 // the single-instance path (its own RoundArgs, grid-reduction counter and
 // device transcript), so a proof does not depend on what else is in flight.
@@ -67,6 +72,8 @@ struct Req {
     u64* res = nullptr;    // RES_WORDS proof words | transcript | counter
     u32 round = 0;         // next round (n: finalize)
     bool two_pass = false; // InnerProduct over Fp3, n >= 3: rounds 0-2 in two steps (ip01.cuh)
+    bool in_tail = false;  // the remaining rounds are running in a tail launch
+    cudaEvent_t tail_ev = nullptr;
     int slot = -1;         // pinned result slot
     cudaEvent_t ev = nullptr;
     u64* in(int t) const { return mem + (size_t)t * words_per_table(); }
@@ -109,9 +116,14 @@ struct effsc_server {
         ServeSeg* h_segs = nullptr;
         RoundArgs* h_args = nullptr;
         DevTranscript* h_tx = nullptr;
+        TailArgs* h_tail = nullptr;   // tail launches of the step (pinned)
+        TailArgs* d_tail = nullptr;
         cudaEvent_t ev = nullptr;
-        bool busy = false;
+        cudaEvent_t pre = nullptr;    // main stream before the step's kernel
+        cudaEvent_t tail_done = nullptr;
+        bool busy = false, tail_busy = false;
     } stage[SERVE_INFLIGHT];
+    cudaStream_t tail_stream = nullptr;
     int next_stage = 0;
     ServeSeg* d_segs = nullptr;
     RoundArgs* d_args = nullptr;
@@ -208,6 +220,44 @@ int admit(effsc_server* s, effsc_server::Stage& st, u32* ntx, std::vector<Req*>&
     return EFFSC_OK;
 }
 
+// Current table length of a request about to run round `round`.
+u64 req_len(const Req& r) { return r.round == 0 ? (1ULL << r.n) : (1ULL << (r.n - r.round + 1)); }
+
+// The request's remaining rounds fit one tail launch: its tables fit in one
+// block's shared memory (not in the middle of the two-pass start).
+bool tail_eligible(const Req& r) {
+    if (r.in_tail || r.round >= r.n) return false;
+    if (r.two_pass && (r.round == 1 || r.round == 2)) return false;
+    const int pol = r.kind == EFFSC_IP ? POL_IP : POL_ML, fw = r.field == EFFSC_FP3 ? 3 : 1;
+    return req_len(r) <= tail_max_len(pol, fw, TAIL_SMEM_CAP);
+}
+
+void fill_tail(const Req& r, TailArgs& ta) {
+    memset(&ta, 0, sizeof ta);
+    const bool f3 = r.field == EFFSC_FP3;
+    const int F3W = f3 ? 3 : 1;
+    const u32 rd = r.round;
+    const u64 half0 = 1ULL << (r.n - 1);
+    ta.L = req_len(r);
+    ta.nrounds = r.n - rd;
+    ta.first_fold = rd ? 1 : 0;
+    ta.chal_in = rd ? r.chal() + 3 * (rd - 1) : nullptr;
+    ta.tx = r.tx();
+    ta.proof_wire = r.wire() + (size_t)3 * deg_of_kind(r.kind) * rd;
+    ta.proof_chal = r.chal() + 3 * rd;
+    const u32 folds = ta.nrounds - (rd ? 0 : 1);
+    for (int t = 0; t < r.ntab; t++) {
+        if (rd <= 1) ta.in[t][0] = r.in(t);
+        else {
+            for (int c = 0; c < F3W; c++) ta.in[t][c] = r.work(t) + c * half0;
+            if (f3) ta.in_ext |= 1u << t;
+        }
+        // the folded tables of length 2 go where the final fold reads them
+        if (folds)
+            for (int c = 0; c < F3W; c++) ta.out[t][c] = r.work(t) + c * half0;
+    }
+}
+
 // One serving step: every active request runs its next round or finalises.
 int step(effsc_server* s) {
     cudaStream_t cs = s->stream;
@@ -215,6 +265,10 @@ int step(effsc_server* s) {
     if (st.busy) {
         SCK(cudaEventSynchronize(st.ev));
         st.busy = false;
+    }
+    if (st.tail_busy) {
+        SCK(cudaEventSynchronize(st.tail_done));
+        st.tail_busy = false;
     }
     u32 ntx = 0;
     std::vector<Req*> fresh;
@@ -228,8 +282,19 @@ int step(effsc_server* s) {
     const int maxb = max_grid();
     const u64 per_block = (u64)KERNEL_TPB * s->quads_per_thread;
     u32 first = 0, nseg = 0;
-    std::vector<Req*> finals;
+    std::vector<Req*> finals, tails;
     for (Req* r : s->active) {
+        if (r->in_tail) {
+            const cudaError_t q = cudaEventQuery(r->tail_ev);
+            if (q == cudaErrorNotReady) continue;   // still in its tail: nothing this step
+            if (q != cudaSuccess) return effsc_set_error(EFFSC_CUDA_ERROR, "serving tail: %s", cudaGetErrorString(q));
+            s->free_events.push_back(r->tail_ev);
+            r->tail_ev = nullptr;
+            r->in_tail = false;                      // round == n: the final fold below
+        } else if (tail_eligible(*r)) {
+            tails.push_back(r);
+            continue;
+        }
         const bool f3 = r->field == EFFSC_FP3;
         const int F3W = f3 ? 3 : 1;
         const int pol = r->kind == EFFSC_IP ? POL_IP : POL_ML;
@@ -299,15 +364,55 @@ int step(effsc_server* s) {
         nseg++;
     }
     if (first > s->partial_blocks) return effsc_set_error(EFFSC_INVALID_ARG, "serving step larger than planned");
-    for (u32 k = 0; k < nseg; k++) st.h_args[k].partials = s->d_partials + (size_t)st.h_segs[k].first_block * 12;
-    SCK(cudaMemcpyAsync(s->d_segs, st.h_segs, nseg * sizeof(ServeSeg), cudaMemcpyHostToDevice, cs));
-    SCK(cudaMemcpyAsync(s->d_args, st.h_args, nseg * sizeof(RoundArgs), cudaMemcpyHostToDevice, cs));
-    launch_serve_step(s->d_segs, nseg, s->d_args, first, cs);
-    cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess) return effsc_set_error(EFFSC_CUDA_ERROR, "serving step launch: %s", cudaGetErrorString(e));
-    s->kernels++;
+    if (!tails.empty()) {
+        // the tails depend on the requests' earlier rounds and admission
+        // copies, all on the main stream before this point
+        SCK(cudaEventRecord(st.pre, cs));
+        SCK(cudaStreamWaitEvent(s->tail_stream, st.pre, 0));
+    }
+    if (nseg) {
+        for (u32 k = 0; k < nseg; k++) st.h_args[k].partials = s->d_partials + (size_t)st.h_segs[k].first_block * 12;
+        SCK(cudaMemcpyAsync(s->d_segs, st.h_segs, nseg * sizeof(ServeSeg), cudaMemcpyHostToDevice, cs));
+        SCK(cudaMemcpyAsync(s->d_args, st.h_args, nseg * sizeof(RoundArgs), cudaMemcpyHostToDevice, cs));
+        launch_serve_step(s->d_segs, nseg, s->d_args, first, cs);
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return effsc_set_error(EFFSC_CUDA_ERROR, "serving step launch: %s", cudaGetErrorString(e));
+        s->kernels++;
+        effsc_internal_add_launches(1);
+    }
     s->steps++;
-    effsc_internal_add_launches(1);
+    if (!tails.empty()) {
+        // one tail launch per (kind, field) group, a block per request
+        cudaStream_t ts = s->tail_stream;
+        u32 nt = 0;
+        for (int pol : {POL_IP, POL_ML})
+            for (int fw : {1, 3}) {
+                const u32 off = nt;
+                u64 maxL = 0;
+                for (Req* r : tails) {
+                    if ((r->kind == EFFSC_IP ? POL_IP : POL_ML) != pol || (r->field == EFFSC_FP3 ? 3 : 1) != fw) continue;
+                    fill_tail(*r, st.h_tail[nt]);
+                    maxL = std::max<u64>(maxL, st.h_tail[nt].L);
+                    nt++;
+                }
+                if (nt == off) continue;
+                SCK(cudaMemcpyAsync(st.d_tail + off, st.h_tail + off, (nt - off) * sizeof(TailArgs), cudaMemcpyHostToDevice, ts));
+                if (!launch_tail(pol, fw, st.d_tail + off, nullptr, nt - off, maxL, ts))
+                    return effsc_set_error(EFFSC_CUDA_ERROR, "serving tail launch failed");
+                cudaError_t e = cudaGetLastError();
+                if (e != cudaSuccess) return effsc_set_error(EFFSC_CUDA_ERROR, "serving tail launch: %s", cudaGetErrorString(e));
+                s->kernels++;
+                effsc_internal_add_launches(1);
+            }
+        for (Req* r : tails) {
+            r->tail_ev = get_event(s);
+            SCK(cudaEventRecord(r->tail_ev, ts));
+            r->in_tail = true;
+            r->round = r->n;
+        }
+        SCK(cudaEventRecord(st.tail_done, ts));
+        st.tail_busy = true;
+    }
     // finished requests: proof to pinned memory, memory back to the pool
     for (Req* r : finals) {
         if (s->free_slots.empty()) {
@@ -331,7 +436,9 @@ int step(effsc_server* s) {
     std::vector<Req*> still;
     still.reserve(s->active.size());
     for (Req* r : s->active) {
-        if (r->round < r->n) {
+        if (r->in_tail) {
+            still.push_back(r);            // its final fold comes after the tail
+        } else if (r->round < r->n) {
             r->round += (r->two_pass && r->round == 0) ? 2 : 1;
             still.push_back(r);
         }
@@ -421,9 +528,15 @@ int effsc_server_create(effsc_ctx* ctx, uint64_t hbm_budget_bytes, uint32_t max_
         if (cudaHostAlloc((void**)&st.h_segs, max_active * sizeof(ServeSeg), cudaHostAllocDefault) != cudaSuccess ||
             cudaHostAlloc((void**)&st.h_args, max_active * sizeof(RoundArgs), cudaHostAllocDefault) != cudaSuccess ||
             cudaHostAlloc((void**)&st.h_tx, max_active * sizeof(DevTranscript), cudaHostAllocDefault) != cudaSuccess ||
-            cudaEventCreateWithFlags(&st.ev, cudaEventDisableTiming) != cudaSuccess)
+            cudaHostAlloc((void**)&st.h_tail, max_active * sizeof(TailArgs), cudaHostAllocDefault) != cudaSuccess ||
+            cudaMalloc((void**)&st.d_tail, max_active * sizeof(TailArgs)) != cudaSuccess ||
+            cudaEventCreateWithFlags(&st.ev, cudaEventDisableTiming) != cudaSuccess ||
+            cudaEventCreateWithFlags(&st.pre, cudaEventDisableTiming) != cudaSuccess ||
+            cudaEventCreateWithFlags(&st.tail_done, cudaEventDisableTiming) != cudaSuccess)
             return bail(effsc_set_error(EFFSC_OOM, "serving: pinned staging allocation failed"));
     }
+    if (cudaStreamCreateWithFlags(&s->tail_stream, cudaStreamNonBlocking) != cudaSuccess)
+        return bail(effsc_set_error(EFFSC_CUDA_ERROR, "serving: stream creation failed"));
     const size_t nslots = (size_t)2 * max_active * SERVE_INFLIGHT;
     if (cudaMalloc((void**)&s->d_segs, max_active * sizeof(ServeSeg)) != cudaSuccess ||
         cudaMalloc((void**)&s->d_args, max_active * sizeof(RoundArgs)) != cudaSuccess ||
@@ -441,10 +554,12 @@ int effsc_server_create(effsc_ctx* ctx, uint64_t hbm_budget_bytes, uint32_t max_
 int effsc_server_destroy(effsc_server* s) {
     if (!s) return EFFSC_OK;
     cudaSetDevice(s->device);
+    if (s->tail_stream) cudaStreamSynchronize(s->tail_stream);
     cudaStreamSynchronize(s->stream);
     for (Req* r : s->active) {
         if (r->mem) cudaFreeAsync(r->mem, s->stream);
         if (r->res) cudaFreeAsync(r->res, s->stream);
+        if (r->tail_ev) cudaEventDestroy(r->tail_ev);
         delete r;
     }
     for (Req* r : s->queue) delete r;
@@ -456,8 +571,13 @@ int effsc_server_destroy(effsc_server* s) {
         if (st.h_segs) cudaFreeHost(st.h_segs);
         if (st.h_args) cudaFreeHost(st.h_args);
         if (st.h_tx) cudaFreeHost(st.h_tx);
+        if (st.h_tail) cudaFreeHost(st.h_tail);
+        if (st.d_tail) cudaFree(st.d_tail);
         if (st.ev) cudaEventDestroy(st.ev);
+        if (st.pre) cudaEventDestroy(st.pre);
+        if (st.tail_done) cudaEventDestroy(st.tail_done);
     }
+    if (s->tail_stream) cudaStreamDestroy(s->tail_stream);
     if (s->d_segs) cudaFree(s->d_segs);
     if (s->d_args) cudaFree(s->d_args);
     if (s->d_partials) cudaFree(s->d_partials);
