@@ -98,19 +98,20 @@ size_t res_bytes() { return (RES_WORDS + TX_WORDS + 1) * sizeof(u64); }
 
 }  // namespace
 
-struct effsc_server {
-    effsc_ctx* ctx = nullptr;
-    int device = 0;
+// Requests are split by size into two lanes, each with its own stream, FIFO
+// queue, step staging and active set: a step of the small lane does not wait
+// for the large requests' early rounds, and large requests do not block the
+// admission of small ones.  Both lanes share the HBM budget, the slot limit,
+// the memory pool and the result slots.
+constexpr int SERVE_LANES = 2;
+constexpr u32 SERVE_BIG_N = 22;   // requests of at least 2^22 entries per table: lane 1
+
+struct Lane {
     cudaStream_t stream = nullptr;
-    cudaMemPool_t pool = nullptr;
-    uint64_t budget = 0, reserved = 0;
-    u32 max_active = 0;
-    int quads_per_thread = 8;
-    uint64_t next_id = 0;
+    bool own_stream = false;
+    cudaStream_t tail_stream = nullptr;
     std::deque<Req*> queue;
     std::vector<Req*> active;
-    std::deque<Req*> finishing;
-    std::deque<Done> done;
     // step staging: pinned host + device copies of segments and args
     struct Stage {
         ServeSeg* h_segs = nullptr;
@@ -119,15 +120,27 @@ struct effsc_server {
         TailArgs* h_tail = nullptr;   // tail launches of the step (pinned)
         TailArgs* d_tail = nullptr;
         cudaEvent_t ev = nullptr;
-        cudaEvent_t pre = nullptr;    // main stream before the step's kernel
+        cudaEvent_t pre = nullptr;    // lane stream before the step's kernel
         cudaEvent_t tail_done = nullptr;
         bool busy = false, tail_busy = false;
     } stage[SERVE_INFLIGHT];
-    cudaStream_t tail_stream = nullptr;
     int next_stage = 0;
     ServeSeg* d_segs = nullptr;
     RoundArgs* d_args = nullptr;
     u64* d_partials = nullptr;
+};
+
+struct effsc_server {
+    effsc_ctx* ctx = nullptr;
+    int device = 0;
+    cudaMemPool_t pool = nullptr;
+    uint64_t budget = 0, reserved = 0;
+    u32 max_active = 0, n_active = 0;
+    int quads_per_thread = 8;
+    uint64_t next_id = 0;
+    Lane lane[SERVE_LANES];
+    std::deque<Req*> finishing;
+    std::deque<Done> done;
     u32* h_status = nullptr;
     u32* d_status = nullptr;
     size_t partial_blocks = 0;
@@ -185,12 +198,13 @@ int retire(effsc_server* s, bool wait_one) {
     return EFFSC_OK;
 }
 
-// Admit queued requests (FIFO) while a slot and the HBM budget allow.
-// Initial transcript states go through the pinned staging of the next step.
-int admit(effsc_server* s, effsc_server::Stage& st, u32* ntx, std::vector<Req*>& fresh) {
-    cudaStream_t cs = s->stream;
-    while (!s->queue.empty() && s->active.size() < s->max_active) {
-        Req* r = s->queue.front();
+// Admit the lane's queued requests (FIFO) while a slot and the HBM budget
+// allow.  Initial transcript states go through the pinned staging of the
+// lane's next step.
+int admit(effsc_server* s, Lane& ln, Lane::Stage& st, u32* ntx, std::vector<Req*>& fresh) {
+    cudaStream_t cs = ln.stream;
+    while (!ln.queue.empty() && s->n_active < s->max_active) {
+        Req* r = ln.queue.front();
         if (s->reserved + r->bytes > s->budget) break;
         void* mem = nullptr;
         void* res = nullptr;
@@ -214,8 +228,9 @@ int admit(effsc_server* s, effsc_server::Stage& st, u32* ntx, std::vector<Req*>&
         fresh.push_back(r);
         r->round = 0;
         r->t_admit = now_s();
-        s->queue.pop_front();
-        s->active.push_back(r);
+        ln.queue.pop_front();
+        ln.active.push_back(r);
+        s->n_active++;
     }
     return EFFSC_OK;
 }
@@ -258,10 +273,11 @@ void fill_tail(const Req& r, TailArgs& ta) {
     }
 }
 
-// One serving step: every active request runs its next round or finalises.
-int step(effsc_server* s) {
-    cudaStream_t cs = s->stream;
-    effsc_server::Stage& st = s->stage[s->next_stage];
+// One serving step of a lane: every active request runs its next round or
+// finalises (or its remaining rounds start in a tail launch).
+int step(effsc_server* s, Lane& ln) {
+    cudaStream_t cs = ln.stream;
+    Lane::Stage& st = ln.stage[ln.next_stage];
     if (st.busy) {
         SCK(cudaEventSynchronize(st.ev));
         st.busy = false;
@@ -272,18 +288,18 @@ int step(effsc_server* s) {
     }
     u32 ntx = 0;
     std::vector<Req*> fresh;
-    int rc = admit(s, st, &ntx, fresh);
+    int rc = admit(s, ln, st, &ntx, fresh);
     if (rc != EFFSC_OK) return rc;
     // initial transcript states of the admitted requests: one H2D each from
     // the pinned stage (they are small and few)
     for (u32 k = 0; k < ntx; k++)
         SCK(cudaMemcpyAsync(fresh[k]->tx(), &st.h_tx[k], sizeof(DevTranscript), cudaMemcpyHostToDevice, cs));
-    if (s->active.empty()) return EFFSC_OK;
+    if (ln.active.empty()) return EFFSC_OK;
     const int maxb = max_grid();
     const u64 per_block = (u64)KERNEL_TPB * s->quads_per_thread;
     u32 first = 0, nseg = 0;
     std::vector<Req*> finals, tails;
-    for (Req* r : s->active) {
+    for (Req* r : ln.active) {
         if (r->in_tail) {
             const cudaError_t q = cudaEventQuery(r->tail_ev);
             if (q == cudaErrorNotReady) continue;   // still in its tail: nothing this step
@@ -366,15 +382,15 @@ int step(effsc_server* s) {
     if (first > s->partial_blocks) return effsc_set_error(EFFSC_INVALID_ARG, "serving step larger than planned");
     if (!tails.empty()) {
         // the tails depend on the requests' earlier rounds and admission
-        // copies, all on the main stream before this point
+        // copies, all on the lane's stream before this point
         SCK(cudaEventRecord(st.pre, cs));
-        SCK(cudaStreamWaitEvent(s->tail_stream, st.pre, 0));
+        SCK(cudaStreamWaitEvent(ln.tail_stream, st.pre, 0));
     }
     if (nseg) {
-        for (u32 k = 0; k < nseg; k++) st.h_args[k].partials = s->d_partials + (size_t)st.h_segs[k].first_block * 12;
-        SCK(cudaMemcpyAsync(s->d_segs, st.h_segs, nseg * sizeof(ServeSeg), cudaMemcpyHostToDevice, cs));
-        SCK(cudaMemcpyAsync(s->d_args, st.h_args, nseg * sizeof(RoundArgs), cudaMemcpyHostToDevice, cs));
-        launch_serve_step(s->d_segs, nseg, s->d_args, first, cs);
+        for (u32 k = 0; k < nseg; k++) st.h_args[k].partials = ln.d_partials + (size_t)st.h_segs[k].first_block * 12;
+        SCK(cudaMemcpyAsync(ln.d_segs, st.h_segs, nseg * sizeof(ServeSeg), cudaMemcpyHostToDevice, cs));
+        SCK(cudaMemcpyAsync(ln.d_args, st.h_args, nseg * sizeof(RoundArgs), cudaMemcpyHostToDevice, cs));
+        launch_serve_step(ln.d_segs, nseg, ln.d_args, first, cs);
         cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) return effsc_set_error(EFFSC_CUDA_ERROR, "serving step launch: %s", cudaGetErrorString(e));
         s->kernels++;
@@ -383,7 +399,7 @@ int step(effsc_server* s) {
     s->steps++;
     if (!tails.empty()) {
         // one tail launch per (kind, field) group, a block per request
-        cudaStream_t ts = s->tail_stream;
+        cudaStream_t ts = ln.tail_stream;
         u32 nt = 0;
         for (int pol : {POL_IP, POL_ML})
             for (int fw : {1, 3}) {
@@ -431,11 +447,12 @@ int step(effsc_server* s) {
         r->mem = nullptr;
         r->res = nullptr;
         s->reserved -= r->bytes;
+        s->n_active--;
         s->finishing.push_back(r);
     }
     std::vector<Req*> still;
-    still.reserve(s->active.size());
-    for (Req* r : s->active) {
+    still.reserve(ln.active.size());
+    for (Req* r : ln.active) {
         if (r->in_tail) {
             still.push_back(r);            // its final fold comes after the tail
         } else if (r->round < r->n) {
@@ -443,11 +460,17 @@ int step(effsc_server* s) {
             still.push_back(r);
         }
     }
-    s->active.swap(still);
+    ln.active.swap(still);
     SCK(cudaEventRecord(st.ev, cs));
     st.busy = true;
-    s->next_stage = (s->next_stage + 1) % SERVE_INFLIGHT;
+    ln.next_stage = (ln.next_stage + 1) % SERVE_INFLIGHT;
     return EFFSC_OK;
+}
+
+size_t n_queued(const effsc_server* s) {
+    size_t q = 0;
+    for (const Lane& ln : s->lane) q += ln.queue.size();
+    return q;
 }
 
 int submit_one(effsc_server* s, int kind, int field, uint32_t num_vars, const uint64_t* const* host_tables,
@@ -477,7 +500,7 @@ int submit_one(effsc_server* s, int kind, int field, uint32_t num_vars, const ui
         return effsc_set_error(EFFSC_INVALID_ARG, "request needs %zu bytes, more than the HBM budget", b);
     }
     r->t_submit = t_submit;
-    s->queue.push_back(r);
+    s->lane[num_vars >= SERVE_BIG_N ? 1 : 0].queue.push_back(r);
     if (id) *id = r->id;
     return EFFSC_OK;
 }
@@ -509,7 +532,6 @@ int effsc_server_create(effsc_ctx* ctx, uint64_t hbm_budget_bytes, uint32_t max_
     effsc_server* s = new effsc_server();
     s->ctx = ctx;
     s->device = effsc_internal_ctx_device(ctx);
-    s->stream = effsc_internal_ctx_stream(ctx);
     s->budget = hbm_budget_bytes;
     s->max_active = max_active;
     auto bail = [&](int rc) { effsc_server_destroy(s); return rc; };
@@ -523,25 +545,33 @@ int effsc_server_create(effsc_ctx* ctx, uint64_t hbm_budget_bytes, uint32_t max_
     uint64_t keep = ~0ULL;   // keep freed memory in the pool for the next admissions
     cudaMemPoolSetAttribute(s->pool, cudaMemPoolAttrReleaseThreshold, &keep);
     s->partial_blocks = (size_t)max_active * max_grid();
-    for (int k = 0; k < SERVE_INFLIGHT; k++) {
-        effsc_server::Stage& st = s->stage[k];
-        if (cudaHostAlloc((void**)&st.h_segs, max_active * sizeof(ServeSeg), cudaHostAllocDefault) != cudaSuccess ||
-            cudaHostAlloc((void**)&st.h_args, max_active * sizeof(RoundArgs), cudaHostAllocDefault) != cudaSuccess ||
-            cudaHostAlloc((void**)&st.h_tx, max_active * sizeof(DevTranscript), cudaHostAllocDefault) != cudaSuccess ||
-            cudaHostAlloc((void**)&st.h_tail, max_active * sizeof(TailArgs), cudaHostAllocDefault) != cudaSuccess ||
-            cudaMalloc((void**)&st.d_tail, max_active * sizeof(TailArgs)) != cudaSuccess ||
-            cudaEventCreateWithFlags(&st.ev, cudaEventDisableTiming) != cudaSuccess ||
-            cudaEventCreateWithFlags(&st.pre, cudaEventDisableTiming) != cudaSuccess ||
-            cudaEventCreateWithFlags(&st.tail_done, cudaEventDisableTiming) != cudaSuccess)
-            return bail(effsc_set_error(EFFSC_OOM, "serving: pinned staging allocation failed"));
+    for (int l = 0; l < SERVE_LANES; l++) {
+        Lane& ln = s->lane[l];
+        if (l == 0) ln.stream = effsc_internal_ctx_stream(ctx);
+        else if (cudaStreamCreateWithFlags(&ln.stream, cudaStreamNonBlocking) != cudaSuccess)
+            return bail(effsc_set_error(EFFSC_CUDA_ERROR, "serving: stream creation failed"));
+        else ln.own_stream = true;
+        if (cudaStreamCreateWithFlags(&ln.tail_stream, cudaStreamNonBlocking) != cudaSuccess)
+            return bail(effsc_set_error(EFFSC_CUDA_ERROR, "serving: stream creation failed"));
+        for (int k = 0; k < SERVE_INFLIGHT; k++) {
+            Lane::Stage& st = ln.stage[k];
+            if (cudaHostAlloc((void**)&st.h_segs, max_active * sizeof(ServeSeg), cudaHostAllocDefault) != cudaSuccess ||
+                cudaHostAlloc((void**)&st.h_args, max_active * sizeof(RoundArgs), cudaHostAllocDefault) != cudaSuccess ||
+                cudaHostAlloc((void**)&st.h_tx, max_active * sizeof(DevTranscript), cudaHostAllocDefault) != cudaSuccess ||
+                cudaHostAlloc((void**)&st.h_tail, max_active * sizeof(TailArgs), cudaHostAllocDefault) != cudaSuccess ||
+                cudaMalloc((void**)&st.d_tail, max_active * sizeof(TailArgs)) != cudaSuccess ||
+                cudaEventCreateWithFlags(&st.ev, cudaEventDisableTiming) != cudaSuccess ||
+                cudaEventCreateWithFlags(&st.pre, cudaEventDisableTiming) != cudaSuccess ||
+                cudaEventCreateWithFlags(&st.tail_done, cudaEventDisableTiming) != cudaSuccess)
+                return bail(effsc_set_error(EFFSC_OOM, "serving: pinned staging allocation failed"));
+        }
+        if (cudaMalloc((void**)&ln.d_segs, max_active * sizeof(ServeSeg)) != cudaSuccess ||
+            cudaMalloc((void**)&ln.d_args, max_active * sizeof(RoundArgs)) != cudaSuccess ||
+            cudaMalloc((void**)&ln.d_partials, s->partial_blocks * 12 * sizeof(u64)) != cudaSuccess)
+            return bail(effsc_set_error(EFFSC_OOM, "serving: allocation failed"));
     }
-    if (cudaStreamCreateWithFlags(&s->tail_stream, cudaStreamNonBlocking) != cudaSuccess)
-        return bail(effsc_set_error(EFFSC_CUDA_ERROR, "serving: stream creation failed"));
     const size_t nslots = (size_t)2 * max_active * SERVE_INFLIGHT;
-    if (cudaMalloc((void**)&s->d_segs, max_active * sizeof(ServeSeg)) != cudaSuccess ||
-        cudaMalloc((void**)&s->d_args, max_active * sizeof(RoundArgs)) != cudaSuccess ||
-        cudaMalloc((void**)&s->d_partials, s->partial_blocks * 12 * sizeof(u64)) != cudaSuccess ||
-        cudaHostAlloc((void**)&s->h_results, nslots * RES_WORDS * sizeof(u64), cudaHostAllocDefault) != cudaSuccess ||
+    if (cudaHostAlloc((void**)&s->h_results, nslots * RES_WORDS * sizeof(u64), cudaHostAllocDefault) != cudaSuccess ||
         cudaHostAlloc((void**)&s->h_status, sizeof(u32), cudaHostAllocMapped) != cudaSuccess ||
         cudaHostGetDevicePointer((void**)&s->d_status, s->h_status, 0) != cudaSuccess)
         return bail(effsc_set_error(EFFSC_OOM, "serving: allocation failed"));
@@ -554,33 +584,40 @@ int effsc_server_create(effsc_ctx* ctx, uint64_t hbm_budget_bytes, uint32_t max_
 int effsc_server_destroy(effsc_server* s) {
     if (!s) return EFFSC_OK;
     cudaSetDevice(s->device);
-    if (s->tail_stream) cudaStreamSynchronize(s->tail_stream);
-    cudaStreamSynchronize(s->stream);
-    for (Req* r : s->active) {
-        if (r->mem) cudaFreeAsync(r->mem, s->stream);
-        if (r->res) cudaFreeAsync(r->res, s->stream);
-        if (r->tail_ev) cudaEventDestroy(r->tail_ev);
-        delete r;
+    for (Lane& ln : s->lane) {
+        if (ln.tail_stream) cudaStreamSynchronize(ln.tail_stream);
+        if (ln.stream) cudaStreamSynchronize(ln.stream);
     }
-    for (Req* r : s->queue) delete r;
+    for (Lane& ln : s->lane) {
+        for (Req* r : ln.active) {
+            if (r->mem) cudaFreeAsync(r->mem, ln.stream);
+            if (r->res) cudaFreeAsync(r->res, ln.stream);
+            if (r->tail_ev) cudaEventDestroy(r->tail_ev);
+            delete r;
+        }
+        for (Req* r : ln.queue) delete r;
+        if (ln.stream) cudaStreamSynchronize(ln.stream);
+    }
     for (Req* r : s->finishing) { if (r->ev) cudaEventDestroy(r->ev); delete r; }
-    cudaStreamSynchronize(s->stream);
     for (cudaEvent_t e : s->free_events) cudaEventDestroy(e);
-    for (int k = 0; k < SERVE_INFLIGHT; k++) {
-        effsc_server::Stage& st = s->stage[k];
-        if (st.h_segs) cudaFreeHost(st.h_segs);
-        if (st.h_args) cudaFreeHost(st.h_args);
-        if (st.h_tx) cudaFreeHost(st.h_tx);
-        if (st.h_tail) cudaFreeHost(st.h_tail);
-        if (st.d_tail) cudaFree(st.d_tail);
-        if (st.ev) cudaEventDestroy(st.ev);
-        if (st.pre) cudaEventDestroy(st.pre);
-        if (st.tail_done) cudaEventDestroy(st.tail_done);
+    for (Lane& ln : s->lane) {
+        for (int k = 0; k < SERVE_INFLIGHT; k++) {
+            Lane::Stage& st = ln.stage[k];
+            if (st.h_segs) cudaFreeHost(st.h_segs);
+            if (st.h_args) cudaFreeHost(st.h_args);
+            if (st.h_tx) cudaFreeHost(st.h_tx);
+            if (st.h_tail) cudaFreeHost(st.h_tail);
+            if (st.d_tail) cudaFree(st.d_tail);
+            if (st.ev) cudaEventDestroy(st.ev);
+            if (st.pre) cudaEventDestroy(st.pre);
+            if (st.tail_done) cudaEventDestroy(st.tail_done);
+        }
+        if (ln.d_segs) cudaFree(ln.d_segs);
+        if (ln.d_args) cudaFree(ln.d_args);
+        if (ln.d_partials) cudaFree(ln.d_partials);
+        if (ln.tail_stream) cudaStreamDestroy(ln.tail_stream);
+        if (ln.own_stream) cudaStreamDestroy(ln.stream);
     }
-    if (s->tail_stream) cudaStreamDestroy(s->tail_stream);
-    if (s->d_segs) cudaFree(s->d_segs);
-    if (s->d_args) cudaFree(s->d_args);
-    if (s->d_partials) cudaFree(s->d_partials);
     if (s->h_results) cudaFreeHost(s->h_results);
     if (s->h_status) cudaFreeHost(s->h_status);
     if (s->pool) cudaMemPoolDestroy(s->pool);
@@ -599,15 +636,16 @@ int effsc_server_progress(effsc_server* s, int wait, uint32_t* pending) {
     SCK(cudaSetDevice(s->device));
     int rc = retire(s, false);
     if (rc != EFFSC_OK) return rc;
-    if (!s->active.empty() || !s->queue.empty()) {
-        rc = step(s);
-        if (rc != EFFSC_OK) return rc;
-    }
+    for (Lane& ln : s->lane)
+        if (!ln.active.empty() || !ln.queue.empty()) {
+            rc = step(s, ln);
+            if (rc != EFFSC_OK) return rc;
+        }
     if (wait && s->done.empty() && !s->finishing.empty()) {
         rc = retire(s, true);
         if (rc != EFFSC_OK) return rc;
     }
-    if (pending) *pending = (uint32_t)(s->queue.size() + s->active.size() + s->finishing.size());
+    if (pending) *pending = (uint32_t)(n_queued(s) + s->n_active + s->finishing.size());
     return EFFSC_OK;
 }
 
@@ -631,7 +669,7 @@ int effsc_server_run_trace(effsc_server* s, size_t n, const int* kinds, int fiel
                            uint64_t* final_values) {
     if (!s || !kinds || !num_vars || !seeds || !transcripts || !arrival_s || !latency_s)
         return effsc_set_error(EFFSC_INVALID_ARG, "NULL argument");
-    if (!s->queue.empty() || !s->active.empty() || !s->finishing.empty() || !s->done.empty())
+    if (n_queued(s) || s->n_active || !s->finishing.empty() || !s->done.empty())
         return effsc_set_error(EFFSC_INVALID_ARG, "run_trace needs an idle server");
     SCK(cudaSetDevice(s->device));
     std::vector<size_t> row(n + 1, 0), order(n);
@@ -656,7 +694,7 @@ int effsc_server_run_trace(effsc_server* s, size_t n, const int* kinds, int fiel
             of_id[id - id0] = i;
             next++;
         }
-        const bool idle = s->queue.empty() && s->active.empty();
+        const bool idle = !n_queued(s) && !s->n_active;
         if (!idle) {
             int rc = effsc_server_progress(s, 0, nullptr);
             if (rc != EFFSC_OK) return rc;
