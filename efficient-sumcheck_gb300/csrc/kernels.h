@@ -92,6 +92,11 @@ u64 tail_max_len(int pol, int fw, u64 smem_cap);
 constexpr u64 TAIL_SMEM_CAP = 200 * 1024;
 // One block per TailArgs; `smem_len` = largest L among them.
 bool launch_tail(int pol, int fw, const TailArgs* dev_args, const TailArgs* one, u32 n, u64 smem_len, cudaStream_t s);
+// Cluster tail: 2^cs_log CTAs hold a table of a.L entries (a.L >> cs_log per
+// CTA within TAIL_SMEM_CAP); needs a.first_fold = 1 and a.nrounds > cs_log + 1.
+bool launch_tail_cluster(int pol, int fw, const TailArgs& a, u32 cs_log, cudaStream_t s);
+// Largest cluster size the device runs for it (16, 8 or 0).
+u32 tail_cluster_max(void);
 
 // Serving steps: one entry per request in the step, sorted by first_block;
 // `code` = SERVE_IP (else ML) | SERVE_FP3 (else Fp) | phase << SERVE_PHASE_SHIFT.

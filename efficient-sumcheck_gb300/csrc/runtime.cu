@@ -555,7 +555,30 @@ bool tail_ok(const effsc_prover* P, size_t r, size_t num_rounds, const Chal& ch)
     return folds < 63 && (L >> folds) >= 2;
 }
 
-int do_tail(effsc_prover* P, size_t r, size_t num_rounds, const Chal& ch, const TxIO& tx, bool dry) {
+// cluster tail: the same tables up to tail_cluster_max() times one block's
+// capacity, entered mid-proof (a challenge to fold with), with at least
+// log2(CS) + 1 rounds left; *cs_log = log2(CS), CS = L / capacity.
+bool cluster_tail_ok(const effsc_prover* P, size_t r, size_t num_rounds, const Chal& ch, u32* cs_log) {
+    if ((P->kind != EFFSC_ML && P->kind != EFFSC_IP) || P->order != EFFSC_MSB || !P->tail_len) return false;
+    if (r >= num_rounds || !ch.has || !ch.dev) return false;
+    const size_t L = P->t[0].len;
+    for (int i = 1; i < P->ntab; i++)
+        if (P->t[i].len != L) return false;
+    if (!is_pow2(L) || L > P->tail_len) return false;
+    const int fw = P->field == EFFSC_FP3 ? 3 : 1;
+    const size_t cap = (size_t)tail_max_len(pol_of(P), fw, TAIL_SMEM_CAP);
+    if (L <= cap) return false;
+    const size_t cs = L / cap, csmax = tail_cluster_max();
+    if (cs > csmax || cs < 2 || cap < 32 * cs) return false;   // slices of whole 16-entry groups
+    u32 lg = 0;
+    while (((size_t)1 << lg) < cs) lg++;
+    const size_t rounds = num_rounds - r;
+    if (rounds < lg + 1 || rounds >= 63 || (L >> rounds) < 2) return false;
+    *cs_log = lg;
+    return true;
+}
+
+int do_tail(effsc_prover* P, size_t r, size_t num_rounds, const Chal& ch, const TxIO& tx, bool dry, u32 cs_log = 0) {
     const int pol = pol_of(P), fw = P->field == EFFSC_FP3 ? 3 : 1, nt = P->ntab;
     const size_t L = P->t[0].len, rounds = num_rounds - r, folds = rounds - (ch.has ? 0 : 1);
     TailArgs ta;
@@ -583,7 +606,10 @@ int do_tail(effsc_prover* P, size_t r, size_t num_rounds, const Chal& ch, const 
             bytes += (L >> folds) * wbytes(out_ext);
         }
     }
-    if (!dry) TRY(timed_launch(P->ctx->stream, "tail", bytes, [&] { return launch_tail(pol, fw, nullptr, &ta, 1, L, P->ctx->stream); }));
+    if (!dry) {
+        if (cs_log) TRY(timed_launch(P->ctx->stream, "tail_cluster", bytes, [&] { return launch_tail_cluster(pol, fw, ta, cs_log, P->ctx->stream); }));
+        else TRY(timed_launch(P->ctx->stream, "tail", bytes, [&] { return launch_tail(pol, fw, nullptr, &ta, 1, L, P->ctx->stream); }));
+    }
     if (folds)
         for (int i = 0; i < nt; i++) {
             Table& T = P->t[i];
@@ -1247,6 +1273,7 @@ int effsc_ctx_create(int device, effsc_ctx** out) {
     if (e != cudaSuccess) { delete c; return fail(EFFSC_CUDA_ERROR, "cudaStreamCreate: %s", cudaGetErrorString(e)); }
     c->stream = c->own;
     kernels_init(device);
+    tail_cluster_max();   // probe the cluster size once, outside any stream capture
     cudaMemPool_t pool;
     if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
         uint64_t thr = UINT64_MAX;
@@ -1682,6 +1709,11 @@ int effsc_prove(effsc_prover* P, size_t num_rounds, effsc_transcript* T, const u
             tx.chal_next = nullptr;
             if (tail_ok(P, r, num_rounds, ch)) {
                 TRY(do_tail(P, r, num_rounds, ch, tx, dry));
+                break;
+            }
+            u32 cs_log = 0;
+            if (cluster_tail_ok(P, r, num_rounds, ch, &cs_log)) {
+                TRY(do_tail(P, r, num_rounds, ch, tx, dry, cs_log));
                 break;
             }
             TRY(do_round(P, ch, tx, dry));
