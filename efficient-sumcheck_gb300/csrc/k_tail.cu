@@ -377,8 +377,8 @@ u32 tail_cluster_max(void) {
     if (v >= 0) return (u32)v;
     v = 0;
     for (u32 cs : {16u, 8u}) {
-        cudaFuncSetAttribute(k_tail_cluster<POL_IP, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TAIL_SMEM_CAP);
-        if (cs > 8 && cudaFuncSetAttribute(k_tail_cluster<POL_IP, 3>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess) {
+        cudaFuncSetAttribute(k_tail_cluster<POL_ML, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TAIL_SMEM_CAP);
+        if (cs > 8 && cudaFuncSetAttribute(k_tail_cluster<POL_ML, 3>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess) {
             cudaGetLastError();
             continue;
         }
@@ -395,7 +395,7 @@ u32 tail_cluster_max(void) {
         cfg.attrs = attr;
         cfg.numAttrs = 1;
         int n = 0;
-        if (cudaOccupancyMaxActiveClusters(&n, k_tail_cluster<POL_IP, 3>, &cfg) == cudaSuccess && n > 0) { v = (int)cs; break; }
+        if (cudaOccupancyMaxActiveClusters(&n, k_tail_cluster<POL_ML, 3>, &cfg) == cudaSuccess && n > 0) { v = (int)cs; break; }
         cudaGetLastError();
     }
     cached.store(v);
@@ -403,11 +403,10 @@ u32 tail_cluster_max(void) {
 }
 
 bool launch_tail_cluster(int pol, int fw, const TailArgs& a, u32 cs_log, cudaStream_t s) {
+    // Multilinear only (InnerProduct keeps its multi-block rounds at these sizes)
     switch (pol * 4 + fw) {
     case POL_ML * 4 + 1: return tail_cluster_inst<POL_ML, 1>(a, cs_log, s);
     case POL_ML * 4 + 3: return tail_cluster_inst<POL_ML, 3>(a, cs_log, s);
-    case POL_IP * 4 + 1: return tail_cluster_inst<POL_IP, 1>(a, cs_log, s);
-    case POL_IP * 4 + 3: return tail_cluster_inst<POL_IP, 3>(a, cs_log, s);
     default: return false;
     }
 }

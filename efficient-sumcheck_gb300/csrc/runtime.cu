@@ -329,8 +329,14 @@ int sem_of(const effsc_prover* p) {
 }
 size_t next_pow2(size_t n) { size_t r = 1; while (r < n) r <<= 1; return r; }
 bool is_pow2(size_t n) { return n && !(n & (n - 1)); }
-int grid_for(u64 work) {
-    u64 g = (work + KERNEL_TPB - 1) / KERNEL_TPB;
+// Blocks for `work` items, at least `per_thread` items per thread and at
+// most max_grid().  The cheap Multilinear rounds take four per thread (fewer
+// blocks: fewer grid-ticket atomics and partials for the last block to sum,
+// which dominate their mid-size rounds); the other provers keep one, their
+// mid-size rounds want every thread (measured).
+bool cheap_pol(int pol) { return pol == POL_ML; }
+int grid_for(u64 work, u64 per_thread = 1) {
+    u64 g = (work + per_thread * KERNEL_TPB - 1) / (per_thread * KERNEL_TPB);
     if (g < 1) g = 1;
     u64 mg = (u64)max_grid();
     return (int)(g < mg ? g : mg);
@@ -509,7 +515,7 @@ int round_std(effsc_prover* P, const Chal& ch, const TxIO& tx, bool dry) {
                 int g = std::min<int>((int)ntiles, (max_grid() / 8) * fused_tma_blocks_per_sm());
                 if (!dry) TRY(timed_launch(P->ctx->stream, nm, bytes, [&] { return launch_fused_tma(pol, sem, mask, ech, a, ntiles, g, P->ctx->stream); }));
             } else {
-                if (!dry) TRY(timed_launch(P->ctx->stream, nm, bytes, [&] { return launch_fused(pol, sem, mask, ech, a, grid_for(L / 4), P->ctx->stream); }));
+                if (!dry) TRY(timed_launch(P->ctx->stream, nm, bytes, [&] { return launch_fused(pol, sem, mask, ech, a, grid_for(L / 4, cheap_pol(pol) ? 4 : 1), P->ctx->stream); }));
             }
             for (int i = 0; i < nt; i++) {
                 Table& T = P->t[i];
@@ -532,7 +538,7 @@ int round_std(effsc_prover* P, const Chal& ch, const TxIO& tx, bool dry) {
     u64 work = sem == SEM_MSB_PAD ? (L > 1 ? next_pow2(L) / 2 : 1) : sem == SEM_MSB_FLOOR ? L / 2 : (L + 1) / 2;
     uint64_t bytes = 0;
     for (int i = 0; i < nt; i++) bytes += L * wbytes(P->t[i].ext);
-    if (!dry) TRY(timed_launch(P->ctx->stream, "evaluate", bytes, [&] { return launch_eval(pol, sem, mask_of(P, idx, nt), a, grid_for(work), P->ctx->stream); }));
+    if (!dry) TRY(timed_launch(P->ctx->stream, "evaluate", bytes, [&] { return launch_eval(pol, sem, mask_of(P, idx, nt), a, grid_for(work, cheap_pol(pol) ? 4 : 1), P->ctx->stream); }));
     return EFFSC_OK;
 }
 
@@ -559,7 +565,9 @@ bool tail_ok(const effsc_prover* P, size_t r, size_t num_rounds, const Chal& ch)
 // capacity, entered mid-proof (a challenge to fold with), with at least
 // log2(CS) + 1 rounds left; *cs_log = log2(CS), CS = L / capacity.
 bool cluster_tail_ok(const effsc_prover* P, size_t r, size_t num_rounds, const Chal& ch, u32* cs_log) {
-    if ((P->kind != EFFSC_ML && P->kind != EFFSC_IP) || P->order != EFFSC_MSB || !P->tail_len) return false;
+    // Multilinear only: for InnerProduct the cluster rounds cost what the
+    // multi-block rounds they replace cost (measured), so it keeps those
+    if (P->kind != EFFSC_ML || P->order != EFFSC_MSB || !P->tail_len) return false;
     if (r >= num_rounds || !ch.has || !ch.dev) return false;
     const size_t L = P->t[0].len;
     for (int i = 1; i < P->ntab; i++)

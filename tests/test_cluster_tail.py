@@ -1,8 +1,9 @@
 """The cluster tail (tables of up to 16 times one block's capacity held in the
-distributed shared memory of a thread-block cluster, then handed to one CTA):
-proofs, hooks and post-state tables against the oracle at sizes where it
-runs, for Multilinear and InnerProduct over Fp and Fp3, and the same proof
-with the tail kernels switched off."""
+distributed shared memory of a thread-block cluster, then handed to one CTA;
+Multilinear proofs): proofs, hooks and post-state tables against the oracle
+at sizes where it runs, over Fp and Fp3, and the same proof with the tail
+kernels switched off.  InnerProduct proofs of the same sizes (multi-block
+rounds there, then the one-block tail) are checked alongside."""
 import os
 
 import numpy as np
