@@ -16,10 +16,14 @@
 
 namespace effsc {
 
-template <bool EA, bool EW>
-__device__ __forceinline__ void gkr_point(ProdAcc<EA, EW>& acc, const F3& a, const F3& m, const F3& wb, const F3& wc) {
-    acc.mac(a, f3_add<EW>(wb, wc));
-    acc.mac(m, f3_mul<EW, EW>(wb, wc));
+// W_b and W_c keep their own representation: W_c stays in the base field
+// through the first k rounds (it is folded only in the last k) and W_b is
+// base in round 0, so the W sum and product are mixed or base there.
+template <bool EA, bool EWB, bool EWC>
+__device__ __forceinline__ void gkr_point(ProdAcc<EA, EWB || EWC>& acc, const F3& a, const F3& m, const F3& wb,
+                                          const F3& wc) {
+    acc.mac(a, f3_add_mixed<EWB || EWC, EWB && EWC>(EWB || !EWC ? wb : wc, EWB || !EWC ? wc : wb));
+    acc.mac(m, f3_mul<EWB, EWC>(wb, wc));
 }
 
 template <bool E>
@@ -27,9 +31,16 @@ __device__ __forceinline__ F3 twice_minus(const F3& hi, const F3& lo) {
     return f3_sub<E>(f3_add<E>(hi, hi), lo);
 }
 
-template <bool FUSED, bool EAI, bool EW, bool ECH>
-__global__ void __launch_bounds__(TPB, 2) k_gkr(RoundArgs a) {
+// Blocks per SM the register budget is sized for: Fp3 gate tables with an
+// Fp3 witness keep three Fp3 x Fp3 accumulators (75 registers) live, which
+// fit without spills only at one block per SM.
+template <bool FUSED, bool EAI, bool EWB, bool EWC, bool ECH>
+constexpr int gkr_min_blocks() { return ((FUSED ? (EAI || ECH) : EAI) && (EWB || EWC)) ? 1 : 2; }
+
+template <bool FUSED, bool EAI, bool EWB, bool EWC, bool ECH>
+__global__ void __launch_bounds__(TPB, (gkr_min_blocks<FUSED, EAI, EWB, EWC, ECH>())) k_gkr(RoundArgs a) {
     constexpr bool EA = FUSED ? (EAI || ECH) : EAI;   // add / mult after the fold
+    constexpr bool EW = EWB || EWC;
     ProdAcc<EA, EW> q0, q1, q2;
     q0.init();
     q1.init();
@@ -44,10 +55,10 @@ __global__ void __launch_bounds__(TPB, 2) k_gkr(RoundArgs a) {
         if (tid == 0) {
             const F3 al = ld<EA>(FUSED ? (const u64* const*)a.t[0].out : a.t[0].in, 0);
             const F3 ml = ld<EA>(FUSED ? (const u64* const*)a.t[1].out : a.t[1].in, 0);
-            const F3 wb = ld<EW>(a.t[2].in, 0), wc = ld<EW>(a.t[3].in, 0);
-            gkr_point(q0, al, ml, wb, wc);
+            const F3 wb = ld<EWB>(a.t[2].in, 0), wc = ld<EWC>(a.t[3].in, 0);
+            gkr_point<EA, EWB, EWC>(q0, al, ml, wb, wc);
             // q(2) = -q(0) so that the wire's q(inf) is 0 (src/provers/gkr.rs:119-127)
-            gkr_point(q2, f3_sub<EA>(f3_zero(), al), f3_sub<EA>(f3_zero(), ml), wb, wc);
+            gkr_point<EA, EWB, EWC>(q2, f3_sub<EA>(f3_zero(), al), f3_sub<EA>(f3_zero(), ml), wb, wc);
         }
     } else {
         F3 rr;
@@ -76,25 +87,34 @@ __global__ void __launch_bounds__(TPB, 2) k_gkr(RoundArgs a) {
                 al = ld<EA>(a.t[0].in, i); ah = ld<EA>(a.t[0].in, i + H);
                 ml = ld<EA>(a.t[1].in, i); mh = ld<EA>(a.t[1].in, i + H);
             }
-            const F3 wbl = ld<EW>(a.t[2].in, i >> kc), wbh = ld<EW>(a.t[2].in, (i + H) >> kc);
-            const F3 wcl = ld<EW>(a.t[3].in, i & cm), wch = ld<EW>(a.t[3].in, (i + H) & cm);
-            gkr_point(q0, al, ml, wbl, wcl);
-            gkr_point(q1, ah, mh, wbh, wch);
-            gkr_point(q2, twice_minus<EA>(ah, al), twice_minus<EA>(mh, ml), twice_minus<EW>(wbh, wbl),
-                      twice_minus<EW>(wch, wcl));
+            const F3 wbl = ld<EWB>(a.t[2].in, i >> kc), wbh = ld<EWB>(a.t[2].in, (i + H) >> kc);
+            const F3 wcl = ld<EWC>(a.t[3].in, i & cm), wch = ld<EWC>(a.t[3].in, (i + H) & cm);
+            gkr_point<EA, EWB, EWC>(q0, al, ml, wbl, wcl);
+            gkr_point<EA, EWB, EWC>(q1, ah, mh, wbh, wch);
+            gkr_point<EA, EWB, EWC>(q2, twice_minus<EA>(ah, al), twice_minus<EA>(mh, ml), twice_minus<EWB>(wbh, wbl),
+                                    twice_minus<EWC>(wch, wcl));
         }
     }
     F3 raw[3] = {q0.result(), q1.result(), q2.result()};
     reduce_and_finalize<3>(raw, a, POL_GKR);
 }
 
-#define GKR(F, EA, EW, ECH) \
-    case ((F) * 8 + (EA) * 4 + (EW) * 2 + (ECH)): k_gkr<F, EA, EW, ECH><<<grid, TPB, 0, s>>>(a); return true;
+#define GKR(F, EA, EWB, EWC, ECH) \
+    case ((F) * 16 + (EA) * 8 + (EWB) * 4 + (EWC) * 2 + (ECH)): k_gkr<F, EA, EWB, EWC, ECH><<<grid, TPB, 0, s>>>(a); return true;
 
-bool launch_gkr(bool fused, bool ea, bool ew, bool ech, const RoundArgs& a, int grid, cudaStream_t s) {
-    switch ((fused ? 8 : 0) + (ea ? 4 : 0) + (ew ? 2 : 0) + (ech ? 1 : 0)) {
-        GKR(false, false, false, false) GKR(false, true, true, false) GKR(false, false, true, false)
-        GKR(true, false, false, false) GKR(true, false, true, true) GKR(true, true, true, true)
+bool launch_gkr(bool fused, bool ea, bool ewb, bool ewc, bool ech, const RoundArgs& a, int grid, cudaStream_t s) {
+    switch ((fused ? 16 : 0) + (ea ? 8 : 0) + (ewb ? 4 : 0) + (ewc ? 2 : 0) + (ech ? 1 : 0)) {
+        // evaluate only (round 0, tables of length <= 2)
+        GKR(false, false, false, false, false) GKR(false, false, true, false, false)
+        GKR(false, false, false, true, false) GKR(false, false, true, true, false)
+        GKR(false, true, false, false, false) GKR(false, true, true, false, false)
+        GKR(false, true, false, true, false) GKR(false, true, true, true, false)
+        // fused fold + evaluate: base challenges, or Fp3 challenges
+        GKR(true, false, false, false, false)
+        GKR(true, false, false, false, true) GKR(true, false, true, false, true)
+        GKR(true, false, false, true, true) GKR(true, false, true, true, true)
+        GKR(true, true, false, false, true) GKR(true, true, true, false, true)
+        GKR(true, true, false, true, true) GKR(true, true, true, true, true)
         default: return false;
     }
 }

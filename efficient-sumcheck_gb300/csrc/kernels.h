@@ -145,7 +145,7 @@ int fused_tma_blocks_per_sm(void);
 // variables) and 2^(k - bound c variables) entries).  fused: fold add and
 // mult with the challenge (L a power of two >= 4) and evaluate the folded
 // tables; otherwise evaluate the current ones.
-bool launch_gkr(bool fused, bool ea, bool ew, bool ech, const RoundArgs& a, int grid, cudaStream_t s);
+bool launch_gkr(bool fused, bool ea, bool ewb, bool ewc, bool ech, const RoundArgs& a, int grid, cudaStream_t s);
 // InnerProduct (MSB or LSB) over Fp3 challenges, base tables of length L = 2^n >= 8:
 // rounds 0 and 1 from one read of the tables (launch_ip01), then round 2's
 // fold-twice-and-evaluate from a second read (launch_ip2x).

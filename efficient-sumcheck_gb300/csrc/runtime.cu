@@ -897,12 +897,12 @@ int round_gkr(effsc_prover* P, const Chal& ch, const TxIO& tx, bool dry) {
             TRY(out_buffer(P, P->t[i], P->t[i].ext || ech, L / 2, true, &bi[i]));
             set_out(a, i, P->t[i].bufs[bi[i]]);
         }
-    const bool ew = WB.ext;
+    const bool ewb = WB.ext, ewc = WC.ext;
     const u64 Ln = fused ? L / 2 : L;
     uint64_t bytes = 2 * (L * wbytes(ea) + (fused ? (L / 2) * wbytes(ea || ech) : 0)) +
-                     (WB.len + WC.len) * wbytes(ew);
+                     WB.len * wbytes(ewb) + WC.len * wbytes(ewc);
     if (!dry) TRY(timed_launch(P->ctx->stream, fused ? "gkr_fused_round" : "gkr_evaluate", bytes, [&] {
-        return launch_gkr(fused, ea, ew, fused && (ech || ea), a, grid_for(Ln > 1 ? Ln / 2 : 1), P->ctx->stream);
+        return launch_gkr(fused, ea, ewb, ewc, fused && (ech || ea), a, grid_for(Ln > 1 ? Ln / 2 : 1), P->ctx->stream);
     }));
     if (fused)
         for (int i = 0; i < 2; i++) {
@@ -1100,9 +1100,10 @@ int promote(effsc_prover* P, Table& T) {
 // (eq(r, x) * f * g with base f, g).
 int normalize_masks(effsc_prover* P) {
     if (P->kind == EFFSC_GKR) {
-        // the witness tables are Fp3 whenever the challenges are; add and
-        // mult share one representation
-        if (P->field == EFFSC_FP3 || P->t[2].ext) { TRY(promote(P, P->t[2])); TRY(promote(P, P->t[3])); }
+        // add and mult share one representation, and so do the two witness
+        // tables at the start; each witness table turns Fp3 when its own
+        // fold with an Fp3 challenge does (W_c only in the last k rounds)
+        if (P->t[2].ext != P->t[3].ext) { TRY(promote(P, P->t[2])); TRY(promote(P, P->t[3])); }
         if (P->t[0].ext != P->t[1].ext) { TRY(promote(P, P->t[0])); TRY(promote(P, P->t[1])); }
         return EFFSC_OK;
     }
