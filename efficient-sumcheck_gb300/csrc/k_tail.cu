@@ -372,9 +372,12 @@ static bool tail_cluster_inst(const TailArgs& a, u32 cs_log, cudaStream_t s) {
 // Largest cluster the device runs for the cluster tail (8 or 16 CTAs of
 // TAIL_SMEM_CAP bytes each; 0 when none fits).
 u32 tail_cluster_max(void) {
-    static std::atomic<int> cached{-1};
-    int v = cached.load();
-    if (v >= 0) return (u32)v;
+    static std::atomic<int> cached[64];   // per device: 0 unknown, else size + 1
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+    std::atomic<int>& slot = cached[dev & 63];
+    int v = slot.load();
+    if (v > 0) return (u32)(v - 1);
     v = 0;
     for (u32 cs : {16u, 8u}) {
         cudaFuncSetAttribute(k_tail_cluster<POL_ML, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TAIL_SMEM_CAP);
@@ -398,7 +401,7 @@ u32 tail_cluster_max(void) {
         if (cudaOccupancyMaxActiveClusters(&n, k_tail_cluster<POL_ML, 3>, &cfg) == cudaSuccess && n > 0) { v = (int)cs; break; }
         cudaGetLastError();
     }
-    cached.store(v);
+    slot.store(v + 1);
     return (u32)v;
 }
 

@@ -168,9 +168,11 @@ int effsc_prover_table_len(const effsc_prover* p, int table, size_t* out_len);
 int effsc_prover_read_table(effsc_prover* p, int table, uint64_t* out);
 /* effsc_prove only (no reference counterpart; a tuning knob): once an MSB
  * Multilinear / InnerProduct prover's power-of-two tables are at most
- * max_len long, the remaining rounds run in one thread block with the tables
- * in shared memory (one launch instead of one per round).  Default SIZE_MAX:
- * as long as shared memory allows; 0 disables.  Proofs are identical. */
+ * max_len long, the remaining rounds run in one launch with the tables in
+ * shared memory: one thread block, or (Multilinear, tables up to 16 times
+ * one block's capacity, entered mid-proof) a thread-block cluster that hands
+ * over to one block.  Default SIZE_MAX: as long as shared memory allows; 0
+ * disables.  Proofs are identical. */
 int effsc_prover_set_tail(effsc_prover* p, size_t max_len);
 /* effsc_prove only (no reference counterpart; a tuning knob): for an MSB
  * InnerProduct prover over Fp3 challenges with power-of-two base tables,

@@ -133,3 +133,26 @@ def test_trace_poisson(E):
     assert (lat > 0).all() and makespan >= arrivals[-1]
     for i, (kind, n, seeds) in enumerate(reqs):
         assert same(proofs[i], solo(E, kind, n, seeds, 3, i)), i
+
+
+def test_two_lanes_mix(E):
+    """Requests of 2^22 entries and more go to the second lane (own stream,
+    queue and steps); a mix of both lanes, with small requests finishing in
+    tail launches, gives every request the proof it gets alone."""
+    rng = random.Random(77)
+    reqs = []
+    for i in range(18):
+        big = i % 6 == 0
+        n = rng.randint(22, 23) if big else rng.randint(2, 16)
+        kind = "ml" if rng.random() < 0.3 else "ip"
+        reqs.append((kind, n, [0x7A7E0000 + 2 * i, 0x7A7E0001 + 2 * i]))
+    srv = E.Server(hbm_budget=1 << 36, max_active=6)
+    ids = {}
+    for i, (kind, n, seeds) in enumerate(reqs):
+        ids[srv.submit(E.IP if kind == "ip" else E.ML, n, E.Transcript.keccak(3, label(i)), seeds=seeds)] = i
+    out = srv.drain()
+    assert len(out) == len(reqs)
+    for rid, (proof, q, lat) in out.items():
+        i = ids[rid]
+        kind, n, seeds = reqs[i]
+        assert same(proof, solo(E, kind, n, seeds, 3, i)), i
