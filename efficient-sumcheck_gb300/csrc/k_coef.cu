@@ -15,6 +15,8 @@ bool launch_eval_coef(int pol, int sem, u32 mask, const RoundArgs& a, int grid, 
         EVAL(POL_C2, SEM_LSB, 0) EVAL(POL_C2, SEM_LSB, 3)
         EVAL(POL_C3, SEM_MSB_FLOOR, 0) EVAL(POL_C3, SEM_MSB_FLOOR, 1) EVAL(POL_C3, SEM_MSB_FLOOR, 7)
         EVAL(POL_C3, SEM_LSB, 0) EVAL(POL_C3, SEM_LSB, 1) EVAL(POL_C3, SEM_LSB, 7)
+        EVAL(POL_C3W, SEM_MSB_FLOOR, 0) EVAL(POL_C3W, SEM_MSB_FLOOR, 1) EVAL(POL_C3W, SEM_MSB_FLOOR, 7)
+        EVAL(POL_C3W, SEM_LSB, 0) EVAL(POL_C3W, SEM_LSB, 1) EVAL(POL_C3W, SEM_LSB, 7)
         default: return false;
     }
 }
@@ -34,6 +36,10 @@ bool launch_fused_coef(int pol, int sem, u32 mask, bool ech, const RoundArgs& a,
         FUSED_WIDE(POL_C3, SEM_MSB_FLOOR, 1, true) FUSED_WIDE(POL_C3, SEM_MSB_FLOOR, 7, true)
         FUSED_WIDE(POL_C3, SEM_LSB, 0, false) FUSED_WIDE(POL_C3, SEM_LSB, 0, true)
         FUSED_WIDE(POL_C3, SEM_LSB, 1, true) FUSED_WIDE(POL_C3, SEM_LSB, 7, true)
+        FUSED_WIDE(POL_C3W, SEM_MSB_FLOOR, 0, false) FUSED_WIDE(POL_C3W, SEM_MSB_FLOOR, 0, true)
+        FUSED_WIDE(POL_C3W, SEM_MSB_FLOOR, 1, true) FUSED_WIDE(POL_C3W, SEM_MSB_FLOOR, 7, true)
+        FUSED_WIDE(POL_C3W, SEM_LSB, 0, false) FUSED_WIDE(POL_C3W, SEM_LSB, 0, true)
+        FUSED_WIDE(POL_C3W, SEM_LSB, 1, true) FUSED_WIDE(POL_C3W, SEM_LSB, 7, true)
         default: return false;
     }
 }

@@ -29,14 +29,14 @@ int max_grid(void) { return (g_sms > 0 ? g_sms : 1) * 8; }
 int pol_ntables(int pol) {
     switch (pol) {
     case POL_ML: case POL_C1: return 1;
-    case POL_C3: case POL_EQFL: return 3;
+    case POL_C3: case POL_C3W: case POL_EQFL: return 3;
     case POL_GKR: return 4;
     default: return 2;
     }
 }
 int pol_nraw(int pol) {
     switch (pol) {
-    case POL_C2: case POL_GKR: return 3;
+    case POL_C2: case POL_GKR: case POL_C3W: return 3;
     case POL_C3: return 4;
     default: return 2;
     }
@@ -44,17 +44,17 @@ int pol_nraw(int pol) {
 int pol_nwire(int pol) {
     switch (pol) {
     case POL_ML: case POL_C1: return 1;
-    case POL_C3: return 3;
+    case POL_C3: case POL_C3W: return 3;
     default: return 2;
     }
 }
 
 bool launch_eval(int pol, int sem, u32 mask, const RoundArgs& a, int grid, cudaStream_t s) {
-    if (pol == POL_C1 || pol == POL_C2 || pol == POL_C3) return launch_eval_coef(pol, sem, mask, a, grid, s);
+    if (pol == POL_C1 || pol == POL_C2 || pol == POL_C3 || pol == POL_C3W) return launch_eval_coef(pol, sem, mask, a, grid, s);
     return launch_eval_mlip(pol, sem, mask, a, grid, s);
 }
 bool launch_fused(int pol, int sem, u32 mask, bool ech, const RoundArgs& a, int grid, cudaStream_t s) {
-    if (pol == POL_C1 || pol == POL_C2 || pol == POL_C3) return launch_fused_coef(pol, sem, mask, ech, a, grid, s);
+    if (pol == POL_C1 || pol == POL_C2 || pol == POL_C3 || pol == POL_C3W) return launch_fused_coef(pol, sem, mask, ech, a, grid, s);
     return launch_fused_mlip(pol, sem, mask, ech, a, grid, s);
 }
 

@@ -29,11 +29,13 @@ enum Sem { SEM_MSB_PAD = 0, SEM_MSB_FLOOR = 1, SEM_LSB = 2 };
 //  POL_EQFR: POL_IP on (eq_r, p), times the scalar eq_l[0]  (2 tables)
 //  POL_IP01: InnerProduct rounds 0 and 1 from one pass over the base tables
 //            (eight base-field sums, two transcript steps)
+//  POL_C3W : POL_C3 without h(1) (the wire needs h(0), h(inf), h(2); the
+//            legacy (c0, c1) pair is not produced): the device protocol
 //  POL_GKR : GkrProver, q(0), q(1), q(2) of add (W_b + W_c) + mult W_b W_c;
 //            the wire is [q(0), (q(0) + q(2) - 2 q(1)) / 2]
 enum Pol {
     POL_ML = 0, POL_IP = 1, POL_C1 = 2, POL_C2 = 3, POL_C3 = 4, POL_EQFR = 5, POL_EQFL = 6, POL_IP01 = 7,
-    POL_GKR = 8
+    POL_GKR = 8, POL_C3W = 9
 };
 
 struct TabIO {

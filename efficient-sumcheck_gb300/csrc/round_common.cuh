@@ -161,6 +161,30 @@ struct Policy<POL_C3, M> {
     }
 };
 
+// The degree-3 evaluator for the device protocol: h(0), h(2) and h(inf) only
+// (the wire), one accumulator and one product fewer per pair than POL_C3.
+template <u32 M>
+struct Policy<POL_C3W, M> {
+    static constexpr int NT = 3, NRAW = 3;
+    static constexpr bool LSB_REMAINDER = false;
+    static constexpr bool E0 = ext_of<M>(0), E1 = ext_of<M>(1), E2 = ext_of<M>(2);
+    static constexpr bool EU = E0 || E1;
+    ProdAcc<EU, E2> h0, h2, hi;
+    __device__ __forceinline__ void init() { h0.init(); h2.init(); hi.init(); }
+    __device__ __forceinline__ void point(ProdAcc<EU, E2>& acc, const F3& a, const F3& b, const F3& c) {
+        acc.mac(f3_mul<E0, E1>(a, b), c);
+    }
+    __device__ __forceinline__ void pair(const F3* lo, const F3* hi_) {
+        const F3 da = f3_sub<E0>(hi_[0], lo[0]), db = f3_sub<E1>(hi_[1], lo[1]), dc = f3_sub<E2>(hi_[2], lo[2]);
+        point(h0, lo[0], lo[1], lo[2]);
+        point(h2, f3_add<E0>(hi_[0], da), f3_add<E1>(hi_[1], db), f3_add<E2>(hi_[2], dc));
+        point(hi, da, db, dc);
+    }
+    __device__ __forceinline__ void tail(const F3*) {}
+    __device__ __forceinline__ void single(const F3*) {}
+    __device__ __forceinline__ void result(F3* o) const { o[0] = h0.result(); o[1] = h2.result(); o[2] = hi.result(); }
+};
+
 // ---------------------------------------------------------------------------
 // Finalisation by the last block.
 // ---------------------------------------------------------------------------
@@ -175,7 +199,7 @@ __device__ __forceinline__ F3 ld_scalar(const u64* const* p) {
 __device__ __forceinline__ int pol_nwire_dev(int pol) {
     switch (pol) {
     case POL_ML: case POL_C1: return 1;
-    case POL_C3: return 3;
+    case POL_C3: case POL_C3W: return 3;
     default: return 2;
     }
 }
@@ -269,6 +293,11 @@ static __device__ __noinline__ void finalize_warp(int pol, const u64* raw, const
             r[1] = f3_sub<true>(A, c2);
             break;
         }
+        case POL_C3W:
+            // r = h(0), h(2), h(inf): wire [h(0), h(inf), h(2)]; no aux pair
+            w[0] = r[0]; w[1] = r[2]; w[2] = r[1];
+            r[1] = f3_zero();
+            break;
         case POL_GKR: {
             // src/provers/gkr.rs:185-189: q(inf) = (q(0) + q(2) - 2 q(1)) / 2
             const u64 inv2 = 0x7FFFFFFF80000001ULL;   // (p + 1) / 2

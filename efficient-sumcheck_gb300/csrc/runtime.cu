@@ -475,7 +475,9 @@ u32 mask_of(const effsc_prover* P, const int* idx, int n) {
 // inner_product.rs:61-113, inner_product_lsb.rs:156-164,
 // coefficient.rs:272-294, coefficient_lsb.rs:180-203).
 int round_std(effsc_prover* P, const Chal& ch, const TxIO& tx, bool dry) {
-    const int pol = pol_of(P), sem = sem_of(P), nt = P->ntab;
+    // the device protocol needs only the wire, not the legacy pair: the
+    // degree-3 evaluator then skips h(1)
+    const int pol = (pol_of(P) == POL_C3 && tx.tx) ? POL_C3W : pol_of(P), sem = sem_of(P), nt = P->ntab;
     int idx[3] = {0, 1, 2};
     size_t L = P->t[0].len;
     RoundArgs a = base_args(P);
