@@ -120,6 +120,7 @@ extern "C" int effsc_verify_batch(effsc_ctx* ctx, int field, size_t n, const uin
         return effsc_set_error(EFFSC_INVALID_ARG, "NULL argument");
     if (field != EFFSC_FP && field != EFFSC_FP3) return effsc_set_error(EFFSC_INVALID_ARG, "bad field");
     if (degree < 0 || degree > 3) return effsc_set_error(EFFSC_UNSUPPORTED, "device verification handles degree 0..3");
+    if (hook_len >= (1ull << 32) || n >= (1ull << 32)) return effsc_set_error(EFFSC_INVALID_ARG, "hook or batch too large");
     if (!n) return EFFSC_OK;
     const int dev = effsc_internal_ctx_device(ctx);
     cudaStream_t s = effsc_internal_ctx_stream(ctx);
