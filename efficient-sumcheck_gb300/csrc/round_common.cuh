@@ -251,10 +251,45 @@ static __device__ __noinline__ void finalize_ip01(const u64* raw, const RoundArg
     if (lane < 6) a.tx.proof_chal[lane] = s_c[lane / 3][lane % 3];
 }
 
+// POL_ML01: raw = the quarter sums (S0, S1, S2) of a Multilinear base
+// table.  Round 0's wire is S0 + S1; round 1's is S0 + r0 (S2 - S0).  Both
+// transcript steps (send, hook, challenge) run here.
+static __device__ __noinline__ void finalize_ml01(const u64* raw, const RoundArgs& a) {
+    __shared__ u64 s_w[2][3];
+    __shared__ u64 s_c[2][3];
+    __shared__ __align__(8) uint8_t s_scr[64];
+    const int lane = threadIdx.x & 31;
+    if (lane == 0) { s_w[0][0] = gl_add(raw[0], raw[1]); s_w[0][1] = 0; s_w[0][2] = 0; }
+    __syncwarp();
+    DevTranscript* T = (DevTranscript*)a.tx.tx;
+    WarpTx w = tx_load(T, lane);
+    for (int rd = 0; rd < 2; rd++) {
+        if (rd == 1 && lane == 0) {
+            const F3 r = f3_make(s_c[0][0], s_c[0][1], s_c[0][2]);
+            const F3 v = f3_add<true>(f3_make(raw[0], 0, 0), f3_mul<true, true>(f3_make(gl_sub(raw[2], raw[0]), 0, 0), r));
+            s_w[1][0] = v.c0; s_w[1][1] = v.c1; s_w[1][2] = v.c2;
+        }
+        __syncwarp();
+        tx_send_elems(w, lane, s_w[rd], 1);
+        if (a.tx.hook_len) {
+            const uint8_t* hk = a.tx.hook;
+            tx_absorb(w, lane, a.tx.hook_len, [&](u32 k) -> uint8_t { return hk[k]; });
+        }
+        tx_challenge(w, lane, s_c[rd], s_scr);
+    }
+    tx_store(T, w, lane);
+    if (lane < 6) a.tx.proof_wire[lane] = s_w[lane / 3][lane % 3];
+    if (lane < 6) a.tx.proof_chal[lane] = s_c[lane / 3][lane % 3];
+}
+
 // raw: NRAW Fp3 values in shared memory (3 words each).  Run by warp 0.
 static __device__ __noinline__ void finalize_warp(int pol, const u64* raw, const RoundArgs& a) {
     if (pol == POL_IP01) {
         finalize_ip01(raw, a);
+        return;
+    }
+    if (pol == POL_ML01) {
+        finalize_ml01(raw, a);
         return;
     }
     __shared__ u64 s_wire[9];

@@ -110,3 +110,54 @@ def test_eq_factored_left_phase_from_inner_sums(E, v, extra, field):
     rp, ch, fv = O.sumcheck(O.Prover.eq_factored(field, w3, p), rounds, O.Transcript(field, label=b"eqf"), hook=hook)
     assert np.array_equal(np.asarray(x.round_polys).reshape(rounds, 2, field), rp[:, :, :field])
     assert np.array_equal(np.asarray(x.final_value).reshape(field), fv[:field])
+
+
+# ---- Multilinear: rounds 0-1 from quarter sums, round 2 with a double fold ----
+@pytest.mark.parametrize("n", [3, 4, 5, 7, 10, 13, 16])
+@pytest.mark.parametrize("field", [1, 3])
+@pytest.mark.parametrize("hook", [b"", bytes(range(32)), b"\x05\x06\x07"])
+def test_ml_full_runs(E, n, field, hook):
+    v = tables(n, 300 + n + field + len(hook))[0]
+    p = E.MultilinearProver(v, field=field)
+    p.set_tail(0)
+    q = E.MultilinearProver(v, field=field)
+    q.set_tail(0)
+    q.set_first_rounds(False)
+    for use_graph in (True, False):
+        p.reset()
+        q.reset()
+        x = p.prove(n, E.Transcript.keccak(field, b"mlfr"), hook=hook, use_graph=use_graph)
+        y = q.prove(n, E.Transcript.keccak(field, b"mlfr"), hook=hook, use_graph=use_graph)
+        assert np.array_equal(x.round_polys, y.round_polys)
+        assert np.array_equal(x.challenges, y.challenges)
+        assert np.array_equal(x.final_value, y.final_value)
+    rp, ch, fv = O.sumcheck(O.Prover(O.ML, O.MSB, field, [v]), n, O.Transcript(field, label=b"mlfr"), hook=hook)
+    assert np.array_equal(np.asarray(x.round_polys).reshape(n, 1, field), rp[:, :1, :field])
+    assert np.array_equal(np.asarray(x.challenges).reshape(n, field), ch[:, :field])
+    assert np.array_equal(np.asarray(x.final_value).reshape(field), fv[:field])
+
+
+@pytest.mark.parametrize("n", [18, 20])
+def test_ml_default_schedule(E, n):
+    """Two-pass start, multi-block rounds, cluster tail and one-block tail in
+    one proof, as the default schedule runs them."""
+    v = tables(n, 400 + n)[0]
+    pf = E.MultilinearProver(v, field=1).prove(n, E.Transcript.keccak(1, b"mlds"))
+    rp, ch, fv = O.sumcheck(O.Prover(O.ML, O.MSB, 1, [v]), n, O.Transcript(1, label=b"mlds"))
+    assert np.array_equal(np.asarray(pf.round_polys).reshape(n, 1, 1), rp[:, :1, :1])
+    assert np.array_equal(np.asarray(pf.final_value).reshape(1), fv[:1])
+
+
+@pytest.mark.parametrize("rounds", [3, 4, 6])
+@pytest.mark.parametrize("field", [1, 3])
+def test_ml_partial_post_state(E, rounds, field):
+    n = 9
+    v = tables(n, 500 + rounds + field)[0]
+    p = E.MultilinearProver(v, field=field)
+    p.set_tail(0)
+    pf = p.prove(rounds, E.Transcript.keccak(field, b"mlpart"))
+    orc = O.Prover(O.ML, O.MSB, field, [v])
+    rp, ch, fv = O.sumcheck(orc, rounds, O.Transcript(field, label=b"mlpart"))
+    assert np.array_equal(np.asarray(pf.round_polys).reshape(rounds, 1, field), rp[:, :1, :field])
+    got = np.asarray(p.table(0)).reshape(-1, field)
+    assert np.array_equal(got, orc.table(0)[:, :field])
