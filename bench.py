@@ -60,7 +60,7 @@ def parse():
                     help="serving leg: this many requests, 70%% IP / 30%% ML, num_vars uniform on 14..=26 (0 = skip)")
     ap.add_argument("--serve-slots", type=int, default=128)
     ap.add_argument("--serve-budget-gb", type=float, default=150.0)
-    ap.add_argument("--only", choices=["protogalaxy_fold"],
+    ap.add_argument("--only", choices=["protogalaxy_fold", "multilinear_n20", "gkr_k12"],
                     help="run one secondary workload alone and print its record (for profiling)")
     return ap.parse_args()
 
@@ -682,30 +682,7 @@ def run_configs(args, E, L, ctx, stream, rank):
     if check:
         from oracle import oracle as O
         O.set_threads(os.cpu_count() or 1)
-    # Multilinear MSB, Fp, num_vars = 20, all rounds
-    n = 20
-    v = E.gen_uniform(E.table_seed(0x3170_2026, 0), 1 << n, ctx=ctx)
-    ml = E.MultilinearProver(v, field=E.FP, ctx=ctx)
-    lab = b"effsc-gpu/ml/v1"
-
-    def ml_proof(use_graph=True):
-        ml.reset()
-        return ml.prove(n, E.Transcript.keccak(E.FP, lab), use_graph=use_graph)
-
-    ms, pf = time_proofs(torch, stream, ml_proof, 200)
-    by, _ = profile_bytes(E, L, lambda: ml_proof(False))
-    ok = None
-    if check:
-        rp, ch, fv = O.sumcheck(O.Prover(O.ML, O.MSB, 1, [v]), n, O.Transcript(1, label=lab))
-        ok = bool(np.array_equal(pf.round_polys.reshape(n, 1), rp[:, :, 0]) and
-                  np.array_equal(pf.final_value.reshape(1), fv[:1]))
-        assert ok, "Multilinear n=20 proof differs from the oracle"
-    res["multilinear_fp_n20"] = {
-        "workload": "MultilinearProver MSB over Fp, num_vars=20, seeded uniform table, Fp challenges, label %s, "
-                    "20 rounds + finalize; one CUDA graph per proof (L2-resident, latency-bound)" % lab.decode(),
-        "us_per_proof": ms * 1e3, "evals_per_s": (1 << n) / (ms * 1e-3), "algorithmic_bytes": by,
-        "hbm_gbs": by / (ms * 1e-3) / 1e9, "bit_exact_vs_oracle": ok}
-    del ml
+    res["multilinear_fp_n20"] = run_ml_n20(E, L, ctx, stream, check)
     # Coefficient (eq * f * g, degree 3) and EqFactored (p = f . g), num_vars = 24
     n, rounds = 24, 16
     hook = bytes(range(32))
@@ -753,33 +730,7 @@ def run_configs(args, E, L, ctx, stream, rank):
         "ms_per_proof": ms_e, "evals_per_s": (1 << n) / (ms_e * 1e-3), "algorithmic_bytes": by_e,
         "hbm_gbs": by_e / (ms_e * 1e-3) / 1e9, "bit_exact_vs_oracle": ok_e}
     del coef, eqf
-    # GkrProver, k = 12: add, mult of 2^24 base entries, w of 2^12, 24 rounds
-    k = 12
-    add = E.gen_uniform(E.table_seed(0x6C12_2026, 0), 1 << (2 * k), ctx=ctx)
-    mult = E.gen_uniform(E.table_seed(0x6C12_2026, 1), 1 << (2 * k), ctx=ctx)
-    wv = E.gen_uniform(E.table_seed(0x6C12_2026, 2), 1 << k, ctx=ctx)
-    gk = E.GkrProver(add, mult, wv, ctx=ctx)
-    lab_g = b"effsc-gpu/gkr/v1"
-
-    def gkr_proof(use_graph=True):
-        gk.reset()
-        return gk.prove(2 * k, E.Transcript.keccak(E.FP3, lab_g), use_graph=use_graph)
-
-    ms_g, pf_g = time_proofs(torch, stream, gkr_proof, 20)
-    by_g, _ = profile_bytes(E, L, lambda: gkr_proof(False))
-    ok_g = None
-    if check:
-        orc = O.Prover.gkr(3, add, mult, wv)
-        rp, ch, fv = O.sumcheck(orc, 2 * k, O.Transcript(3, label=lab_g))
-        ok_g = bool(np.array_equal(pf_g.round_polys, rp) and np.array_equal(pf_g.final_value, fv)
-                    and np.array_equal(gk.claimed_w_values(), orc.claimed_w_values()))
-        assert ok_g, "GkrProver k=12 proof differs from the oracle"
-    res["gkr_k12"] = {
-        "workload": "GkrProver (MSB), k=12: add, mult seeded uniform tables of 2^24 Goldilocks values, w of 2^12, "
-                    "Fp3 challenges, 24 rounds + finalize, label %s; witness kept as two 2^12 tables" % lab_g.decode(),
-        "ms_per_proof": ms_g, "evals_per_s": 2 * (1 << (2 * k)) / (ms_g * 1e-3), "algorithmic_bytes": by_g,
-        "hbm_gbs": by_g / (ms_g * 1e-3) / 1e9, "bit_exact_vs_oracle": ok_g}
-    del gk
+    res["gkr_k12"] = run_gkr_k12(E, L, ctx, stream, check)
     # InnerProduct LSB (pair-split), num_vars = 26: the other variant of the
     # headline configuration
     n = 26
@@ -838,6 +789,69 @@ def run_configs(args, E, L, ctx, stream, rank):
     del hp, ah, bh
     res["protogalaxy_fold"] = run_pg_fold(E, L, ctx, stream, check)
     return res
+
+
+def run_ml_n20(E, L, ctx, stream, check, steps=200):
+    """Multilinear MSB over Fp, num_vars = 20 (config 1), all rounds."""
+    import numpy as np
+    import torch
+    if check:
+        from oracle import oracle as O
+    n = 20
+    v = E.gen_uniform(E.table_seed(0x3170_2026, 0), 1 << n, ctx=ctx)
+    ml = E.MultilinearProver(v, field=E.FP, ctx=ctx)
+    lab = b"effsc-gpu/ml/v1"
+
+    def ml_proof(use_graph=True):
+        ml.reset()
+        return ml.prove(n, E.Transcript.keccak(E.FP, lab), use_graph=use_graph)
+
+    ms, pf = time_proofs(torch, stream, ml_proof, steps)
+    by, _ = profile_bytes(E, L, lambda: ml_proof(False))
+    ok = None
+    if check:
+        rp, ch, fv = O.sumcheck(O.Prover(O.ML, O.MSB, 1, [v]), n, O.Transcript(1, label=lab))
+        ok = bool(np.array_equal(pf.round_polys.reshape(n, 1), rp[:, :, 0]) and
+                  np.array_equal(pf.final_value.reshape(1), fv[:1]))
+        assert ok, "Multilinear n=20 proof differs from the oracle"
+    return {
+        "workload": "MultilinearProver MSB over Fp, num_vars=20, seeded uniform table, Fp challenges, label %s, "
+                    "20 rounds + finalize; one CUDA graph per proof (L2-resident, latency-bound)" % lab.decode(),
+        "us_per_proof": ms * 1e3, "evals_per_s": (1 << n) / (ms * 1e-3), "algorithmic_bytes": by,
+        "hbm_gbs": by / (ms * 1e-3) / 1e9, "bit_exact_vs_oracle": ok}
+
+
+def run_gkr_k12(E, L, ctx, stream, check, steps=20):
+    """GkrProver, k = 12: add, mult of 2^24 base entries, w of 2^12, 24 rounds."""
+    import numpy as np
+    import torch
+    if check:
+        from oracle import oracle as O
+    k = 12
+    add = E.gen_uniform(E.table_seed(0x6C12_2026, 0), 1 << (2 * k), ctx=ctx)
+    mult = E.gen_uniform(E.table_seed(0x6C12_2026, 1), 1 << (2 * k), ctx=ctx)
+    wv = E.gen_uniform(E.table_seed(0x6C12_2026, 2), 1 << k, ctx=ctx)
+    gk = E.GkrProver(add, mult, wv, ctx=ctx)
+    lab_g = b"effsc-gpu/gkr/v1"
+
+    def gkr_proof(use_graph=True):
+        gk.reset()
+        return gk.prove(2 * k, E.Transcript.keccak(E.FP3, lab_g), use_graph=use_graph)
+
+    ms_g, pf_g = time_proofs(torch, stream, gkr_proof, steps)
+    by_g, _ = profile_bytes(E, L, lambda: gkr_proof(False))
+    ok_g = None
+    if check:
+        orc = O.Prover.gkr(3, add, mult, wv)
+        rp, ch, fv = O.sumcheck(orc, 2 * k, O.Transcript(3, label=lab_g))
+        ok_g = bool(np.array_equal(pf_g.round_polys, rp) and np.array_equal(pf_g.final_value, fv)
+                    and np.array_equal(gk.claimed_w_values(), orc.claimed_w_values()))
+        assert ok_g, "GkrProver k=12 proof differs from the oracle"
+    return {
+        "workload": "GkrProver (MSB), k=12: add, mult seeded uniform tables of 2^24 Goldilocks values, w of 2^12, "
+                    "Fp3 challenges, 24 rounds + finalize, label %s; witness kept as two 2^12 tables" % lab_g.decode(),
+        "ms_per_proof": ms_g, "evals_per_s": 2 * (1 << (2 * k)) / (ms_g * 1e-3), "algorithmic_bytes": by_g,
+        "hbm_gbs": by_g / (ms_g * 1e-3) / 1e9, "bit_exact_vs_oracle": ok_g}
 
 
 def run_pg_fold(E, L, ctx, stream, check, steps=20):
@@ -996,8 +1010,13 @@ def run_only(args):
     ctx = E.Context(0)
     stream = torch.cuda.current_stream()
     ctx.set_stream(stream.cuda_stream)
+    check = not args.no_cpu_baseline
     if args.only == "protogalaxy_fold":
-        rec = run_pg_fold(E, L, ctx, stream, not args.no_cpu_baseline, steps=max(args.steps, 1))
+        rec = run_pg_fold(E, L, ctx, stream, check, steps=max(args.steps, 1))
+    elif args.only == "multilinear_n20":
+        rec = run_ml_n20(E, L, ctx, stream, check, steps=max(args.steps, 1))
+    else:
+        rec = run_gkr_k12(E, L, ctx, stream, check, steps=max(args.steps, 1))
     print(json.dumps({"only": args.only, "record": rec}))
 
 
