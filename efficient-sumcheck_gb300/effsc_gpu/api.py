@@ -27,7 +27,7 @@ from dataclasses import dataclass
 import numpy as np
 
 from . import _lib
-from ._lib import check, load, u64p, u8p, vp
+from ._lib import check, load, u64p, vp
 
 ML, IP, COEF, EQF, GKR = 0, 1, 2, 3, 4
 MSB, LSB = 0, 1

@@ -6,7 +6,6 @@ instance alone (runner::sumcheck, src/runner.rs:29-69, all rounds, Keccak
 transcript labelled per instance, no hook) and to the single-instance GPU
 path, with and without graph replay, before and after autotuning."""
 import json
-import os
 import random
 
 import numpy as np
