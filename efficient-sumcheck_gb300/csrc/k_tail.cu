@@ -353,8 +353,7 @@ static bool tail_cluster_inst(const TailArgs& a, u32 cs_log, cudaStream_t s) {
     if (bytes > TAIL_SMEM_CAP || CS > (u32)TAIL_MAX_CS) return false;
     cudaFuncSetAttribute(k_tail_cluster<POL, FW>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TAIL_SMEM_CAP);
     if (CS > 8) cudaFuncSetAttribute(k_tail_cluster<POL, FW>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
-    cudaLaunchConfig_t cfg;
-    memset(&cfg, 0, sizeof cfg);
+    cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(CS, 1, 1);
     cfg.blockDim = dim3(TAIL_TPB, 1, 1);
     cfg.dynamicSmemBytes = bytes;
@@ -385,8 +384,7 @@ u32 tail_cluster_max(void) {
             cudaGetLastError();
             continue;
         }
-        cudaLaunchConfig_t cfg;
-        memset(&cfg, 0, sizeof cfg);
+        cudaLaunchConfig_t cfg = {};
         cfg.gridDim = dim3(cs, 1, 1);
         cfg.blockDim = dim3(TAIL_TPB, 1, 1);
         cfg.dynamicSmemBytes = TAIL_SMEM_CAP;

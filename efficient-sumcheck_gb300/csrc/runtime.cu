@@ -1617,7 +1617,7 @@ int effsc_prover_table_len(const effsc_prover* P, int table, size_t* out) {
 }
 
 int effsc_prover_read_table(effsc_prover* P, int table, uint64_t* out) {
-    size_t n;
+    size_t n = 0;
     TRY(effsc_prover_table_len(P, table, &n));
     if (!n) return EFFSC_OK;
     if (!out) return fail(EFFSC_INVALID_ARG, "out is NULL");
