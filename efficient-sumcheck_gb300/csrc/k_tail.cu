@@ -177,6 +177,23 @@ __device__ void tail_loop(u64* smb, u64 stride, u64 len, u32 k0, bool fold, cons
         fold = true;
     }
     if (warp == 0) tx_store((DevTranscript*)a.tx, w, lane);
+    if (a.final_fold && len >= 2) {
+        // SumcheckProver::finalize with the last challenge: one MSB fold
+        // (src/inner_product_sumcheck.rs:143-176, src/multilinear_sumcheck.rs:132-178)
+        constexpr bool E = FW == 3;
+        const Mul3 m = mul3_prepare<E>(f3_make(sh.chal[0], sh.chal[1], sh.chal[2]));
+        const u64 half = len >> 1;
+        for (u64 j = threadIdx.x; j < half; j += TAIL_TPB)
+#pragma unroll
+            for (int t = 0; t < NT; t++)
+                sm_st<FW>(smb, stride, t, j, f3_fold<E, E>(sm_ld<FW>(smb, stride, t, j), sm_ld<FW>(smb, stride, t, j + half), m));
+        __syncthreads();
+        len = half;
+    }
+    if (a.first_out && threadIdx.x < 12) {
+        const int t = threadIdx.x / 3, c = threadIdx.x % 3;
+        a.first_out[threadIdx.x] = (t < NT && c < FW) ? smb[(u64)(t * FW + c) * stride] : 0;
+    }
     // write back the tables after the last fold
     if (a.out[0][0]) {
         for (int t = 0; t < NT; t++)

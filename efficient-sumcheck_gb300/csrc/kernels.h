@@ -88,6 +88,9 @@ struct TailArgs {
     const uint8_t* hook;
     u64* proof_wire;       // round r0's wire values (3 * nwire words per round)
     u64* proof_chal;       // round r0's challenge (3 words per round)
+    u32 final_fold;        // 1: the runner's finalize (one more fold with the last
+                           // challenge) before the tables are written back
+    u64* first_out;        // (optional) the tables' first entries, 3 words per table, 4 tables
 };
 // Largest table length (a power of two) the tail kernel holds for this
 // policy and field width (1: Fp, 3: Fp3), within `smem_cap` bytes.

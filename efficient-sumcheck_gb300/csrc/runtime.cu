@@ -588,9 +588,12 @@ bool cluster_tail_ok(const effsc_prover* P, size_t r, size_t num_rounds, const C
     return true;
 }
 
-int do_tail(effsc_prover* P, size_t r, size_t num_rounds, const Chal& ch, const TxIO& tx, bool dry, u32 cs_log = 0) {
+// fin: the tail also runs the runner's finalize (the last challenge's fold)
+// and writes the tables' first entries to `first` (the proof read-back).
+int do_tail(effsc_prover* P, size_t r, size_t num_rounds, const Chal& ch, const TxIO& tx, bool dry, u32 cs_log = 0,
+            bool fin = false, u64* first = nullptr) {
     const int pol = pol_of(P), fw = P->field == EFFSC_FP3 ? 3 : 1, nt = P->ntab;
-    const size_t L = P->t[0].len, rounds = num_rounds - r, folds = rounds - (ch.has ? 0 : 1);
+    const size_t L = P->t[0].len, rounds = num_rounds - r, folds = rounds - (ch.has ? 0 : 1) + (fin ? 1 : 0);
     TailArgs ta;
     memset(&ta, 0, sizeof ta);
     ta.L = L;
@@ -602,6 +605,8 @@ int do_tail(effsc_prover* P, size_t r, size_t num_rounds, const Chal& ch, const 
     ta.hook_len = tx.hook_len;
     ta.proof_wire = tx.proof_wire;
     ta.proof_chal = tx.proof_chal;
+    ta.final_fold = fin ? 1 : 0;
+    ta.first_out = first;
     const bool out_ext = fw == 3;
     int bi[3] = {0, 0, 0};
     uint64_t bytes = 0;
@@ -1726,6 +1731,7 @@ int effsc_prove(effsc_prover* P, size_t num_rounds, effsc_transcript* T, const u
 
     auto launch_all = [&](bool dry) -> int {
         size_t r0 = 0;
+        bool tail_done = false;
         if (fuse_first_ok(P, num_rounds)) {
             TxIO t0, t2;
             memset(&t0, 0, sizeof t0);
@@ -1773,17 +1779,22 @@ int effsc_prove(effsc_prover* P, size_t num_rounds, effsc_transcript* T, const u
             tx.proof_wire = P->d_wire + (size_t)r * 3 * d;
             tx.proof_chal = P->d_chals + 3 * r;
             tx.chal_next = nullptr;
+            // the tail runs the remaining rounds, the runner's finalize and
+            // the read-back gather in its one launch
             if (tail_ok(P, r, num_rounds, ch)) {
-                TRY(do_tail(P, r, num_rounds, ch, tx, dry));
+                TRY(do_tail(P, r, num_rounds, ch, tx, dry, 0, true, P->d_first));
+                tail_done = true;
                 break;
             }
             u32 cs_log = 0;
             if (cluster_tail_ok(P, r, num_rounds, ch, &cs_log)) {
-                TRY(do_tail(P, r, num_rounds, ch, tx, dry, cs_log));
+                TRY(do_tail(P, r, num_rounds, ch, tx, dry, cs_log, true, P->d_first));
+                tail_done = true;
                 break;
             }
             TRY(do_round(P, ch, tx, dry));
         }
+        if (tail_done) return EFFSC_OK;
         if (num_rounds) {
             Chal ch;
             ch.has = true; ch.ext = P->field == EFFSC_FP3; ch.dev = P->d_chals + 3 * (num_rounds - 1);
