@@ -55,7 +55,8 @@ def parse():
                     help="batching leg: this many IP instances, num_vars uniform on 10..=22 (0 = skip)")
     ap.add_argument("--batch-steps", type=int, default=10)
     ap.add_argument("--no-configs", action="store_true",
-                    help="skip the Multilinear n=20 and Coefficient/EqFactored n=24 legs")
+                    help="skip the other single-proof workloads (Multilinear n=20, Coefficient / EqFactored "
+                         "n=24, GKR k=12, InnerProduct LSB n=26, host-resident n=28, ProtoGalaxy fold)")
     ap.add_argument("--serve-requests", type=int, default=20000,
                     help="serving leg: this many requests, 70%% IP / 30%% ML, num_vars uniform on 14..=26 (0 = skip)")
     ap.add_argument("--serve-slots", type=int, default=128)
