@@ -38,6 +38,14 @@ __device__ __forceinline__ void sm_st(u64* sm, u64 L, int t, u64 i, const F3& v)
 constexpr int TAIL_TPB = 512;
 constexpr int TAIL_NW = TAIL_TPB / 32;
 
+// Index i of a table of 2^lg entries with its lg bits reversed.  An LSB
+// prover's table held in this order makes its folds (2j, 2j+1) -> j MSB
+// folds (p, p + L/2) -> p, in place, with entry j of every later length at
+// the reversed position again; so the LSB tail is the MSB tail on a
+// bit-reversed layout, reversed back when the tables are written out.
+__device__ __forceinline__ u64 tail_rev(u64 i, u32 lg) { return lg ? (u64)(__brev((u32)i) >> (32 - lg)) : 0; }
+__device__ __forceinline__ u32 tail_lg(u64 n) { return n > 1 ? 63 - __clzll(n) : 0; }
+
 // Shared state of a tail block: block partials, round totals, challenge,
 // squeeze scratch, and (cluster kernel, CTA 0) the partials of every CTA.
 constexpr int TAIL_NW3 = 12;
@@ -194,13 +202,14 @@ __device__ void tail_loop(u64* smb, u64 stride, u64 len, u32 k0, bool fold, cons
         const int t = threadIdx.x / 3, c = threadIdx.x % 3;
         a.first_out[threadIdx.x] = (t < NT && c < FW) ? smb[(u64)(t * FW + c) * stride] : 0;
     }
-    // write back the tables after the last fold
+    // write back the tables after the last fold (LSB: from the reversed layout)
     if (a.out[0][0]) {
+        const u32 lg = tail_lg(len);
         for (int t = 0; t < NT; t++)
             for (int c = 0; c < FW; c++) {
                 const u64* src = smb + (u64)(t * FW + c) * stride;
                 u64* dst = a.out[t][c];
-                for (u64 i = threadIdx.x; i < len; i += TAIL_TPB) dst[i] = src[i];
+                for (u64 i = threadIdx.x; i < len; i += TAIL_TPB) dst[i] = src[a.lsb ? tail_rev(i, lg) : i];
             }
     }
 }
@@ -217,11 +226,12 @@ __device__ void tail_body(const TailArgs& a) {
     __shared__ TailShared sh;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const u64 L0 = a.L;
+    const u32 lg0 = tail_lg(L0);
     for (int t = 0; t < NT; t++)
         for (int c = 0; c < FW; c++) {
             const u64* src = (c == 0 || ((a.in_ext >> t) & 1u)) ? a.in[t][c] : nullptr;
             u64* dst = sm + (u64)(t * FW + c) * L0;
-            for (u64 i = threadIdx.x; i < L0; i += TAIL_TPB) dst[i] = src ? src[i] : 0;
+            for (u64 i = threadIdx.x; i < L0; i += TAIL_TPB) dst[a.lsb ? tail_rev(i, lg0) : i] = src ? src[i] : 0;
         }
     if (threadIdx.x < 3) sh.chal[threadIdx.x] = a.first_fold ? a.chal_in[threadIdx.x] : 0;
     WarpTx w;

@@ -91,6 +91,7 @@ struct TailArgs {
     u32 final_fold;        // 1: the runner's finalize (one more fold with the last
                            // challenge) before the tables are written back
     u64* first_out;        // (optional) the tables' first entries, 3 words per table, 4 tables
+    u32 lsb;               // LSB prover: pairs (2j, 2j+1); held bit-reversed in shared memory
 };
 // Largest table length (a power of two) the tail kernel holds for this
 // policy and field width (1: Fp, 3: Fp3), within `smem_cap` bytes.

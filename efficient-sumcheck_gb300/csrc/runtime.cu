@@ -545,12 +545,13 @@ int round_std(effsc_prover* P, const Chal& ch, const TxIO& tx, bool dry) {
 }
 
 // Whether rounds r .. num_rounds-1 of effsc_prove can run in the one-block
-// tail kernel: MSB Multilinear / InnerProduct, equal power-of-two tables that
+// tail kernel: Multilinear / InnerProduct (MSB, or LSB on a bit-reversed
+// layout), equal power-of-two tables that
 // fit in shared memory, challenges in device memory, and every round still
 // folding to at least two entries (the length-1 cases stay on the per-round
 // path).
 bool tail_ok(const effsc_prover* P, size_t r, size_t num_rounds, const Chal& ch) {
-    if ((P->kind != EFFSC_ML && P->kind != EFFSC_IP) || P->order != EFFSC_MSB || !P->tail_len) return false;
+    if ((P->kind != EFFSC_ML && P->kind != EFFSC_IP) || !P->tail_len) return false;
     if (r >= num_rounds || (ch.has && !ch.dev)) return false;
     const size_t L = P->t[0].len;
     for (int i = 1; i < P->ntab; i++)
@@ -607,6 +608,7 @@ int do_tail(effsc_prover* P, size_t r, size_t num_rounds, const Chal& ch, const 
     ta.proof_chal = tx.proof_chal;
     ta.final_fold = fin ? 1 : 0;
     ta.first_out = first;
+    ta.lsb = P->order == EFFSC_LSB ? 1 : 0;
     const bool out_ext = fw == 3;
     int bi[3] = {0, 0, 0};
     uint64_t bytes = 0;

@@ -1,4 +1,4 @@
-"""The one-block tail kernel of effsc_prove (MSB Multilinear / InnerProduct):
+"""The one-block tail kernel of effsc_prove (Multilinear / InnerProduct, MSB and LSB):
 proofs and post-states identical to the per-round path and to the oracle for
 every switch point, field, partial run and hook."""
 import random
@@ -102,3 +102,26 @@ def test_hook_lengths(E, hook_len, tail):
     assert np.array_equal(pf.round_polys, rp)
     assert np.array_equal(pf.challenges, ch)
     assert np.array_equal(pf.final_value, fv)
+
+
+@pytest.mark.parametrize("kind", ["ml", "ip"])
+@pytest.mark.parametrize("field", [1, 3])
+@pytest.mark.parametrize("n,rounds", [(6, 6), (9, 4), (11, 7), (12, 12)])
+def test_lsb_tail_proof_and_post_state(E, kind, field, n, rounds):
+    """LSB provers run their tail on a bit-reversed shared-memory layout: the
+    proof, the tables left after the runner's finalize and the final value
+    equal the oracle's, full and partial runs, with a hook."""
+    g = np.random.default_rng(1000 + n * 7 + rounds + field)
+    k = 2 if kind == "ip" else 1
+    tabs = [g.integers(0, O.P, size=1 << n, dtype=np.uint64) for _ in range(k)]
+    cls = E.InnerProductProverLSB if kind == "ip" else E.MultilinearProverLSB
+    p = cls(*tabs, field=field)
+    hook = bytes(range(24))
+    pf = p.prove(rounds, E.Transcript.keccak(field, b"lsbtail"), hook=hook)
+    orc = O.Prover(O.IP if kind == "ip" else O.ML, O.LSB, field, tabs)
+    rp, ch, fv = O.sumcheck(orc, rounds, O.Transcript(field, label=b"lsbtail"), hook=hook)
+    assert np.array_equal(np.asarray(pf.round_polys).reshape(rounds, k, field), rp[:, :k, :field])
+    assert np.array_equal(np.asarray(pf.challenges).reshape(rounds, field), ch[:, :field])
+    assert np.array_equal(np.asarray(pf.final_value).reshape(field), fv[:field])
+    for t in range(k):
+        assert np.array_equal(np.asarray(p.table(t)).reshape(-1, field), orc.table(t)[:, :field]), t
