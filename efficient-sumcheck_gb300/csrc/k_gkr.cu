@@ -7,12 +7,20 @@
 // compact tables: W_b (folded during the first k rounds) and W_c (folded
 // during the last k); entry i of the current gate tables reads
 //   W_b[i >> kc] and W_c[i & (2^kc - 1)],  kc = min(k, log2 |add|),
-// the same values the broadcast tables hold.  Each round evaluates
-// f(x) = add (W_b + W_c) + mult W_b W_c at x = 0, 1, 2 over the pairs
-// (i, i + half) -- optionally right after folding add and mult with the
-// previous challenge in the same pass -- and the last block turns the three
-// sums into the wire [q(0), (q(0) + q(2) - 2 q(1)) / 2].
-#include "round_common.cuh"
+// the same values the broadcast tables hold.  Each round pairs (i, i + half)
+// -- optionally right after folding add and mult with the previous challenge
+// in the same pass.  The two ends of a pair differ in one variable: a b
+// variable while the pair's W_b indices differ (the first k rounds), else a c
+// variable, and the other witness table reads one entry s at both ends.  So
+//   f(x) = add (W_b + W_c) + mult W_b W_c
+// is quadratic in x, and the wire the reference derives from q(0), q(1), q(2),
+// [q(0), (q(0) + q(2) - 2 q(1)) / 2], is q(0) and f's x^2 coefficient
+//   c2 = sum d_w (d_add + d_mult s),
+// d_* the differences across the pair and d_w that of the varying witness
+// table: one product per pair in place of the points x = 1 and x = 2.  With
+// two accumulators every variant fits 128 registers without spills and runs
+// two blocks per SM (measured, k = 12 over Fp3: 0.98 -> 0.90 ms per proof).
+#include "ml01.cuh"
 
 namespace effsc {
 
@@ -26,39 +34,46 @@ __device__ __forceinline__ void gkr_point(ProdAcc<EA, EWB || EWC>& acc, const F3
     acc.mac(m, f3_mul<EWB, EWC>(wb, wc));
 }
 
-template <bool E>
-__device__ __forceinline__ F3 twice_minus(const F3& hi, const F3& lo) {
-    return f3_sub<E>(f3_add<E>(hi, hi), lo);
+// Pair (i, i + H) of the gate tables (add al / ah, mult ml / mh): q(0) gets
+// the point x = 0 and c2 the product d_w (d_add + d_mult s).
+template <bool EA, bool EWB, bool EWC>
+__device__ __forceinline__ void gkr_pair(ProdAcc<EA, EWB || EWC>& q0, ProdAcc<EA || EWB || EWC, EWB || EWC>& qc,
+                                         const RoundArgs& a, const F3& al, const F3& ah, const F3& ml, const F3& mh,
+                                         u64 i, u64 H, u32 kc, u64 cm, bool bvar) {
+    const F3 wbl = ld<EWB>(a.t[2].in, i >> kc), wcl = ld<EWC>(a.t[3].in, i & cm);
+    gkr_point<EA, EWB, EWC>(q0, al, ml, wbl, wcl);
+    const F3 da = f3_sub<EA>(ah, al), dm = f3_sub<EA>(mh, ml);
+    if (bvar) {
+        const F3 dw = f3_sub<EWB>(ld<EWB>(a.t[2].in, (i + H) >> kc), wbl);
+        qc.mac(f3_add_mixed<EA || EWC, EA>(f3_mul<EA, EWC>(dm, wcl), da), dw);
+    } else {
+        const F3 dw = f3_sub<EWC>(ld<EWC>(a.t[3].in, (i + H) & cm), wcl);
+        qc.mac(f3_add_mixed<EA || EWB, EA>(f3_mul<EA, EWB>(dm, wbl), da), dw);
+    }
 }
 
-// Blocks per SM the register budget is sized for: Fp3 gate tables with an
-// Fp3 witness keep three Fp3 x Fp3 accumulators (75 registers) live, which
-// fit without spills only at one block per SM.
 template <bool FUSED, bool EAI, bool EWB, bool EWC, bool ECH>
-constexpr int gkr_min_blocks() { return ((FUSED ? (EAI || ECH) : EAI) && (EWB || EWC)) ? 1 : 2; }
-
-template <bool FUSED, bool EAI, bool EWB, bool EWC, bool ECH>
-__global__ void __launch_bounds__(TPB, (gkr_min_blocks<FUSED, EAI, EWB, EWC, ECH>())) k_gkr(RoundArgs a) {
+__global__ void __launch_bounds__(TPB, 2) k_gkr(RoundArgs a) {
     constexpr bool EA = FUSED ? (EAI || ECH) : EAI;   // add / mult after the fold
     constexpr bool EW = EWB || EWC;
-    ProdAcc<EA, EW> q0, q1, q2;
+    ProdAcc<EA, EW> q0;
+    ProdAcc<EA || EW, EW> qc;                         // c2
     q0.init();
-    q1.init();
-    q2.init();
+    qc.init();
     const u64 L = a.L;
     const u64 Ln = FUSED ? L >> 1 : L;                 // length evaluated
     const u32 lg = 63 - __clzll(Ln > 0 ? Ln : 1);
     const u32 kc = a.m_shift < lg ? a.m_shift : lg;
     const u64 cm = (1ULL << kc) - 1;
+    const bool bvar = kc < lg;                         // the pairs differ in W_b's index
     const u64 tid = (u64)blockIdx.x * TPB + threadIdx.x, stride = (u64)gridDim.x * TPB;
     if (Ln == 1) {
+        // q(1) = 0 and q(2) = -q(0), so the wire's q(inf) is 0 (src/provers/gkr.rs:119-127)
         if (tid == 0) {
             const F3 al = ld<EA>(FUSED ? (const u64* const*)a.t[0].out : a.t[0].in, 0);
             const F3 ml = ld<EA>(FUSED ? (const u64* const*)a.t[1].out : a.t[1].in, 0);
             const F3 wb = ld<EWB>(a.t[2].in, 0), wc = ld<EWC>(a.t[3].in, 0);
             gkr_point<EA, EWB, EWC>(q0, al, ml, wb, wc);
-            // q(2) = -q(0) so that the wire's q(inf) is 0 (src/provers/gkr.rs:119-127)
-            gkr_point<EA, EWB, EWC>(q2, f3_sub<EA>(f3_zero(), al), f3_sub<EA>(f3_zero(), ml), wb, wc);
         }
     } else {
         F3 rr;
@@ -87,16 +102,128 @@ __global__ void __launch_bounds__(TPB, (gkr_min_blocks<FUSED, EAI, EWB, EWC, ECH
                 al = ld<EA>(a.t[0].in, i); ah = ld<EA>(a.t[0].in, i + H);
                 ml = ld<EA>(a.t[1].in, i); mh = ld<EA>(a.t[1].in, i + H);
             }
-            const F3 wbl = ld<EWB>(a.t[2].in, i >> kc), wbh = ld<EWB>(a.t[2].in, (i + H) >> kc);
-            const F3 wcl = ld<EWC>(a.t[3].in, i & cm), wch = ld<EWC>(a.t[3].in, (i + H) & cm);
-            gkr_point<EA, EWB, EWC>(q0, al, ml, wbl, wcl);
-            gkr_point<EA, EWB, EWC>(q1, ah, mh, wbh, wch);
-            gkr_point<EA, EWB, EWC>(q2, twice_minus<EA>(ah, al), twice_minus<EA>(mh, ml), twice_minus<EWB>(wbh, wbl),
-                                    twice_minus<EWC>(wch, wcl));
+            gkr_pair<EA, EWB, EWC>(q0, qc, a, al, ah, ml, mh, i, H, kc, cm, bvar);
         }
     }
-    F3 raw[3] = {q0.result(), q1.result(), q2.result()};
-    reduce_and_finalize<3>(raw, a, POL_GKR);
+    F3 raw[2] = {q0.result(), qc.result()};
+    reduce_and_finalize<2>(raw, a, POL_GKR);
+}
+
+// Two-pass start (k >= 3, base add, mult and witness, Fp or Fp3
+// challenges): rounds 0 and 1 from one pass, round 2 with a double fold from
+// a second -- the GKR counterpart of ip01.cuh.
+//
+// Pass 1, quadruple j < Q = N/4 (N = n^2 = |add|): x_s = x[j + s Q] of add (a)
+// and mult (m), the witness entries w_s = W_b[(j >> k) + s n/4] (quarter s's
+// b index) and c = W_c[j mod n].  Rounds 0 and 1 both bind b variables; with
+// d_s = x_{s+2} - x_s (s = 0, 1) round 0's pairs give
+//   P_s = a_s (w_s + c) + c m_s w_s,  D_s = dw_s (da_s + c dm_s),
+// its wire is [sum P_0 + P_1, sum D_0 + D_1], and round 1's, on the tables
+// folded with r0, is quadratic in r0:
+//   q(0) = sum P_0 + r0 sum B + r0^2 sum D_0,
+//   B = a_0 dw_0 + da_0 (w_0 + c) + c (m_0 dw_0 + dm_0 w_0),
+//   c2 = sum e g + r0 sum (f g + e h) + r0^2 sum f h,
+//   e = w_1 - w_0, f = dw_1 - dw_0, g = (a_1 - a_0) + c (m_1 - m_0),
+//   h = (da_1 - da_0) + c (dm_1 - dm_0).
+// The eight sums take the places of POL_IP01's (T0, T1, T2, U0, U1, U2, V0,
+// V2), whose finalize runs both transcript steps.
+__device__ __forceinline__ void gkr01_quad(Acc (&s)[8], u64 a0, u64 a1, u64 a2, u64 a3, u64 m0, u64 m1, u64 m2, u64 m3,
+                                           u64 w0, u64 w1, u64 w2, u64 w3, u64 c) {
+    const u64 da0 = gl_sub(a2, a0), da1 = gl_sub(a3, a1), dm0 = gl_sub(m2, m0), dm1 = gl_sub(m3, m1);
+    const u64 dw0 = gl_sub(w2, w0), dw1 = gl_sub(w3, w1);
+    const u64 w0c = gl_add(w0, c);
+    const u64 cdm0 = gl_mul(c, dm0), cdm1 = gl_mul(c, dm1);
+    acc_mac(s[0], a0, w0c);                              // P_0
+    acc_mac(s[0], c, gl_mul(m0, w0));
+    acc_mac(s[6], a1, gl_add(w1, c));                    // P_1
+    acc_mac(s[6], c, gl_mul(m1, w1));
+    acc_mac(s[2], dw0, gl_add(da0, cdm0));               // D_0
+    acc_mac(s[7], dw1, gl_add(da1, cdm1));               // D_1
+    Acc t = acc_zero();                                   // B
+    acc_mac(t, m0, dw0);
+    acc_mac(t, dm0, w0);
+    acc_mac(s[1], c, acc_reduce(t));
+    acc_mac(s[1], a0, dw0);
+    acc_mac(s[1], da0, w0c);
+    const u64 e = gl_sub(w1, w0), f = gl_sub(dw1, dw0);
+    const u64 g = gl_add(gl_sub(a1, a0), gl_mul(c, gl_sub(m1, m0)));
+    const u64 h = gl_add(gl_sub(da1, da0), gl_sub(cdm1, cdm0));
+    acc_mac(s[3], e, g);
+    acc_mac(s[4], f, g);
+    acc_mac(s[4], e, h);
+    acc_mac(s[5], f, h);
+}
+
+__global__ void __launch_bounds__(TPB, 2) k_gkr_r01(RoundArgs a) {
+    Acc s[8];
+#pragma unroll
+    for (int i = 0; i < 8; i++) s[i] = acc_zero();
+    const u64 Q = a.L >> 2;
+    const u32 k = a.m_shift;
+    const u64 nq = (1ULL << k) >> 2, cm = (1ULL << k) - 1;
+    const u64* A = a.t[0].in[0];
+    const u64* M = a.t[1].in[0];
+    const u64* WB = a.t[2].in[0];
+    const u64* WC = a.t[3].in[0];
+    const u64 tid = (u64)blockIdx.x * TPB + threadIdx.x, stride = (u64)gridDim.x * TPB;
+    for (u64 j = tid; j < Q; j += stride) {
+        const u64 a0 = __ldcs(A + j), a1 = __ldcs(A + j + Q), a2 = __ldcs(A + j + 2 * Q), a3 = __ldcs(A + j + 3 * Q);
+        const u64 m0 = __ldcs(M + j), m1 = __ldcs(M + j + Q), m2 = __ldcs(M + j + 2 * Q), m3 = __ldcs(M + j + 3 * Q);
+        const u64 b = j >> k;
+        gkr01_quad(s, a0, a1, a2, a3, m0, m1, m2, m3, WB[b], WB[b + nq], WB[b + 2 * nq], WB[b + 3 * nq], WC[j & cm]);
+    }
+    F3 raw[3];
+    raw[0] = f3_make(acc_reduce(s[0]), acc_reduce(s[1]), acc_reduce(s[2]));
+    raw[1] = f3_make(acc_reduce(s[3]), acc_reduce(s[4]), acc_reduce(s[5]));
+    raw[2] = f3_make(acc_reduce(s[6]), acc_reduce(s[7]), 0);
+    reduce_and_finalize_seg<3>(raw, a, POL_IP01, gridDim.x, blockIdx.x);
+}
+
+// Pass 2: add and mult folded with r0 and r1 at once from the base tables
+// (ml_fold2 on the quarters x[i + s Q]; the entry i + H of the length-Q table
+// from x[i + H + s Q], H = Q/2), written out, and round 2 -- a b variable,
+// k >= 3 -- evaluated on them with W_b folded twice (t[2]) and W_c as is.
+template <bool ECH>
+__global__ void __launch_bounds__(TPB, 2) k_gkr_r2x(RoundArgs a) {
+    constexpr bool EA = ECH, EWB = ECH, EWC = false;
+    ProdAcc<EA, EWB> q0;
+    ProdAcc<EA || EWB, EWB> qc;
+    q0.init();
+    qc.init();
+    const F3 r0 = f3_make(a.chal_ptr[0], a.chal_ptr[1], a.chal_ptr[2]);
+    const F3 r1 = f3_make(a.chal2_ptr[0], a.chal2_ptr[1], a.chal2_ptr[2]);
+    const F3 r01 = f3_mul<ECH, ECH>(r0, r1);
+    const u64 Q = a.L >> 2, H = Q >> 1;
+    const u32 kc = a.m_shift;
+    const u64 cm = (1ULL << kc) - 1;
+    const u64 tid = (u64)blockIdx.x * TPB + threadIdx.x, stride = (u64)gridDim.x * TPB;
+    for (u64 i = tid; i < H; i += stride) {
+        F3 lo[2], hi[2];
+#pragma unroll
+        for (int t = 0; t < 2; t++) {
+            const u64* X = a.t[t].in[0];
+            u64 x[8];
+#pragma unroll
+            for (int j = 0; j < 8; j++) x[j] = __ldcs(X + i + j * H);
+            lo[t] = ml_fold2<ECH>(x[0], x[2], x[4], x[6], r0, r1, r01);
+            hi[t] = ml_fold2<ECH>(x[1], x[3], x[5], x[7], r0, r1, r01);
+            st<EA>(a.t[t].out, i, lo[t]);
+            st<EA>(a.t[t].out, i + H, hi[t]);
+        }
+        gkr_pair<EA, EWB, EWC>(q0, qc, a, lo[0], hi[0], lo[1], hi[1], i, H, kc, cm, true);
+    }
+    F3 raw[2] = {q0.result(), qc.result()};
+    reduce_and_finalize_seg<2>(raw, a, POL_GKR, gridDim.x, blockIdx.x);
+}
+
+bool launch_gkr01(const RoundArgs& a, int grid, cudaStream_t s) {
+    k_gkr_r01<<<grid, TPB, 0, s>>>(a);
+    return true;
+}
+bool launch_gkr2x(bool ech, const RoundArgs& a, int grid, cudaStream_t s) {
+    if (ech) k_gkr_r2x<true><<<grid, TPB, 0, s>>>(a);
+    else k_gkr_r2x<false><<<grid, TPB, 0, s>>>(a);
+    return true;
 }
 
 #define GKR(F, EA, EWB, EWC, ECH) \

@@ -36,7 +36,7 @@ int pol_ntables(int pol) {
 }
 int pol_nraw(int pol) {
     switch (pol) {
-    case POL_C2: case POL_GKR: case POL_C3W: return 3;
+    case POL_C2: case POL_C3W: return 3;
     case POL_C3: return 4;
     default: return 2;
     }

@@ -32,8 +32,8 @@ enum Sem { SEM_MSB_PAD = 0, SEM_MSB_FLOOR = 1, SEM_LSB = 2 };
 //  POL_C3W : POL_C3 without h(1) (the wire needs h(0), h(inf), h(2); the
 //            legacy (c0, c1) pair is not produced): the device protocol
 //  POL_ML01: Multilinear rounds 0 and 1 from one pass (quarter sums)
-//  POL_GKR : GkrProver, q(0), q(1), q(2) of add (W_b + W_c) + mult W_b W_c;
-//            the wire is [q(0), (q(0) + q(2) - 2 q(1)) / 2]
+//  POL_GKR : GkrProver, q(0) and the x^2 coefficient of the quadratic
+//            add (W_b + W_c) + mult W_b W_c: the wire [q(0), q(inf)]
 enum Pol {
     POL_ML = 0, POL_IP = 1, POL_C1 = 2, POL_C2 = 3, POL_C3 = 4, POL_EQFR = 5, POL_EQFL = 6, POL_IP01 = 7,
     POL_GKR = 8, POL_C3W = 9, POL_ML01 = 10
@@ -160,6 +160,8 @@ bool launch_ip01(bool lsb, const RoundArgs& a, int grid, cudaStream_t s);
 bool launch_ip2x(bool lsb, const RoundArgs& a, int grid, cudaStream_t s);
 bool launch_ml01(const RoundArgs& a, int grid, cudaStream_t s);
 bool launch_ml2x(bool ech, const RoundArgs& a, int grid, cudaStream_t s);
+bool launch_gkr01(const RoundArgs& a, int grid, cudaStream_t s);
+bool launch_gkr2x(bool ech, const RoundArgs& a, int grid, cudaStream_t s);
 void launch_batch_finalize(const RoundArgs* args, const unsigned char* ext, u32 n, int ntab, u64* finals, cudaStream_t s);
 
 // Utility kernels.

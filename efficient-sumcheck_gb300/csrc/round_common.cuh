@@ -333,15 +333,11 @@ static __device__ __noinline__ void finalize_warp(int pol, const u64* raw, const
             w[0] = r[0]; w[1] = r[2]; w[2] = r[1];
             r[1] = f3_zero();
             break;
-        case POL_GKR: {
-            // src/provers/gkr.rs:185-189: q(inf) = (q(0) + q(2) - 2 q(1)) / 2
-            const u64 inv2 = 0x7FFFFFFF80000001ULL;   // (p + 1) / 2
-            F3 t = f3_sub<true>(f3_add<true>(r[0], r[2]), f3_add<true>(r[1], r[1]));
-            w[0] = r[0];
-            w[1] = f3_make(gl_mul(t.c0, inv2), gl_mul(t.c1, inv2), gl_mul(t.c2, inv2));
-            r[1] = w[1];
+        case POL_GKR:
+            // r = q(0), c2: q is quadratic, so the reference's
+            // q(inf) = (q(0) + q(2) - 2 q(1)) / 2 (src/provers/gkr.rs:185-189) is c2
+            w[0] = r[0]; w[1] = r[1];
             break;
-        }
         default:   // IP, EQF
             w[0] = r[0]; w[1] = r[1];
             break;

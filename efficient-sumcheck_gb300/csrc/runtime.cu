@@ -725,6 +725,59 @@ int do_ml_first(effsc_prover* P, const TxIO& tx0, const TxIO& tx2, const u64* ch
     return EFFSC_OK;
 }
 
+// effsc_prove of a GkrProver with k >= 3 over base add, mult and witness:
+// rounds 0 and 1 from one pass, round 2 with the folds of add and mult by r0
+// and r1 from a second (k_gkr.cu).  Leaves the state the per-round path
+// leaves after round 2: add and mult folded twice, W_b folded by r0 and r1.
+bool gkr_first_ok(const effsc_prover* P, size_t num_rounds) {
+    if (!P->fuse_first || P->kind != EFFSC_GKR || P->rounds != 0 || num_rounds < 3 || P->v_l < 3) return false;
+    const size_t n = (size_t)1 << P->v_l;
+    for (int i = 0; i < 4; i++) {
+        const Table& T = P->t[i];
+        if (T.ext || T.cur != 0 || T.len != (i < 2 ? n * n : n)) return false;
+    }
+    return true;
+}
+
+int do_gkr_first(effsc_prover* P, const TxIO& tx0, const TxIO& tx2, const u64* chals, bool dry) {
+    const size_t N = P->t[0].len, n = P->t[2].len;
+    const bool ech = P->field == EFFSC_FP3;
+    cudaStream_t s = P->ctx->stream;
+    RoundArgs a = base_args(P);
+    a.tx = tx0;
+    a.L = N;
+    a.m_shift = (u32)P->v_l;
+    for (int i = 0; i < 4; i++) set_in(a, i, P->t[i]);
+    if (!dry) TRY(timed_launch(s, "gkr_rounds_0_1", 16 * (uint64_t)N + 16 * (uint64_t)n, [&] { return launch_gkr01(a, grid_for(N / 4), s); }));
+    // W_b folded by r0, then r1 (the per-round path folds it as rounds 1 and 2 start)
+    for (int r = 0; r < 2; r++) {
+        Chal c;
+        c.has = true;
+        c.ext = ech;
+        c.dev = chals + 3 * r;
+        TRY(fold_table(P, 2, SEM_MSB_PAD, c, ech, dry));
+    }
+    int bi[2];
+    for (int i = 0; i < 2; i++) TRY(out_buffer(P, P->t[i], ech, N / 4, true, &bi[i]));
+    RoundArgs b = base_args(P);
+    b.tx = tx2;
+    b.L = N;
+    b.m_shift = (u32)P->v_l;
+    b.chal_ptr = chals;
+    b.chal2_ptr = chals + 3;
+    for (int i = 0; i < 4; i++) set_in(b, i, P->t[i]);
+    for (int i = 0; i < 2; i++) set_out(b, i, P->t[i].bufs[bi[i]]);
+    if (!dry) TRY(timed_launch(s, "gkr_round_2_double_fold", 16 * (uint64_t)N + 2 * (N / 4) * wbytes(ech), [&] { return launch_gkr2x(ech, b, grid_for(N / 8), s); }));
+    for (int i = 0; i < 2; i++) {
+        Table& T = P->t[i];
+        T.cur = bi[i];
+        T.len = N / 4;
+        T.ext = ech;
+    }
+    P->rounds = 3;
+    return EFFSC_OK;
+}
+
 // effsc_prove of an EqFactored prover whose run covers the whole left phase
 // (num_rounds >= v_l >= 2) with eq_l small enough for the one-block tail: the
 // left rounds are InnerProduct rounds on (eq_l, S), S[a] = sum_b eq_r[b]
@@ -1759,6 +1812,19 @@ int effsc_prove(effsc_prover* P, size_t num_rounds, effsc_transcript* T, const u
             t2.proof_wire = P->d_wire + (size_t)2 * 3 * d;
             t2.proof_chal = P->d_chals + 3 * 2;
             TRY(do_ml_first(P, t0, t2, P->d_chals, dry));
+            r0 = 3;
+        } else if (gkr_first_ok(P, num_rounds)) {
+            TxIO t0, t2;
+            memset(&t0, 0, sizeof t0);
+            t0.tx = P->d_tx;
+            t0.hook = P->d_hook;
+            t0.hook_len = (u32)hook_len;
+            t2 = t0;
+            t0.proof_wire = P->d_wire;
+            t0.proof_chal = P->d_chals;
+            t2.proof_wire = P->d_wire + (size_t)2 * 3 * d;
+            t2.proof_chal = P->d_chals + 3 * 2;
+            TRY(do_gkr_first(P, t0, t2, P->d_chals, dry));
             r0 = 3;
         } else if (eqf_fast_ok(P, num_rounds)) {
             TxIO t0;

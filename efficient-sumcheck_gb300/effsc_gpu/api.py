@@ -277,7 +277,8 @@ class _Prover:
         check(load().effsc_prover_reset(self.h))
 
     def set_first_rounds(self, fused):
-        """prove(): InnerProduct rounds 0-2 in two passes (True) or three."""
+        """prove(): rounds 0-2 of an InnerProduct, Multilinear or GkrProver
+        proof in two passes over the base tables (True) or three."""
         check(load().effsc_prover_set_first_rounds(self.h, 1 if fused else 0))
 
     def set_tail(self, max_len):

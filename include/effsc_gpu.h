@@ -175,10 +175,12 @@ int effsc_prover_read_table(effsc_prover* p, int table, uint64_t* out);
  * disables.  Proofs are identical. */
 int effsc_prover_set_tail(effsc_prover* p, size_t max_len);
 /* effsc_prove only (no reference counterpart; a tuning knob): for an MSB
- * InnerProduct prover over Fp3 challenges with power-of-two base tables,
- * compute rounds 0-2 in two passes over the base tables (round 1 from sums
- * gathered during round 0; round 2 folds with both challenges).  Default 1;
- * 0 runs one pass per round.  Proofs are identical. */
+ * InnerProduct prover over Fp3 challenges or an MSB Multilinear prover with
+ * power-of-two base tables, and for a GkrProver with |w| >= 8 over base
+ * add, mult and w, compute rounds 0-2 in two passes over the base tables
+ * (round 1 from sums gathered during round 0; round 2 folds with both
+ * challenges).  Default 1; 0 runs one pass per round.  Proofs are
+ * identical. */
 int effsc_prover_set_first_rounds(effsc_prover* p, int fused);
 
 /* Restore the state right after construction (the input tables are never

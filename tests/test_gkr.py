@@ -91,3 +91,33 @@ def test_gkr_rejects(E):
         E.GkrProver(np.zeros(8, np.uint64), np.zeros(9, np.uint64), np.zeros(3, np.uint64))
     with pytest.raises(E.EffscError):      # |w| not a power of two
         E.GkrProver(np.zeros(9, np.uint64), np.zeros(9, np.uint64), np.zeros(3, np.uint64))
+
+
+@pytest.mark.parametrize("k", [3, 4, 7])
+@pytest.mark.parametrize("field", [1, 3])
+@pytest.mark.parametrize("rounds_of", [lambda k: 3, lambda k: k + 1, lambda k: 2 * k])
+@pytest.mark.parametrize("hook", [b"", b"\x05\x06\x07"])
+def test_gkr_first_rounds_equal_per_round(E, k, field, rounds_of, hook):
+    """Rounds 0-1 from one pass and round 2 from a double fold (base inputs,
+    k >= 3) give the per-round path's proof, gate tables and claimed W values,
+    and the oracle's proof."""
+    rounds = rounds_of(k)
+    add, mult, w = inputs(k, False, 900 + 7 * k + rounds + field + len(hook))
+    p = E.GkrProver(add, mult, w, field=field)
+    q = E.GkrProver(add, mult, w, field=field)
+    q.set_first_rounds(False)
+    for use_graph in (True, False):
+        p.reset()
+        q.reset()
+        x = p.prove(rounds, E.Transcript.keccak(field, b"g01"), hook=hook, use_graph=use_graph)
+        y = q.prove(rounds, E.Transcript.keccak(field, b"g01"), hook=hook, use_graph=use_graph)
+        assert np.array_equal(x.round_polys, y.round_polys)
+        assert np.array_equal(x.challenges, y.challenges)
+        assert np.array_equal(x.final_value, y.final_value)
+        for t in range(2):
+            assert np.array_equal(p.table(t), q.table(t))
+        assert np.array_equal(p.claimed_w_values(), q.claimed_w_values())
+    orc = O.Prover.gkr(field, add, mult, w)
+    rp, ch, fv = O.sumcheck(orc, rounds, O.Transcript(field, label=b"g01"), hook=hook)
+    check(E, x, field, rp, ch, fv)
+    assert np.array_equal(p.claimed_w_values(), orc.claimed_w_values()[:, :field])
