@@ -52,36 +52,112 @@ __device__ __forceinline__ void gkr_pair(ProdAcc<EA, EWB || EWC>& q0, ProdAcc<EA
     }
 }
 
+__device__ __forceinline__ u64 f3c(const F3& v, int c) { return c == 0 ? v.c0 : c == 1 ? v.c1 : v.c2; }
+
+// Pairs (or quadruples) per lane of a run: a warp's run is 32 gr consecutive
+// units inside one W_b index (2^kc of them), and every warp of the grid gets
+// at least one.  A power of two up to 8, or 0 when a lane would get a single
+// unit (the per-pair forms cost the same there).
+__device__ __forceinline__ u32 gkr_run_len(u64 count, u32 kc) {
+    const u64 nw = ((u64)gridDim.x * TPB) >> 5, cap = (1ULL << kc) >> 5;
+    u64 g = count / (32 * nw);
+    if (g > 8) g = 8;
+    if (g > cap) g = cap;
+    return g < 2 ? 0u : 1u << (63 - __clzll(g));
+}
+
+// Per-pair evaluation: gates(i, al, ah, ml, mh) gives the pair's gate values.
+template <bool EA, bool EWB, bool EWC, class Gates>
+__device__ __forceinline__ void gkr_pairs(const RoundArgs& a, u64 H, u32 kc, u64 cm, bool bvar, F3 (&raw)[2], Gates gates) {
+    constexpr bool EW = EWB || EWC;
+    ProdAcc<EA, EW> q0;
+    ProdAcc<EA || EW, EW> qc;
+    q0.init();
+    qc.init();
+    const u64 tid = (u64)blockIdx.x * TPB + threadIdx.x, stride = (u64)gridDim.x * TPB;
+    for (u64 i = tid; i < H; i += stride) {
+        F3 al, ah, ml, mh;
+        gates(i, al, ah, ml, mh);
+        gkr_pair<EA, EWB, EWC>(q0, qc, a, al, ah, ml, mh, i, H, kc, cm, bvar);
+    }
+    raw[0] = q0.result();
+    raw[1] = qc.result();
+}
+
+// A b variable with W_c in the base field, by runs: W_b reads one entry per
+// run (wl at i, wh at i + H), so a pair only accumulates add + mult s,
+// add s and d_add + d_mult s (s = W_c's entry), and the run finishes
+//   q(0) += wl sum (add + mult s) + sum add s,   c2 += (wh - wl) sum (d_add + d_mult s).
+template <bool EA, bool EWB, class Gates>
+__device__ __forceinline__ void gkr_runs(const RoundArgs& a, u64 H, u32 kc, u64 cm, u32 gr, F3 (&raw)[2], Gates gates) {
+    constexpr int NC = EA ? 3 : 1;
+    const u32 lane = threadIdx.x & 31;
+    const u64 nw = ((u64)gridDim.x * TPB) >> 5, rl = 32ULL * gr, nruns = H / rl;
+    const u64* WC = a.t[3].in[0];
+    F3 q0 = f3_zero(), qc = f3_zero();
+    for (u64 u = ((u64)blockIdx.x * TPB + threadIdx.x) >> 5; u < nruns; u += nw) {
+        const u64 i0 = u * rl;
+        Acc xa[NC], ya[NC], zd[NC];
+#pragma unroll
+        for (int c = 0; c < NC; c++) xa[c] = ya[c] = zd[c] = acc_zero();
+        for (u32 t = 0; t < gr; t++) {
+            const u64 i = i0 + lane + 32 * t;
+            F3 al, ah, ml, mh;
+            gates(i, al, ah, ml, mh);
+            const u64 sv = WC[i & cm];
+#pragma unroll
+            for (int c = 0; c < NC; c++) {
+                const u64 l = f3c(al, c);
+                acc_add64(xa[c], l);
+                acc_mac(xa[c], f3c(ml, c), sv);
+                acc_mac(ya[c], l, sv);
+                acc_add64(zd[c], gl_sub(f3c(ah, c), l));
+                acc_mac(zd[c], gl_sub(f3c(mh, c), f3c(ml, c)), sv);
+            }
+        }
+        F3 x = f3_zero(), y = f3_zero(), z = f3_zero();
+        x.c0 = acc_reduce(xa[0]); y.c0 = acc_reduce(ya[0]); z.c0 = acc_reduce(zd[0]);
+        if constexpr (EA) {
+            x.c1 = acc_reduce(xa[1]); x.c2 = acc_reduce(xa[2]);
+            y.c1 = acc_reduce(ya[1]); y.c2 = acc_reduce(ya[2]);
+            z.c1 = acc_reduce(zd[1]); z.c2 = acc_reduce(zd[2]);
+        }
+        const F3 wl = ld<EWB>(a.t[2].in, i0 >> kc), wh = ld<EWB>(a.t[2].in, (i0 + H) >> kc);
+        q0 = f3_add<true>(q0, f3_add<true>(f3_mul<EA, EWB>(x, wl), y));
+        qc = f3_add<true>(qc, f3_mul<EA, EWB>(z, f3_sub<EWB>(wh, wl)));
+    }
+    raw[0] = q0;
+    raw[1] = qc;
+}
+
 template <bool FUSED, bool EAI, bool EWB, bool EWC, bool ECH>
 __global__ void __launch_bounds__(TPB, 2) k_gkr(RoundArgs a) {
     constexpr bool EA = FUSED ? (EAI || ECH) : EAI;   // add / mult after the fold
-    constexpr bool EW = EWB || EWC;
-    ProdAcc<EA, EW> q0;
-    ProdAcc<EA || EW, EW> qc;                         // c2
-    q0.init();
-    qc.init();
     const u64 L = a.L;
     const u64 Ln = FUSED ? L >> 1 : L;                 // length evaluated
     const u32 lg = 63 - __clzll(Ln > 0 ? Ln : 1);
     const u32 kc = a.m_shift < lg ? a.m_shift : lg;
     const u64 cm = (1ULL << kc) - 1;
     const bool bvar = kc < lg;                         // the pairs differ in W_b's index
-    const u64 tid = (u64)blockIdx.x * TPB + threadIdx.x, stride = (u64)gridDim.x * TPB;
+    F3 raw[2];
     if (Ln == 1) {
         // q(1) = 0 and q(2) = -q(0), so the wire's q(inf) is 0 (src/provers/gkr.rs:119-127)
-        if (tid == 0) {
+        ProdAcc<EA, EWB || EWC> q0;
+        q0.init();
+        if (blockIdx.x == 0 && threadIdx.x == 0) {
             const F3 al = ld<EA>(FUSED ? (const u64* const*)a.t[0].out : a.t[0].in, 0);
             const F3 ml = ld<EA>(FUSED ? (const u64* const*)a.t[1].out : a.t[1].in, 0);
             const F3 wb = ld<EWB>(a.t[2].in, 0), wc = ld<EWC>(a.t[3].in, 0);
             gkr_point<EA, EWB, EWC>(q0, al, ml, wb, wc);
         }
+        raw[0] = q0.result();
+        raw[1] = f3_zero();
     } else {
         F3 rr;
         Mul3 r = load_challenge_mul(a, rr);
         if (!ECH) r = mul3_prepare<false>(rr);
         const u64 H = Ln >> 1;
-        for (u64 i = tid; i < H; i += stride) {
-            F3 al, ah, ml, mh;
+        auto gates = [&](u64 i, F3& al, F3& ah, F3& ml, F3& mh) {
             if (FUSED) {
                 F3 x[2][4];
 #pragma unroll
@@ -102,10 +178,15 @@ __global__ void __launch_bounds__(TPB, 2) k_gkr(RoundArgs a) {
                 al = ld<EA>(a.t[0].in, i); ah = ld<EA>(a.t[0].in, i + H);
                 ml = ld<EA>(a.t[1].in, i); mh = ld<EA>(a.t[1].in, i + H);
             }
-            gkr_pair<EA, EWB, EWC>(q0, qc, a, al, ah, ml, mh, i, H, kc, cm, bvar);
+        };
+        if constexpr (!EWC) {
+            const u32 gr = bvar ? gkr_run_len(H, kc) : 0;
+            if (gr) gkr_runs<EA, EWB>(a, H, kc, cm, gr, raw, gates);
+            else gkr_pairs<EA, EWB, EWC>(a, H, kc, cm, bvar, raw, gates);
+        } else {
+            gkr_pairs<EA, EWB, EWC>(a, H, kc, cm, bvar, raw, gates);
         }
     }
-    F3 raw[2] = {q0.result(), qc.result()};
     reduce_and_finalize<2>(raw, a, POL_GKR);
 }
 
@@ -154,6 +235,35 @@ __device__ __forceinline__ void gkr01_quad(Acc (&s)[8], u64 a0, u64 a1, u64 a2, 
     acc_mac(s[5], f, h);
 }
 
+// Runs of 32 gr quadruples inside one b (n >= 64): w_0 .. w_3 are the same
+// for the whole run, so the eight sums factor into the run sums
+//   X_s = sum (a_s + c m_s) (s < 4),  C_s = sum c a_s (s < 3),
+// finished with the w's once per run:
+//   P_0 = w_0 X_0 + C_0,  P_1 = w_1 X_1 + C_1,
+//   D_0 = dw_0 (X_2 - X_0),  D_1 = dw_1 (X_3 - X_1),
+//   B = dw_0 X_0 + w_0 (X_2 - X_0) + C_2 - C_0,
+//   g = X_1 - X_0,  h = (X_3 - X_1) - (X_2 - X_0).
+__device__ __forceinline__ void gkr01_run(Acc (&s)[8], const Acc (&x)[4], const Acc (&ca)[3], u64 w0, u64 w1, u64 w2,
+                                          u64 w3) {
+    const u64 X0 = acc_reduce(x[0]), X1 = acc_reduce(x[1]), X2 = acc_reduce(x[2]), X3 = acc_reduce(x[3]);
+    const u64 C0 = acc_reduce(ca[0]), C1 = acc_reduce(ca[1]), C2 = acc_reduce(ca[2]);
+    const u64 dw0 = gl_sub(w2, w0), dw1 = gl_sub(w3, w1), e = gl_sub(w1, w0), f = gl_sub(dw1, dw0);
+    const u64 d20 = gl_sub(X2, X0), d31 = gl_sub(X3, X1), g = gl_sub(X1, X0), h = gl_sub(d31, d20);
+    acc_mac(s[0], w0, X0);
+    acc_add64(s[0], C0);
+    acc_mac(s[6], w1, X1);
+    acc_add64(s[6], C1);
+    acc_mac(s[2], dw0, d20);
+    acc_mac(s[7], dw1, d31);
+    acc_mac(s[1], dw0, X0);
+    acc_mac(s[1], w0, d20);
+    acc_add64(s[1], gl_sub(C2, C0));
+    acc_mac(s[3], e, g);
+    acc_mac(s[4], f, g);
+    acc_mac(s[4], e, h);
+    acc_mac(s[5], f, h);
+}
+
 __global__ void __launch_bounds__(TPB, 2) k_gkr_r01(RoundArgs a) {
     Acc s[8];
 #pragma unroll
@@ -166,11 +276,45 @@ __global__ void __launch_bounds__(TPB, 2) k_gkr_r01(RoundArgs a) {
     const u64* WB = a.t[2].in[0];
     const u64* WC = a.t[3].in[0];
     const u64 tid = (u64)blockIdx.x * TPB + threadIdx.x, stride = (u64)gridDim.x * TPB;
-    for (u64 j = tid; j < Q; j += stride) {
-        const u64 a0 = __ldcs(A + j), a1 = __ldcs(A + j + Q), a2 = __ldcs(A + j + 2 * Q), a3 = __ldcs(A + j + 3 * Q);
-        const u64 m0 = __ldcs(M + j), m1 = __ldcs(M + j + Q), m2 = __ldcs(M + j + 2 * Q), m3 = __ldcs(M + j + 3 * Q);
-        const u64 b = j >> k;
-        gkr01_quad(s, a0, a1, a2, a3, m0, m1, m2, m3, WB[b], WB[b + nq], WB[b + 2 * nq], WB[b + 3 * nq], WC[j & cm]);
+    const u32 gr = gkr_run_len(Q, k);
+    if (gr) {
+        const u32 lane = threadIdx.x & 31;
+        const u64 rl = 32ULL * gr, nruns = Q / rl;
+        for (u64 u = tid >> 5; u < nruns; u += stride >> 5) {
+            const u64 i0 = u * rl;
+            Acc x[4], ca[3];
+#pragma unroll
+            for (int t = 0; t < 4; t++) x[t] = acc_zero();
+#pragma unroll
+            for (int t = 0; t < 3; t++) ca[t] = acc_zero();
+            for (u32 t = 0; t < gr; t += 2) {   // two quadruples: sixteen loads in flight
+                u64 av[2][4], mv[2][4], c[2];
+#pragma unroll
+                for (int h = 0; h < 2; h++) {
+                    const u64 j = i0 + lane + 32 * (t + h);
+#pragma unroll
+                    for (int q = 0; q < 4; q++) { av[h][q] = __ldcs(A + j + q * Q); mv[h][q] = __ldcs(M + j + q * Q); }
+                    c[h] = WC[j & cm];
+                }
+#pragma unroll
+                for (int h = 0; h < 2; h++)
+#pragma unroll
+                    for (int q = 0; q < 4; q++) {
+                        acc_add64(x[q], av[h][q]);
+                        acc_mac(x[q], c[h], mv[h][q]);
+                        if (q < 3) acc_mac(ca[q], c[h], av[h][q]);
+                    }
+            }
+            const u64 b = i0 >> k;
+            gkr01_run(s, x, ca, WB[b], WB[b + nq], WB[b + 2 * nq], WB[b + 3 * nq]);
+        }
+    } else {
+        for (u64 j = tid; j < Q; j += stride) {
+            const u64 a0 = __ldcs(A + j), a1 = __ldcs(A + j + Q), a2 = __ldcs(A + j + 2 * Q), a3 = __ldcs(A + j + 3 * Q);
+            const u64 m0 = __ldcs(M + j), m1 = __ldcs(M + j + Q), m2 = __ldcs(M + j + 2 * Q), m3 = __ldcs(M + j + 3 * Q);
+            const u64 b = j >> k;
+            gkr01_quad(s, a0, a1, a2, a3, m0, m1, m2, m3, WB[b], WB[b + nq], WB[b + 2 * nq], WB[b + 3 * nq], WC[j & cm]);
+        }
     }
     F3 raw[3];
     raw[0] = f3_make(acc_reduce(s[0]), acc_reduce(s[1]), acc_reduce(s[2]));
@@ -185,19 +329,14 @@ __global__ void __launch_bounds__(TPB, 2) k_gkr_r01(RoundArgs a) {
 // k >= 3 -- evaluated on them with W_b folded twice (t[2]) and W_c as is.
 template <bool ECH>
 __global__ void __launch_bounds__(TPB, 2) k_gkr_r2x(RoundArgs a) {
-    constexpr bool EA = ECH, EWB = ECH, EWC = false;
-    ProdAcc<EA, EWB> q0;
-    ProdAcc<EA || EWB, EWB> qc;
-    q0.init();
-    qc.init();
+    constexpr bool EA = ECH, EWB = ECH;
     const F3 r0 = f3_make(a.chal_ptr[0], a.chal_ptr[1], a.chal_ptr[2]);
     const F3 r1 = f3_make(a.chal2_ptr[0], a.chal2_ptr[1], a.chal2_ptr[2]);
     const F3 r01 = f3_mul<ECH, ECH>(r0, r1);
     const u64 Q = a.L >> 2, H = Q >> 1;
     const u32 kc = a.m_shift;
     const u64 cm = (1ULL << kc) - 1;
-    const u64 tid = (u64)blockIdx.x * TPB + threadIdx.x, stride = (u64)gridDim.x * TPB;
-    for (u64 i = tid; i < H; i += stride) {
+    auto gates = [&](u64 i, F3& al, F3& ah, F3& ml, F3& mh) {
         F3 lo[2], hi[2];
 #pragma unroll
         for (int t = 0; t < 2; t++) {
@@ -210,9 +349,12 @@ __global__ void __launch_bounds__(TPB, 2) k_gkr_r2x(RoundArgs a) {
             st<EA>(a.t[t].out, i, lo[t]);
             st<EA>(a.t[t].out, i + H, hi[t]);
         }
-        gkr_pair<EA, EWB, EWC>(q0, qc, a, lo[0], hi[0], lo[1], hi[1], i, H, kc, cm, true);
-    }
-    F3 raw[2] = {q0.result(), qc.result()};
+        al = lo[0]; ah = hi[0]; ml = lo[1]; mh = hi[1];
+    };
+    F3 raw[2];
+    const u32 gr = gkr_run_len(H, kc);
+    if (gr) gkr_runs<EA, EWB>(a, H, kc, cm, gr, raw, gates);
+    else gkr_pairs<EA, EWB, false>(a, H, kc, cm, true, raw, gates);
     reduce_and_finalize_seg<2>(raw, a, POL_GKR, gridDim.x, blockIdx.x);
 }
 

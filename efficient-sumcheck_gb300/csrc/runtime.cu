@@ -342,6 +342,12 @@ int grid_for(u64 work, u64 per_thread = 1) {
     return (int)(g < mg ? g : mg);
 }
 
+// GkrProver passes whose b-variable pairs run in groups sharing one W_b entry
+// (k_gkr.cu): from GKR_RUNS_MIN pairs on, a grid of a quarter of the threads
+// gives each lane a run of four.
+constexpr u64 GKR_RUNS_MIN = 1ULL << 17;
+int gkr_grid(u64 pairs, bool runs) { return grid_for(pairs, runs && pairs >= GKR_RUNS_MIN ? 4 : 1); }
+
 int alloc_buf(effsc_prover* P, Buf& b, size_t cap, bool ext) {
     b.cap = cap;
     b.ext = ext;
@@ -748,7 +754,7 @@ int do_gkr_first(effsc_prover* P, const TxIO& tx0, const TxIO& tx2, const u64* c
     a.L = N;
     a.m_shift = (u32)P->v_l;
     for (int i = 0; i < 4; i++) set_in(a, i, P->t[i]);
-    if (!dry) TRY(timed_launch(s, "gkr_rounds_0_1", 16 * (uint64_t)N + 16 * (uint64_t)n, [&] { return launch_gkr01(a, grid_for(N / 4), s); }));
+    if (!dry) TRY(timed_launch(s, "gkr_rounds_0_1", 16 * (uint64_t)N + 16 * (uint64_t)n, [&] { return launch_gkr01(a, gkr_grid(N / 4, true), s); }));
     // W_b folded by r0, then r1 (the per-round path folds it as rounds 1 and 2 start)
     for (int r = 0; r < 2; r++) {
         Chal c;
@@ -767,7 +773,7 @@ int do_gkr_first(effsc_prover* P, const TxIO& tx0, const TxIO& tx2, const u64* c
     b.chal2_ptr = chals + 3;
     for (int i = 0; i < 4; i++) set_in(b, i, P->t[i]);
     for (int i = 0; i < 2; i++) set_out(b, i, P->t[i].bufs[bi[i]]);
-    if (!dry) TRY(timed_launch(s, "gkr_round_2_double_fold", 16 * (uint64_t)N + 2 * (N / 4) * wbytes(ech), [&] { return launch_gkr2x(ech, b, grid_for(N / 8), s); }));
+    if (!dry) TRY(timed_launch(s, "gkr_round_2_double_fold", 16 * (uint64_t)N + 2 * (N / 4) * wbytes(ech), [&] { return launch_gkr2x(ech, b, gkr_grid(N / 8, true), s); }));
     for (int i = 0; i < 2; i++) {
         Table& T = P->t[i];
         T.cur = bi[i];
@@ -1006,7 +1012,8 @@ int round_gkr(effsc_prover* P, const Chal& ch, const TxIO& tx, bool dry) {
     uint64_t bytes = 2 * (L * wbytes(ea) + (fused ? (L / 2) * wbytes(ea || ech) : 0)) +
                      WB.len * wbytes(ewb) + WC.len * wbytes(ewc);
     if (!dry) TRY(timed_launch(P->ctx->stream, fused ? "gkr_fused_round" : "gkr_evaluate", bytes, [&] {
-        return launch_gkr(fused, ea, ewb, ewc, fused && (ech || ea), a, grid_for(Ln > 1 ? Ln / 2 : 1), P->ctx->stream);
+        const bool runs = !ewc && P->v_l < 64 && ((u64)1 << P->v_l) < Ln;   // a b variable, W_c in the base field
+        return launch_gkr(fused, ea, ewb, ewc, fused && (ech || ea), a, gkr_grid(Ln > 1 ? Ln / 2 : 1, runs), P->ctx->stream);
     }));
     if (fused)
         for (int i = 0; i < 2; i++) {

@@ -121,3 +121,26 @@ def test_gkr_first_rounds_equal_per_round(E, k, field, rounds_of, hook):
     rp, ch, fv = O.sumcheck(orc, rounds, O.Transcript(field, label=b"g01"), hook=hook)
     check(E, x, field, rp, ch, fv)
     assert np.array_equal(p.claimed_w_values(), orc.claimed_w_values()[:, :field])
+
+
+@pytest.mark.parametrize("field", [1, 3])
+def test_gkr_runs_large(E, field):
+    """k = 11: the rounds 0-1 pass, the round-2 pass and rounds 1, 3, 4 of the
+    per-round path are large enough that lanes take runs of pairs sharing one
+    W_b entry; proofs, gate tables after a partial run and claimed W values
+    equal the per-pair forms' (the oracle's)."""
+    k = 11
+    add, mult, w = inputs(k, False, 4242 + field)
+    orc = O.Prover.gkr(field, add, mult, w)
+    rp, ch, fv = O.sumcheck(orc, 2 * k, O.Transcript(field, label=b"runs"))
+    for first in (True, False):
+        g = E.GkrProver(add, mult, w, field=field)
+        g.set_first_rounds(first)
+        check(E, g.prove(2 * k, E.Transcript.keccak(field, b"runs")), field, rp, ch, fv)
+        assert np.array_equal(g.claimed_w_values(), orc.claimed_w_values()[:, :field])
+    part = O.Prover.gkr(field, add, mult, w)
+    O.sumcheck(part, 5, O.Transcript(field, label=b"runs5"))
+    g = E.GkrProver(add, mult, w, field=field)
+    g.prove(5, E.Transcript.keccak(field, b"runs5"))
+    for t in range(2):
+        assert np.array_equal(g.table(t).reshape(-1, field), part.table(t)[:, :field])
