@@ -105,6 +105,29 @@ bool launch_tail_cluster(int pol, int fw, const TailArgs& a, u32 cs_log, cudaStr
 // Largest cluster size the device runs for it (16, 8 or 0).
 u32 tail_cluster_max(void);
 
+// GkrProver tail (k_gkr_tail.cu): add, mult, W_b, W_c in one block's shared
+// memory for the rounds r0 .. r0 + nrounds - 1, then the runner's finalize.
+struct GkrTailArgs {
+    const u64* in[4][3];   // [table][component] current add, mult, W_b, W_c
+    u64* out[4][3];        // the tables after the last fold (null: not written)
+    u64 len[4];            // current lengths (powers of two)
+    u32 in_ext;            // bit t: table t is stored with 3 components
+    u32 nrounds;
+    u32 r0;                // index of the first tail round (W_b folds while the bound variable is < k)
+    u32 k;                 // log2 |w|
+    u32 first_fold;        // 1: the first round folds with chal_in first
+    u32 final_fold;        // 1: the runner's finalize before the tables are written back
+    u32 hook_len;
+    const u64* chal_in;
+    void* tx;              // DevTranscript*
+    const uint8_t* hook;
+    u64* proof_wire;       // round r0's wire values (6 words per round)
+    u64* proof_chal;       // round r0's challenge (3 words per round)
+    u64* first_out;        // (optional) the four tables' first entries, 3 words each
+};
+// Needs 8 * fw * (len[0] + .. + len[3]) bytes <= TAIL_SMEM_CAP.
+bool launch_gkr_tail(int fw, const GkrTailArgs& a, u64 smem_bytes, cudaStream_t s);
+
 // Serving steps: one entry per request in the step, sorted by first_block;
 // `code` = SERVE_IP (else ML) | SERVE_FP3 (else Fp) | phase << SERVE_PHASE_SHIFT.
 struct ServeSeg {

@@ -731,12 +731,81 @@ int do_ml_first(effsc_prover* P, const TxIO& tx0, const TxIO& tx2, const u64* ch
     return EFFSC_OK;
 }
 
+// GkrProver tail: from round r on, the four tables in one block's shared
+// memory (k_gkr_tail.cu) -- the remaining rounds, the finalize and the
+// read-back entries in one launch.  Leaves the state the per-round path and
+// finalize leave.
+bool gkr_tail_ok(const effsc_prover* P, size_t r, size_t num_rounds, const Chal& ch) {
+    if (P->kind != EFFSC_GKR || !P->tail_len || r >= num_rounds || (ch.has && !ch.dev)) return false;
+    if (num_rounds - r > ((size_t)1 << 20) || P->t[0].len > P->tail_len) return false;
+    size_t tot = 0;
+    for (int i = 0; i < 4; i++) {
+        if (!is_pow2(P->t[i].len)) return false;
+        tot += P->t[i].len;
+    }
+    const size_t fw = P->field == EFFSC_FP3 ? 3 : 1;
+    return tot <= TAIL_SMEM_CAP / (8 * fw);
+}
+
+int do_gkr_tail(effsc_prover* P, size_t r, size_t num_rounds, const Chal& ch, const TxIO& tx, bool dry, u64* first) {
+    const int fw = P->field == EFFSC_FP3 ? 3 : 1;
+    const size_t k = P->v_l;
+    GkrTailArgs ta;
+    memset(&ta, 0, sizeof ta);
+    ta.nrounds = (u32)(num_rounds - r);
+    ta.r0 = (u32)r;
+    ta.k = (u32)k;
+    ta.first_fold = ch.has ? 1 : 0;
+    ta.final_fold = 1;
+    ta.chal_in = ch.dev;
+    ta.tx = tx.tx;
+    ta.hook = tx.hook;
+    ta.hook_len = tx.hook_len;
+    ta.proof_wire = tx.proof_wire;
+    ta.proof_chal = tx.proof_chal;
+    ta.first_out = first;
+    // the lengths the folds leave: each round (but a first one without a
+    // challenge) and the finalize fold the gate tables and the witness table
+    // of the variable just bound
+    size_t len[4], tot = 0;
+    for (int i = 0; i < 4; i++) len[i] = P->t[i].len;
+    auto fold_len = [&](size_t var) {
+        for (int i : {0, 1, var < k ? 2 : 3})
+            if (len[i] >= 2) len[i] >>= 1;
+    };
+    for (size_t j = ch.has ? 0 : 1; j < num_rounds - r; j++) fold_len(r + j - 1);
+    fold_len(num_rounds - 1);
+    uint64_t bytes = 0;
+    int bi[4];
+    for (int i = 0; i < 4; i++) {
+        Table& T = P->t[i];
+        for (int c = 0; c < 3; c++) ta.in[i][c] = T.bufs[T.cur].p[c];
+        if (T.ext) ta.in_ext |= 1u << i;
+        ta.len[i] = T.len;
+        tot += T.len;
+        bytes += T.len * wbytes(T.ext) + len[i] * wbytes(fw == 3);
+        TRY(out_buffer(P, T, fw == 3, len[i], true, &bi[i]));
+        for (int c = 0; c < 3; c++) ta.out[i][c] = T.bufs[bi[i]].p[c];
+    }
+    if (!dry) TRY(timed_launch(P->ctx->stream, "gkr_tail", bytes, [&] { return launch_gkr_tail(fw, ta, 8 * fw * tot, P->ctx->stream); }));
+    for (int i = 0; i < 4; i++) {
+        Table& T = P->t[i];
+        T.cur = bi[i];
+        T.len = len[i];
+        T.ext = fw == 3;
+    }
+    P->rounds = num_rounds;
+    return EFFSC_OK;
+}
+
 // effsc_prove of a GkrProver with k >= 3 over base add, mult and witness:
 // rounds 0 and 1 from one pass, round 2 with the folds of add and mult by r0
 // and r1 from a second (k_gkr.cu).  Leaves the state the per-round path
 // leaves after round 2: add and mult folded twice, W_b folded by r0 and r1.
 bool gkr_first_ok(const effsc_prover* P, size_t num_rounds) {
     if (!P->fuse_first || P->kind != EFFSC_GKR || P->rounds != 0 || num_rounds < 3 || P->v_l < 3) return false;
+    Chal none;
+    if (gkr_tail_ok(P, 0, num_rounds, none)) return false;
     const size_t n = (size_t)1 << P->v_l;
     for (int i = 0; i < 4; i++) {
         const Table& T = P->t[i];
@@ -1858,6 +1927,11 @@ int effsc_prove(effsc_prover* P, size_t num_rounds, effsc_transcript* T, const u
             // the read-back gather in its one launch
             if (tail_ok(P, r, num_rounds, ch)) {
                 TRY(do_tail(P, r, num_rounds, ch, tx, dry, 0, true, P->d_first));
+                tail_done = true;
+                break;
+            }
+            if (gkr_tail_ok(P, r, num_rounds, ch)) {
+                TRY(do_gkr_tail(P, r, num_rounds, ch, tx, dry, P->d_first));
                 tail_done = true;
                 break;
             }

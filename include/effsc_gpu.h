@@ -171,8 +171,10 @@ int effsc_prover_read_table(effsc_prover* p, int table, uint64_t* out);
  * max_len long, the remaining rounds run in one launch with the tables in
  * shared memory: one thread block, or (Multilinear, tables up to 16 times
  * one block's capacity, entered mid-proof) a thread-block cluster that hands
- * over to one block.  Default SIZE_MAX: as long as shared memory allows; 0
- * disables.  Proofs are identical. */
+ * over to one block.  A GkrProver's rounds move into one block once add,
+ * mult, W_b and W_c fit in shared memory together and add is at most max_len
+ * long.  Default SIZE_MAX: as long as shared memory allows; 0 disables.
+ * Proofs are identical. */
 int effsc_prover_set_tail(effsc_prover* p, size_t max_len);
 /* effsc_prove only (no reference counterpart; a tuning knob): for an MSB
  * InnerProduct prover over Fp3 challenges or an MSB Multilinear prover with

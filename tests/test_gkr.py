@@ -106,6 +106,8 @@ def test_gkr_first_rounds_equal_per_round(E, k, field, rounds_of, hook):
     p = E.GkrProver(add, mult, w, field=field)
     q = E.GkrProver(add, mult, w, field=field)
     q.set_first_rounds(False)
+    for g in (p, q):
+        g.set_tail(0)         # the one-block tail would take these sizes from round 0
     for use_graph in (True, False):
         p.reset()
         q.reset()
@@ -144,3 +146,32 @@ def test_gkr_runs_large(E, field):
     g.prove(5, E.Transcript.keccak(field, b"runs5"))
     for t in range(2):
         assert np.array_equal(g.table(t).reshape(-1, field), part.table(t)[:, :field])
+
+
+@pytest.mark.parametrize("k", [1, 2, 3, 5, 6, 8])
+@pytest.mark.parametrize("field,ext", [(1, False), (3, False), (3, True)])
+@pytest.mark.parametrize("rounds_of", [lambda k: 1, lambda k: k, lambda k: 2 * k, lambda k: 2 * k + 2])
+def test_gkr_tail_equals_per_round(E, k, field, ext, rounds_of):
+    """The one-block tail (entered at round 0 for small k, mid-proof for
+    k = 8) gives the per-round path's proof, all four tables after the run
+    and claimed W values, and the oracle's proof."""
+    rounds = rounds_of(k)
+    hook = b"\x01\x02\x03" if k % 2 else bytes(range(16))
+    add, mult, w = inputs(k, ext, 1300 + 11 * k + rounds + field + ext)
+    p = E.GkrProver(add, mult, w, field=field)
+    q = E.GkrProver(add, mult, w, field=field)
+    q.set_tail(0)
+    for use_graph in (True, False):
+        p.reset()
+        q.reset()
+        x = p.prove(rounds, E.Transcript.keccak(field, b"gt"), hook=hook, use_graph=use_graph)
+        y = q.prove(rounds, E.Transcript.keccak(field, b"gt"), hook=hook, use_graph=use_graph)
+        assert np.array_equal(x.round_polys, y.round_polys)
+        assert np.array_equal(x.challenges, y.challenges)
+        assert np.array_equal(x.final_value, y.final_value)
+        for t in range(4):
+            assert np.array_equal(p.table(t), q.table(t)), t
+        assert np.array_equal(p.claimed_w_values(), q.claimed_w_values())
+    orc = O.Prover.gkr(field, add, mult, w)
+    rp, ch, fv = O.sumcheck(orc, rounds, O.Transcript(field, label=b"gt"), hook=hook)
+    check(E, x, field, rp, ch, fv)
