@@ -18,8 +18,10 @@
 //   c2 = sum d_w (d_add + d_mult s),
 // d_* the differences across the pair and d_w that of the varying witness
 // table: one product per pair in place of the points x = 1 and x = 2.  With
-// two accumulators every variant fits 128 registers without spills and runs
-// two blocks per SM (measured, k = 12 over Fp3: 0.98 -> 0.90 ms per proof).
+// two accumulators every fused variant fits 128 registers without spills and
+// all run two blocks per SM (measured, k = 12 over Fp3: 0.98 -> 0.90 ms per
+// proof; the evaluate-only variant with every table in Fp3, used on tables of
+// at most two entries, spills 8 bytes).
 #include "ml01.cuh"
 
 namespace effsc {
