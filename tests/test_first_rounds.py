@@ -73,6 +73,34 @@ def test_partial_runs_post_state(E, rounds, order):
     assert np.array_equal(x.final_value, fv)
 
 
+@pytest.mark.parametrize("n", [17, 19])
+@pytest.mark.parametrize("order", ["msb", "lsb"])
+@pytest.mark.parametrize("hook", [b"", b"\x05\x06\x07"])
+def test_large_first_pass(E, n, order, hook):
+    """Tables of 2^17 entries and more (multi-wave grids of the rounds 0-1
+    pass and TMA-staged later rounds): proofs equal the per-round path's and
+    the oracle's, for full and partial runs."""
+    a, b = tables(n, 600 + n + len(hook))
+    cls = E.InnerProductProver if order == "msb" else E.InnerProductProverLSB
+    for rounds in (3, n):
+        p = cls(a, b)
+        q = cls(a, b)
+        q.set_first_rounds(False)
+        x = p.prove(rounds, E.Transcript.keccak(3, b"tma01"), hook=hook)
+        y = q.prove(rounds, E.Transcript.keccak(3, b"tma01"), hook=hook)
+        assert np.array_equal(x.round_polys, y.round_polys)
+        assert np.array_equal(x.challenges, y.challenges)
+        assert np.array_equal(x.final_value, y.final_value)
+        if rounds == 3:
+            for t in range(2):
+                assert np.array_equal(p.table(t), q.table(t))
+    rp, ch, fv = O.sumcheck(O.Prover(O.IP, O.MSB if order == "msb" else O.LSB, 3, [a, b]), n,
+                            O.Transcript(3, label=b"tma01"), hook=hook)
+    assert np.array_equal(x.round_polys, rp)
+    assert np.array_equal(x.challenges, ch)
+    assert np.array_equal(x.final_value, fv)
+
+
 def test_default_path_large(E):
     """n = 20 with the default plan (two-pass start, TMA rounds, tail)."""
     n = 20
