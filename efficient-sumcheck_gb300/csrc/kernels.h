@@ -184,6 +184,9 @@ bool launch_ip2x(bool lsb, const RoundArgs& a, int grid, cudaStream_t s);
 bool launch_ml01(const RoundArgs& a, int grid, cudaStream_t s);
 bool launch_ml2x(bool ech, const RoundArgs& a, int grid, cudaStream_t s);
 bool launch_gkr01(const RoundArgs& a, int grid, cudaStream_t s);
+// The same pass by runs at three blocks per SM: only when each lane gets a run of at least
+// two quadruples inside one W_b entry (grid * TPB / 32 warps, |w| >= 64 * 2).
+bool launch_gkr01_runs(const RoundArgs& a, int grid, cudaStream_t s);
 bool launch_gkr2x(bool ech, const RoundArgs& a, int grid, cudaStream_t s);
 void launch_batch_finalize(const RoundArgs* args, const unsigned char* ext, u32 n, int ntab, u64* finals, cudaStream_t s);
 

@@ -823,7 +823,13 @@ int do_gkr_first(effsc_prover* P, const TxIO& tx0, const TxIO& tx2, const u64* c
     a.L = N;
     a.m_shift = (u32)P->v_l;
     for (int i = 0; i < 4; i++) set_in(a, i, P->t[i]);
-    if (!dry) TRY(timed_launch(s, "gkr_rounds_0_1", 16 * (uint64_t)N + 16 * (uint64_t)n, [&] { return launch_gkr01(a, gkr_grid(N / 4, true), s); }));
+    // large passes: runs of quadruples at three blocks per SM (k_gkr_r01_runs)
+    const int g3 = (int)std::min<u64>((u64)(max_grid() / 8) * 3, (N / 4 + KERNEL_TPB - 1) / KERNEL_TPB);
+    const u64 nw3 = (u64)g3 * KERNEL_TPB / 32;
+    const u64 run3 = std::min<u64>(std::min<u64>((N / 4) / (32 * nw3), 16), (u64)n >> 5);
+    if (!dry) TRY(timed_launch(s, "gkr_rounds_0_1", 16 * (uint64_t)N + 16 * (uint64_t)n, [&] {
+        return run3 >= 2 ? launch_gkr01_runs(a, g3, s) : launch_gkr01(a, gkr_grid(N / 4, true), s);
+    }));
     // W_b folded by r0, then r1 (the per-round path folds it as rounds 1 and 2 start)
     for (int r = 0; r < 2; r++) {
         Chal c;
