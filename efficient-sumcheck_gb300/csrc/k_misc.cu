@@ -2,6 +2,8 @@
 // representation conversion at the boundary, eq-table construction).
 #include "round_common.cuh"
 
+#include <atomic>
+
 namespace effsc {
 
 bool launch_eval_mlip(int pol, int sem, u32 mask, const RoundArgs& a, int grid, cudaStream_t s);
@@ -9,12 +11,23 @@ bool launch_fused_mlip(int pol, int sem, u32 mask, bool ech, const RoundArgs& a,
 bool launch_eval_coef(int pol, int sem, u32 mask, const RoundArgs& a, int grid, cudaStream_t s);
 bool launch_fused_coef(int pol, int sem, u32 mask, bool ech, const RoundArgs& a, int grid, cudaStream_t s);
 
-static int g_sms = 0;
+// SM count per device, read once per device (the attribute never changes, so
+// concurrent first reads store the same value).  Grids are sized for the
+// device current on the calling thread.
+constexpr int SMS_MAX_DEVICES = 64;
+static std::atomic<int> g_sms[SMS_MAX_DEVICES];
 
-void kernels_init(int device) {
-    cudaDeviceGetAttribute(&g_sms, cudaDevAttrMultiProcessorCount, device);
-    if (g_sms <= 0) g_sms = 1;
+static int sms_of(int device) {
+    if (device < 0 || device >= SMS_MAX_DEVICES) return 1;
+    int v = g_sms[device].load(std::memory_order_relaxed);
+    if (v <= 0) {
+        if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, device) != cudaSuccess || v <= 0) v = 1;
+        g_sms[device].store(v, std::memory_order_relaxed);
+    }
+    return v;
 }
+
+void kernels_init(int device) { sms_of(device); }
 __global__ void k_gather_first(FirstSrc src, u64* dst) {
     const int i = threadIdx.x;
     if (i < 12) {
@@ -24,7 +37,11 @@ __global__ void k_gather_first(FirstSrc src, u64* dst) {
 }
 void launch_gather_first(const FirstSrc& src, u64* dst, cudaStream_t s) { k_gather_first<<<1, 32, 0, s>>>(src, dst); }
 
-int max_grid(void) { return (g_sms > 0 ? g_sms : 1) * 8; }
+int max_grid(void) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) dev = 0;
+    return sms_of(dev) * 8;
+}
 
 int pol_ntables(int pol) {
     switch (pol) {

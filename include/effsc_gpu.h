@@ -176,13 +176,16 @@ int effsc_prover_read_table(effsc_prover* p, int table, uint64_t* out);
  * long.  Default SIZE_MAX: as long as shared memory allows; 0 disables.
  * Proofs are identical. */
 int effsc_prover_set_tail(effsc_prover* p, size_t max_len);
-/* effsc_prove only (no reference counterpart; a tuning knob): for an MSB
- * InnerProduct prover over Fp3 challenges or an MSB Multilinear prover with
- * power-of-two base tables, and for a GkrProver with |w| >= 8 over base
- * add, mult and w, compute rounds 0-2 in two passes over the base tables
- * (round 1 from sums gathered during round 0; round 2 folds with both
- * challenges).  Default 1; 0 runs one pass per round.  Proofs are
- * identical. */
+/* effsc_prove only (no reference counterpart; a tuning knob): for an
+ * InnerProduct prover (MSB or LSB) over Fp3 challenges or an MSB Multilinear
+ * prover with power-of-two base tables, and for a GkrProver with |w| >= 8
+ * over base add, mult and w, fused = 1 computes rounds 0-2 in two passes over
+ * the base tables (round 1 from sums gathered during round 0; round 2 folds
+ * with both challenges).  fused = 2 (the default) does the same and, for an
+ * InnerProduct prover with base tables of 2^14 entries or more and at least
+ * 4 rounds, computes rounds 0-3 in two passes instead (rounds 0-2 from 26
+ * interpolation sums of one pass; round 3 folds with three challenges).
+ * 0 runs one pass per round.  Proofs are identical. */
 int effsc_prover_set_first_rounds(effsc_prover* p, int fused);
 
 /* Restore the state right after construction (the input tables are never
@@ -390,8 +393,10 @@ int effsc_server_run_trace(effsc_server* s, size_t n, const int* kinds, int fiel
  * sharing a stream with latency-critical kernels that a synchronising
  * cudaMalloc/cudaFree would stall): one InnerProductProver (MSB) round on the
  * caller's device buffers -- challenge == NULL evaluates round 0 on a, b
- * (len >= 1); otherwise folds a, b with *challenge (3 canonical words, Fp3) and
- * evaluates the next round (len a power of two >= 4).  a, b: Fp3 tables of len
+ * (len >= 1); otherwise folds a, b with *challenge and evaluates the next
+ * round (len a power of two >= 4).  challenge points to 3 words in HOST
+ * memory (one Fp3 element, read before the call returns; words >= p are
+ * reduced mod p).  a, b: Fp3 tables of len
  * elements in structure-of-arrays form (c0[len], c1[len], c2[len], canonical);
  * the folded tables go to the first len/2 entries of each component array of
  * a_out, b_out (same component stride len; a_out == a works in place).

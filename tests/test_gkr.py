@@ -175,3 +175,17 @@ def test_gkr_tail_equals_per_round(E, k, field, ext, rounds_of):
     orc = O.Prover.gkr(field, add, mult, w)
     rp, ch, fv = O.sumcheck(orc, rounds, O.Transcript(field, label=b"gt"), hook=hook)
     check(E, x, field, rp, ch, fv)
+
+
+def test_gkr_runs_k12_fp3(E):
+    """k = 12 over Fp3 challenges with base gate tables (the bench size): the
+    grid gives every lane four pairs, so the b-variable passes group runs of
+    up to 16 pairs per W_b entry (g = 4..16) -- sizes the k = 11 case does
+    not reach.  The proof and claimed W values equal the oracle's."""
+    k = 12
+    add, mult, w = inputs(k, False, 1212)
+    orc = O.Prover.gkr(3, add, mult, w)
+    rp, ch, fv = O.sumcheck(orc, 2 * k, O.Transcript(3, label=b"k12"))
+    g = E.GkrProver(add, mult, w, field=3)
+    check(E, g.prove(2 * k, E.Transcript.keccak(3, b"k12")), 3, rp, ch, fv)
+    assert np.array_equal(g.claimed_w_values(), orc.claimed_w_values())
