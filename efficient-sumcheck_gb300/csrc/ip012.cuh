@@ -1,0 +1,330 @@
+// ip012.cuh -- InnerProduct rounds 0-3 of an MSB or LSB proof over Fp3
+// challenges in two passes over the base tables.
+//
+// Write an octet of a table as v(t0, t1, t2), t_i the variable bound in round
+// i (MSB: entry m + (4 t0 + 2 t1 + t2) L/8; LSB: entry 8m + t0 + 2 t1 + 4 t2),
+// and A(u, v; t2) = v(0,0,t2) + u dA + v eA + u v fA the bilinear form whose
+// value at (r0, r1) is the entry after the folds with r0 and r1
+// (src/inner_product_sumcheck.rs:143-176 applied twice).
+//   round 0: q0 = sum v(0,t1,t2) w(0,t1,t2), qinf = sum of the t0 differences
+//            (src/provers/inner_product.rs:94-103);
+//   round 1: sum_t2 A(r0, 0; t2) B(r0, 0; t2) and sum_t2 A(r0, inf; t2) B(...)
+//            are quadratics in r0;
+//   round 2: A(r0, r1; 0) B(r0, r1; 0) and the product of the t2 differences
+//            are biquadratic in (r0, r1).
+// A quadratic is fixed by its values at 0, 1 and its leading coefficient
+// ("inf"), a biquadratic by its values on {0, 1, inf}^2, and the value of a
+// product of two bilinear forms at such a point is the product of the
+// forms' values there (leading coefficients multiply).  So one pass
+// accumulates 26 base-field sums, each one product per octet
+// (ip012_sums), and the last block interpolates all three rounds' wire
+// values at the challenges as it runs the three transcript steps
+// (finalize_ip012).  The second pass folds every octet with r0, r1, r2 at
+// once -- the multilinear form sum_s D_s prod_{i in s} r_i with D_s the
+// octet's finite differences, 7 base x Fp3 products per component --
+// writes the Fp3 tables of length L/8 and evaluates round 3 on them.
+// Against the two-pass start of rounds 0-2 this skips writing and
+// re-reading the length-L/4 Fp3 tables (24 bytes per entry of L).
+#pragma once
+#include "ip01.cuh"
+
+namespace effsc {
+
+constexpr int IP012_WORDS = 26;   // base-field sums of the first pass
+constexpr int IP012_G1 = 14;      // sums of the first warp group (0..13), the rest in the second
+
+// Sums (grid point index g = 3 u + v, u, v in {0, 1, inf}):
+//   0..8   P0[g]  = sum A(u,v;0) B(u,v;0)
+//   9..11  R1a[u] = sum A(u,0;1) B(u,0;1)
+//   12     R0a    = sum A(0,1;1) B(0,1;1)
+//   13     R0b    = sum A(inf,1;1) B(inf,1;1)
+//   14..22 Pd[g]  = sum dA(u,v) dB(u,v), dA = A(.,.;1) - A(.,.;0)
+//   23..25 R1b[u] = sum A(u,inf;1) B(u,inf;1)
+// Values of one table's octet are v[4 t0 + 2 t1 + t2].
+template <int GROUP>
+__device__ __forceinline__ void ip012_sums(Acc* s, const u64 (&x)[8], const u64 (&y)[8]) {
+    if (GROUP == 0) {
+        // t2 = 0 grid: (0,0) (0,1) (0,inf) (1,0) (1,1) (1,inf) (inf,0) (inf,1) (inf,inf)
+        const u64 xa = gl_sub(x[4], x[0]), ya = gl_sub(y[4], y[0]);     // (inf, 0)
+        const u64 xb = gl_sub(x[6], x[2]), yb = gl_sub(y[6], y[2]);     // (inf, 1)
+        const u64 xc = gl_sub(x[2], x[0]), yc = gl_sub(y[2], y[0]);     // (0, inf)
+        const u64 xd = gl_sub(x[6], x[4]), yd = gl_sub(y[6], y[4]);     // (1, inf)
+        const u64 xe = gl_sub(xd, xc), ye = gl_sub(yd, yc);             // (inf, inf)
+        acc_mac(s[0], x[0], y[0]);
+        acc_mac(s[1], x[2], y[2]);
+        acc_mac(s[2], xc, yc);
+        acc_mac(s[3], x[4], y[4]);
+        acc_mac(s[4], x[6], y[6]);
+        acc_mac(s[5], xd, yd);
+        acc_mac(s[6], xa, ya);
+        acc_mac(s[7], xb, yb);
+        acc_mac(s[8], xe, ye);
+        // t2 = 1 at v = 0 (u = 0, 1, inf), at (0, 1) and at (inf, 1)
+        acc_mac(s[9], x[1], y[1]);
+        acc_mac(s[10], x[5], y[5]);
+        acc_mac(s[11], gl_sub(x[5], x[1]), gl_sub(y[5], y[1]));
+        acc_mac(s[12], x[3], y[3]);
+        acc_mac(s[13], gl_sub(x[7], x[3]), gl_sub(y[7], y[3]));
+    } else {
+        // t2 differences on the grid
+        const u64 p00 = gl_sub(x[1], x[0]), q00 = gl_sub(y[1], y[0]);
+        const u64 p01 = gl_sub(x[3], x[2]), q01 = gl_sub(y[3], y[2]);
+        const u64 p10 = gl_sub(x[5], x[4]), q10 = gl_sub(y[5], y[4]);
+        const u64 p11 = gl_sub(x[7], x[6]), q11 = gl_sub(y[7], y[6]);
+        const u64 p0i = gl_sub(p01, p00), q0i = gl_sub(q01, q00);
+        const u64 p1i = gl_sub(p11, p10), q1i = gl_sub(q11, q10);
+        acc_mac(s[0], p00, q00);
+        acc_mac(s[1], p01, q01);
+        acc_mac(s[2], p0i, q0i);
+        acc_mac(s[3], p10, q10);
+        acc_mac(s[4], p11, q11);
+        acc_mac(s[5], p1i, q1i);
+        acc_mac(s[6], gl_sub(p10, p00), gl_sub(q10, q00));
+        acc_mac(s[7], gl_sub(p11, p01), gl_sub(q11, q01));
+        acc_mac(s[8], gl_sub(p1i, p0i), gl_sub(q1i, q0i));
+        // t2 = 1 at v = inf (u = 0, 1, inf)
+        const u64 e0 = gl_sub(x[3], x[1]), f0 = gl_sub(y[3], y[1]);
+        const u64 e1 = gl_sub(x[7], x[5]), f1 = gl_sub(y[7], y[5]);
+        acc_mac(s[9], e0, f0);
+        acc_mac(s[10], e1, f1);
+        acc_mac(s[11], gl_sub(e1, e0), gl_sub(f1, f0));
+    }
+}
+
+// Octet m of a base table in the v[4 t0 + 2 t1 + t2] order.
+template <bool LSB>
+__device__ __forceinline__ void load_octet(u64 (&v)[8], const u64* X, u64 m, u64 O) {
+    if (LSB) {
+        // entries 8m .. 8m+7: v[4 t0 + 2 t1 + t2] = e[t0 + 2 t1 + 4 t2]
+        const ulonglong2* X2 = (const ulonglong2*)X + 4 * m;
+        const ulonglong2 e01 = X2[0], e23 = X2[1], e45 = X2[2], e67 = X2[3];
+        v[0] = e01.x; v[4] = e01.y; v[2] = e23.x; v[6] = e23.y;
+        v[1] = e45.x; v[5] = e45.y; v[3] = e67.x; v[7] = e67.y;
+    } else {
+#pragma unroll
+        for (int j = 0; j < 8; j++) v[j] = X[m + j * O];
+    }
+}
+
+// Pass 1.  Warps 0..3 of a block accumulate sums 0..13 and warps 4..7 sums
+// 14..25 of the same octets (13-14 accumulators per thread instead of 26);
+// the second group's loads of an octet hit what the first group's brought
+// into the caches.  The last block interpolates and runs rounds 0-2.
+static __device__ __noinline__ void finalize_ip012(const u64* S, const RoundArgs& a);
+
+template <bool LSB>
+__device__ __forceinline__ void ip012_body(const RoundArgs& a, u32 bid, u32 nb) {
+    constexpr int HALF = TPB / 2;
+    const int group = threadIdx.x >= HALF;
+    Acc s[IP012_G1];
+#pragma unroll
+    for (int i = 0; i < IP012_G1; i++) s[i] = acc_zero();
+    const u64 O = a.L >> 3;
+    const u64* A = a.t[0].in[0];
+    const u64* B = a.t[1].in[0];
+    const u64 stride = (u64)nb * HALF;
+    for (u64 m = (u64)bid * HALF + (threadIdx.x & (HALF - 1)); m < O; m += stride) {
+        u64 x[8], y[8];
+        load_octet<LSB>(x, A, m, O);
+        load_octet<LSB>(y, B, m, O);
+        if (group == 0) ip012_sums<0>(s, x, y);
+        else ip012_sums<1>(s, x, y);
+    }
+    // block reduction: each warp reduces its group's words, then the block's
+    // 26 words go to the partials; the last block to finish finalises
+    __shared__ u64 s_red[NWARP][IP012_G1];
+    __shared__ u64 s_fin[NWARP][32];
+    __shared__ u64 s_tot[32];
+    __shared__ int s_last;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int nw = group == 0 ? IP012_G1 : IP012_WORDS - IP012_G1;
+#pragma unroll
+    for (int i = 0; i < IP012_G1; i++) {
+        if (i < nw) {
+            u64 v = acc_reduce(s[i]);
+#pragma unroll
+            for (int off = 16; off; off >>= 1) v = gl_add(v, __shfl_down_sync(0xffffffffu, v, off));
+            if (lane == 0) s_red[warp][i] = v;
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x < IP012_WORDS) {
+        const int g = threadIdx.x < IP012_G1 ? 0 : 1, i = threadIdx.x - g * IP012_G1;
+        u64 v = 0;
+#pragma unroll
+        for (int w = 0; w < NWARP / 2; w++) v = gl_add(v, s_red[g * (NWARP / 2) + w][i]);
+        if (nb == 1) s_tot[threadIdx.x] = v;
+        else a.partials[(u64)bid * 32 + threadIdx.x] = v;
+    }
+    if (nb > 1) {
+        __threadfence();
+        __syncthreads();
+        if (threadIdx.x == 0) s_last = atomicAdd(a.counter, 1u) == nb - 1;
+        __syncthreads();
+        if (!s_last) return;
+        __threadfence();
+        // thread t sums word t % 32 over the blocks t / 32, t / 32 + 8, ...
+        const int wd = threadIdx.x & 31, part = threadIdx.x >> 5;
+        u64 v = 0;
+        if (wd < IP012_WORDS)
+            for (u32 b = part; b < nb; b += NWARP) v = gl_add(v, __ldcg(&a.partials[(u64)b * 32 + wd]));
+        s_fin[part][wd] = v;
+        __syncthreads();
+        if (threadIdx.x < IP012_WORDS) {
+            u64 t = 0;
+#pragma unroll
+            for (int p = 0; p < NWARP; p++) t = gl_add(t, s_fin[p][threadIdx.x]);
+            s_tot[threadIdx.x] = t;
+        }
+        if (threadIdx.x == 0) *a.counter = 0;
+    }
+    __syncthreads();
+    if (warp == 0) finalize_ip012(s_tot, a);
+}
+
+// q(r) of the quadratic with q(0) = s0, q(1) = s1 and leading coefficient
+// sinf: s0 + r (s1 - s0 - sinf) + r^2 sinf.
+__device__ __forceinline__ F3 quad_at(const F3& s0, const F3& s1, const F3& sinf, const F3& r) {
+    const F3 c1 = f3_sub<true>(f3_sub<true>(s1, s0), sinf);
+    return f3_add<true>(f3_mul<true, true>(f3_add<true>(f3_mul<true, true>(sinf, r), c1), r), s0);
+}
+__device__ __forceinline__ F3 quad_base(u64 s0, u64 s1, u64 sinf, const F3& r) {
+    return quad_at(f3_make(s0, 0, 0), f3_make(s1, 0, 0), f3_make(sinf, 0, 0), r);
+}
+// The biquadratic with values G[3u + v] on {0, 1, inf}^2 at (r0, r1).
+__device__ __forceinline__ F3 biquad_at(const u64* G, const F3& r0, const F3& r1) {
+    F3 g[3];
+#pragma unroll
+    for (int v = 0; v < 3; v++) g[v] = quad_base(G[v], G[3 + v], G[6 + v], r0);
+    return quad_at(g[0], g[1], g[2], r1);
+}
+
+// Rounds 0, 1, 2 from the 26 sums: for each, the wire [q0, qinf], the hook,
+// the challenge (src/runner.rs:39-55).  Run by warp 0 of the last block.
+static __device__ __noinline__ void finalize_ip012(const u64* S, const RoundArgs& a) {
+    __shared__ u64 s_w[3][6];
+    __shared__ u64 s_c[3][3];
+    __shared__ __align__(8) uint8_t s_scr[64];
+    const int lane = threadIdx.x & 31;
+    if (lane == 0) {
+        s_w[0][0] = gl_add(gl_add(S[0], S[1]), gl_add(S[9], S[12]));
+        s_w[0][1] = 0; s_w[0][2] = 0;
+        s_w[0][3] = gl_add(gl_add(S[6], S[7]), gl_add(S[11], S[13]));
+        s_w[0][4] = 0; s_w[0][5] = 0;
+    }
+    __syncwarp();
+    DevTranscript* T = (DevTranscript*)a.tx.tx;
+    WarpTx w = tx_load(T, lane);
+    for (int rd = 0; rd < 3; rd++) {
+        if (rd > 0 && lane == 0) {
+            const F3 r0 = f3_make(s_c[0][0], s_c[0][1], s_c[0][2]);
+            F3 q0, qi;
+            if (rd == 1) {
+                q0 = quad_base(gl_add(S[0], S[9]), gl_add(S[3], S[10]), gl_add(S[6], S[11]), r0);
+                qi = quad_base(gl_add(S[2], S[23]), gl_add(S[5], S[24]), gl_add(S[8], S[25]), r0);
+            } else {
+                const F3 r1 = f3_make(s_c[1][0], s_c[1][1], s_c[1][2]);
+                q0 = biquad_at(S, r0, r1);
+                qi = biquad_at(S + 14, r0, r1);
+            }
+            s_w[rd][0] = q0.c0; s_w[rd][1] = q0.c1; s_w[rd][2] = q0.c2;
+            s_w[rd][3] = qi.c0; s_w[rd][4] = qi.c1; s_w[rd][5] = qi.c2;
+        }
+        __syncwarp();
+        tx_send_elems(w, lane, s_w[rd], 2);
+        if (a.tx.hook_len) {
+            const uint8_t* hk = a.tx.hook;
+            tx_absorb(w, lane, a.tx.hook_len, [&](u32 k) -> uint8_t { return hk[k]; });
+        }
+        tx_challenge(w, lane, s_c[rd], s_scr);
+    }
+    tx_store(T, w, lane);
+    if (lane < 18) a.tx.proof_wire[lane] = s_w[lane / 6][lane % 6];
+    if (lane < 9) a.tx.proof_chal[lane] = s_c[lane / 3][lane % 3];
+}
+
+// Pass 2.  The octet's entry after the folds with r0, r1, r2:
+//   D_000 + sum_{s != 0} D_s K_s,  K_s = prod_{i in s} r_i,
+// D_s the finite differences of the octet (three butterfly levels of base
+// subtractions); 7 products per component into three accumulators and
+// three reductions.  K[j] belongs to the difference at index j of the
+// v[4 t0 + 2 t1 + t2] order (bit 2: r0, bit 1: r1, bit 0: r2).
+struct Fold3K {
+    F3 k[8];   // k[0] unused
+};
+__device__ __forceinline__ Fold3K fold3_prepare(const F3& r0, const F3& r1, const F3& r2) {
+    Fold3K K;
+    K.k[0] = f3_make(1, 0, 0);
+    K.k[4] = r0;
+    K.k[2] = r1;
+    K.k[1] = r2;
+    K.k[6] = f3_mul<true, true>(r0, r1);
+    K.k[5] = f3_mul<true, true>(r0, r2);
+    K.k[3] = f3_mul<true, true>(r1, r2);
+    K.k[7] = f3_mul<true, true>(K.k[6], r2);
+    return K;
+}
+__device__ __forceinline__ F3 fold3(u64 (&v)[8], const Fold3K& K) {
+#pragma unroll
+    for (int j = 4; j < 8; j++) v[j] = gl_sub(v[j], v[j - 4]);
+#pragma unroll
+    for (int j = 0; j < 8; j++)
+        if (j & 2) v[j] = gl_sub(v[j], v[j - 2]);
+#pragma unroll
+    for (int j = 0; j < 8; j++)
+        if (j & 1) v[j] = gl_sub(v[j], v[j - 1]);
+    Acc c0 = acc_from(v[0]), c1 = acc_zero(), c2 = acc_zero();
+#pragma unroll
+    for (int j = 1; j < 8; j++) {
+        acc_mac(c0, v[j], K.k[j].c0);
+        acc_mac(c1, v[j], K.k[j].c1);
+        acc_mac(c2, v[j], K.k[j].c2);
+    }
+    return f3_make(acc_reduce(c0), acc_reduce(c1), acc_reduce(c2));
+}
+
+// MSB: lane item m < O/2 (O = L/8) folds octets m and m + O/2 of both tables
+// into entries m and m + O/2 of the Fp3 tables of length O -- round 3's pair.
+// LSB: lane item k folds octets 2k and 2k+1 (entries 16k .. 16k+15) into the
+// pair (2k, 2k+1).
+template <bool LSB>
+__device__ __forceinline__ void ip3x_body(const RoundArgs& a, u32 bid, u32 nb) {
+    using P = Policy<POL_IP, 3>;
+    P acc;
+    acc.init();
+    const Fold3K K = fold3_prepare(f3_make(a.chal_ptr[0], a.chal_ptr[1], a.chal_ptr[2]),
+                                   f3_make(a.chal_ptr[3], a.chal_ptr[4], a.chal_ptr[5]),
+                                   f3_make(a.chal_ptr[6], a.chal_ptr[7], a.chal_ptr[8]));
+    const u64 O = a.L >> 3, H = O >> 1;
+    const u64 tid = (u64)bid * TPB + threadIdx.x, stride = (u64)nb * TPB;
+    F3 lo[2], hi[2];
+    for (u64 m = tid; m < H; m += stride) {
+#pragma unroll
+        for (int t = 0; t < 2; t++) {
+            u64 x[8], y[8];
+            if (LSB) {
+                load_octet<true>(x, a.t[t].in[0], 2 * m, O);
+                load_octet<true>(y, a.t[t].in[0], 2 * m + 1, O);
+            } else {
+                load_octet<false>(x, a.t[t].in[0], m, O);
+                load_octet<false>(y, a.t[t].in[0], m + H, O);
+            }
+            lo[t] = fold3(x, K);
+            hi[t] = fold3(y, K);
+            if (LSB) {
+                ((ulonglong2*)a.t[t].out[0])[m] = make_ulonglong2(lo[t].c0, hi[t].c0);
+                ((ulonglong2*)a.t[t].out[1])[m] = make_ulonglong2(lo[t].c1, hi[t].c1);
+                ((ulonglong2*)a.t[t].out[2])[m] = make_ulonglong2(lo[t].c2, hi[t].c2);
+            } else {
+                st<true>(a.t[t].out, m, lo[t]);
+                st<true>(a.t[t].out, m + H, hi[t]);
+            }
+        }
+        acc.pair(lo, hi);
+    }
+    F3 raw[2];
+    acc.result(raw);
+    reduce_and_finalize_seg<2>(raw, a, POL_IP, nb, bid);
+}
+
+}  // namespace effsc

@@ -181,6 +181,13 @@ bool launch_gkr(bool fused, bool ea, bool ewb, bool ewc, bool ech, const RoundAr
 // fold-twice-and-evaluate from a second read (launch_ip2x).
 bool launch_ip01(bool lsb, const RoundArgs& a, int grid, cudaStream_t s);
 bool launch_ip2x(bool lsb, const RoundArgs& a, int grid, cudaStream_t s);
+// InnerProduct rounds 0-3 in two passes (k_ip012.cu): rounds 0, 1 and 2 from
+// 26 base-field sums of one read of the tables (launch_ip012; partials of 32
+// words per block, grid at most max_grid() * 3 / 8 blocks), then the fold with r0,
+// r1, r2 at once and round 3 from a second read (launch_ip3x; a.chal_ptr
+// holds r0, r1, r2 as 9 consecutive words).
+bool launch_ip012(bool lsb, const RoundArgs& a, int grid, cudaStream_t s);
+bool launch_ip3x(bool lsb, const RoundArgs& a, int grid, cudaStream_t s);
 bool launch_ml01(const RoundArgs& a, int grid, cudaStream_t s);
 bool launch_ml2x(bool ech, const RoundArgs& a, int grid, cudaStream_t s);
 bool launch_gkr01(const RoundArgs& a, int grid, cudaStream_t s);

@@ -293,9 +293,11 @@ struct effsc_prover {
     // effsc_prove: tables of at most this length finish in the one-block tail
     // kernel (SIZE_MAX: as large as shared memory allows; 0: never)
     size_t tail_len = SIZE_MAX;
-    // effsc_prove: InnerProduct rounds 0-2 in two passes (k_ip01.cu);
-    // EqFactored left phase from the inner sums (k_eqf.cu)
-    bool fuse_first = true;
+    // effsc_prove: 0 = one pass per round; 1 = InnerProduct rounds 0-2 in
+    // two passes (k_ip01.cu), the Multilinear and GkrProver starts, the
+    // EqFactored left phase from the inner sums (k_eqf.cu); 2 = as 1, with
+    // InnerProduct rounds 0-3 in two passes (k_ip012.cu) where they apply
+    int fuse_first = 2;
     u64* eqf_scratch = nullptr;               // inner sums, eq weights, partial sums
     size_t eqf_cap = 0;
     // effsc_prove outputs: pinned staging (wire | challenges | transcript |
@@ -659,6 +661,46 @@ bool fuse_first_ok(const effsc_prover* P, size_t num_rounds) {
             if (((uintptr_t)P->t[i].bufs[0].p[0] & 15) != 0) return false;
     Chal none;
     return !tail_ok(P, 0, num_rounds, none);
+}
+
+// Rounds 0-3 in two passes (k_ip012.cu) from num_vars = 14 on (below, the
+// one-block tail takes the proof within a few rounds): leaves the state the
+// per-round path leaves after round 3.
+constexpr size_t FUSE3_MIN_LEN = 1 << 14;
+bool fuse3_ok(const effsc_prover* P, size_t num_rounds) {
+    if (P->fuse_first < 2 || num_rounds < 4 || !fuse_first_ok(P, num_rounds)) return false;
+    return P->t[0].len >= FUSE3_MIN_LEN;
+}
+
+int do_fuse3(effsc_prover* P, const TxIO& tx0, const TxIO& tx3, const u64* chals, bool dry) {
+    const size_t L = P->t[0].len;
+    const bool lsb = P->order == EFFSC_LSB;
+    RoundArgs a = base_args(P);
+    a.tx = tx0;
+    a.L = L;
+    for (int i = 0; i < 2; i++) set_in(a, i, P->t[i]);
+    // a block takes 128 octets per step; one wave of two blocks per SM at most
+    // (the partials hold 32 words for each of them)
+    const int g1 = std::min<int>(grid_for(L / 8, 2), (max_grid() / 8) * 2);
+    if (!dry) TRY(timed_launch(P->ctx->stream, "ip_rounds_0_2", 16 * (uint64_t)L, [&] { return launch_ip012(lsb, a, g1, P->ctx->stream); }));
+    int bi[2];
+    for (int i = 0; i < 2; i++) TRY(out_buffer(P, P->t[i], true, L / 8, true, &bi[i]));
+    RoundArgs b = base_args(P);
+    b.tx = tx3;
+    b.L = L;
+    b.chal_ptr = chals;
+    for (int i = 0; i < 2; i++) {
+        set_in(b, i, P->t[i]);
+        set_out(b, i, P->t[i].bufs[bi[i]]);
+    }
+    if (!dry) TRY(timed_launch(P->ctx->stream, "ip_round_3_triple_fold", 16 * (uint64_t)L + 6 * (uint64_t)L, [&] { return launch_ip3x(lsb, b, grid_for(L / 16), P->ctx->stream); }));
+    for (int i = 0; i < 2; i++) {
+        Table& T = P->t[i];
+        T.cur = bi[i];
+        T.len = L / 8;
+        T.ext = true;
+    }
+    return EFFSC_OK;
 }
 
 int do_fuse_first(effsc_prover* P, const TxIO& tx0, const TxIO& tx2, const u64* chals, bool dry) {
@@ -1802,8 +1844,9 @@ int effsc_diag_bounded_wait(effsc_ctx* ctx, uint64_t limit_ns, int arrive, uint3
 
 int effsc_prover_set_first_rounds(effsc_prover* P, int fused) {
     if (!P) return fail(EFFSC_INVALID_ARG, "prover is NULL");
-    if ((fused != 0) != P->fuse_first && P->gexec) { cudaGraphExecDestroy(P->gexec); P->gexec = nullptr; }
-    P->fuse_first = fused != 0;
+    const int level = fused < 0 ? 0 : fused > 2 ? 2 : fused;
+    if (level != P->fuse_first && P->gexec) { cudaGraphExecDestroy(P->gexec); P->gexec = nullptr; }
+    P->fuse_first = level;
     return EFFSC_OK;
 }
 
@@ -1869,7 +1912,20 @@ int effsc_prove(effsc_prover* P, size_t num_rounds, effsc_transcript* T, const u
     auto launch_all = [&](bool dry) -> int {
         size_t r0 = 0;
         bool tail_done = false;
-        if (fuse_first_ok(P, num_rounds)) {
+        if (fuse3_ok(P, num_rounds)) {
+            TxIO t0, t3;
+            memset(&t0, 0, sizeof t0);
+            t0.tx = P->d_tx;
+            t0.hook = P->d_hook;
+            t0.hook_len = (u32)hook_len;
+            t3 = t0;
+            t0.proof_wire = P->d_wire;
+            t0.proof_chal = P->d_chals;
+            t3.proof_wire = P->d_wire + (size_t)3 * 3 * d;
+            t3.proof_chal = P->d_chals + 3 * 3;
+            TRY(do_fuse3(P, t0, t3, P->d_chals, dry));
+            r0 = 4;
+        } else if (fuse_first_ok(P, num_rounds)) {
             TxIO t0, t2;
             memset(&t0, 0, sizeof t0);
             t0.tx = P->d_tx;

@@ -277,9 +277,13 @@ class _Prover:
         check(load().effsc_prover_reset(self.h))
 
     def set_first_rounds(self, fused):
-        """prove(): rounds 0-2 of an InnerProduct, Multilinear or GkrProver
-        proof in two passes over the base tables (True) or three."""
-        check(load().effsc_prover_set_first_rounds(self.h, 1 if fused else 0))
+        """prove(): how the first rounds read the base tables.  False / 0: one
+        pass per round; 1: rounds 0-2 of an InnerProduct, Multilinear or
+        GkrProver proof in two passes; True / 2 (the default): as 1, and
+        rounds 0-3 of an InnerProduct proof in two passes where they apply
+        (Fp3 challenges, power-of-two base tables of 2^14 entries or more)."""
+        level = 2 if fused is True else 0 if fused is False else int(fused)
+        check(load().effsc_prover_set_first_rounds(self.h, level))
 
     def set_tail(self, max_len):
         """prove(): tables of at most max_len entries finish in the one-block

@@ -189,3 +189,57 @@ def test_ml_partial_post_state(E, rounds, field):
     assert np.array_equal(np.asarray(pf.round_polys).reshape(rounds, 1, field), rp[:, :1, :field])
     got = np.asarray(p.table(0)).reshape(-1, field)
     assert np.array_equal(got, orc.table(0)[:, :field])
+
+
+# ---- InnerProduct rounds 0-3 in two passes (26 interpolation sums, triple fold) ----
+@pytest.mark.parametrize("n", [14, 15, 17, 19])
+@pytest.mark.parametrize("order", ["msb", "lsb"])
+@pytest.mark.parametrize("hook", [b"", b"\x05\x06\x07", bytes(range(32))])
+def test_rounds_0_3_two_passes(E, n, order, hook):
+    """The three-round start gives the two-pass start's and the per-round
+    path's proofs and post-state tables (full and partial runs, graph and
+    direct launches) and the oracle's proof."""
+    a, b = tables(n, 800 + n + len(hook))
+    cls = E.InnerProductProver if order == "msb" else E.InnerProductProverLSB
+    for rounds in (4, 5, n):
+        provers = []
+        for level in (2, 1, 0):
+            p = cls(a, b)
+            p.set_first_rounds(level)
+            provers.append(p)
+        for use_graph in (True, False):
+            proofs = []
+            for p in provers:
+                p.reset()
+                proofs.append(p.prove(rounds, E.Transcript.keccak(3, b"r03"), hook=hook, use_graph=use_graph))
+            for y in proofs[1:]:
+                assert np.array_equal(proofs[0].round_polys, y.round_polys)
+                assert np.array_equal(proofs[0].challenges, y.challenges)
+                assert np.array_equal(proofs[0].final_value, y.final_value)
+            if rounds < n:
+                for t in range(2):
+                    for q in provers[1:]:
+                        assert np.array_equal(provers[0].table(t), q.table(t))
+        rp, ch, fv = O.sumcheck(O.Prover(O.IP, O.MSB if order == "msb" else O.LSB, 3, [a, b]), rounds,
+                                O.Transcript(3, label=b"r03"), hook=hook)
+        assert np.array_equal(proofs[0].round_polys, rp)
+        assert np.array_equal(proofs[0].challenges, ch)
+        assert np.array_equal(proofs[0].final_value, fv)
+
+
+@pytest.mark.parametrize("order", ["msb", "lsb"])
+def test_rounds_0_3_edge_values(E, order):
+    """Tables of the extreme canonical values 0, 1, p - 1 and 2^32 (every
+    difference and interpolation sum wraps): the three-round start equals the
+    oracle."""
+    n = 14
+    g = np.random.default_rng(4)
+    pick = np.array([0, 1, O.P - 1, 1 << 32, O.P - 2, (1 << 32) - 1], dtype=np.uint64)
+    a = pick[g.integers(0, pick.size, size=1 << n)]
+    b = pick[g.integers(0, pick.size, size=1 << n)]
+    cls = E.InnerProductProver if order == "msb" else E.InnerProductProverLSB
+    x = cls(a, b).prove(n, E.Transcript.keccak(3, b"edge"))
+    rp, ch, fv = O.sumcheck(O.Prover(O.IP, O.MSB if order == "msb" else O.LSB, 3, [a, b]), n,
+                            O.Transcript(3, label=b"edge"))
+    assert np.array_equal(x.round_polys, rp)
+    assert np.array_equal(x.final_value, fv)
