@@ -182,12 +182,18 @@ def run_reference(args):
             times.append(dt)
     total = sum(times)
     value = args.steps * 2 * (1 << sample_vars) / total
+    cfg = config(n_vars, args.gpus, "reference")
+    if sample_vars != n_vars:
+        # a slower host: the steps ran a smaller proof; say so in the config
+        cfg["num_vars"] = sample_vars
+        cfg["workload_num_vars"] = n_vars
+        cfg["workload"] += " (this host ran num_vars=%d per step to bound the run)" % sample_vars
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "u64 (Goldilocks Fp / Fp3)", "data": "synthetic: seeded uniform Goldilocks tables",
-        "config": config(n_vars, args.gpus, "reference"),
+        "config": cfg,
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
                          "sample": "full protocol (IP MSB, Fp3 challenges, Keccak transcript) at "
                                    "num_vars=%d per step; C restatement of the reference algorithms "
@@ -531,17 +537,23 @@ def run_batch(args, E, L, ctx, stream, rank):
     del solos
 
     oracle_checked = 0
+    cpu_b = None
     if rank == 0 and not args.no_cpu_baseline:
         from oracle import oracle as O
         O.set_threads(os.cpu_count() or 1)
+        cpu_s = 0.0
         for i in range(count):
             n = 1 << nv[i]
             pr = O.Prover(O.IP, O.MSB, 3, [O.gen_table(seeds[i][0], n), O.gen_table(seeds[i][1], n)])
+            t0 = time.perf_counter()
             orp, och, ofv = O.sumcheck(pr, nv[i], O.Transcript(3, label=batch_label(i)))
+            cpu_s += time.perf_counter() - t0
             ok = (np.array_equal(orp, rp[rows[i]:rows[i + 1]]) and np.array_equal(och, ch[rows[i]:rows[i + 1]])
                   and np.array_equal(ofv, fv[i]))
             assert ok, "batched proof %d differs from the oracle" % i
             oracle_checked += 1
+        cpu_b = cpu_rec(count, cpu_s, "proofs/s", "the %d proofs of the cohort one after another (sumcheck "
+                        "time only, table generation excluded)" % count)
     verify = run_verify_batch(E, L, ctx, b, nv, rp, fv, rows)
     alg = sum(ip_fp3_bytes_as_run(n) for n in nv)
     alg_textbook = sum(ip_fp3_bytes(n) for n in nv)
@@ -566,6 +578,7 @@ def run_batch(args, E, L, ctx, stream, rank):
         "one_at_a_time": {"ms_per_cohort": ms_solo, "proofs_per_s": count / (ms_solo * 1e-3),
                           "path": "effsc_prove per instance (its own CUDA graph), device-resident tables"},
         "speedup_proofs_per_s": ms_solo / ms_batch,
+        "cpu_baseline": cpu_b,
         "autotune": tune_rec,
         "bit_exact": {"batched_vs_one_at_a_time": count, "batched_vs_oracle": oracle_checked},
         "verify": verify,
@@ -675,6 +688,26 @@ def time_proofs(torch, stream, fn, steps):
     return e0.elapsed_time(e1) / steps, out
 
 
+def cpu_rec(work, seconds, unit, sample, scale=1.0):
+    """A cpu_baseline record: the oracle (C restatement of the reference
+    algorithms, all host threads) timed on this host."""
+    return {"value": work / seconds * scale, "unit": unit, "cores": os.cpu_count() or 1, "kind": "port",
+            "seconds": seconds, "sample": sample + "; C restatement of the reference algorithms (oracle/), "
+                                                    "not the Rust reference binary",
+            "cpu_model": cpu_model()}
+
+
+def cpu_model():
+    try:
+        for line in open("/proc/cpuinfo"):
+            if line.lower().startswith(("model name", "cpu model")):
+                return line.split(":", 1)[1].strip()
+        import platform
+        return platform.machine()
+    except OSError:
+        return None
+
+
 def run_configs(args, E, L, ctx, stream, rank):
     import numpy as np
     import torch
@@ -710,13 +743,20 @@ def run_configs(args, E, L, ctx, stream, rank):
 
     ms_e, pf_e = time_proofs(torch, stream, eqf_proof, 20)
     by_e, _ = profile_bytes(E, L, lambda: eqf_proof(False))
-    ok_c = ok_e = None
+    ok_c = ok_e = cpu_c = cpu_e = None
     if check:
-        rp, ch, fv = O.sumcheck(O.Prover(O.COEF, O.MSB, 3, [eq, f, g]), rounds, O.Transcript(3, label=lab_c),
-                                hook=hook)
+        pr = O.Prover(O.COEF, O.MSB, 3, [eq, f, g])
+        t0 = time.perf_counter()
+        rp, ch, fv = O.sumcheck(pr, rounds, O.Transcript(3, label=lab_c), hook=hook)
+        cpu_c = cpu_rec(3 * (1 << n), time.perf_counter() - t0, "evals/s",
+                        "one full proof of the same workload (same inputs, transcript and hook)")
         ok_c = bool(np.array_equal(pf_c.round_polys, rp) and np.array_equal(pf_c.final_value, fv))
         assert ok_c, "Coefficient n=24 proof differs from the oracle"
-        rp, ch, fv = O.sumcheck(O.Prover.eq_factored(3, w, pvals), rounds, O.Transcript(3, label=lab_e), hook=hook)
+        pr = O.Prover.eq_factored(3, w, pvals)
+        t0 = time.perf_counter()
+        rp, ch, fv = O.sumcheck(pr, rounds, O.Transcript(3, label=lab_e), hook=hook)
+        cpu_e = cpu_rec(1 << n, time.perf_counter() - t0, "evals/s",
+                        "one full proof of the same workload (same inputs, transcript and hook)")
         ok_e = bool(np.array_equal(pf_e.round_polys, rp) and np.array_equal(pf_e.final_value, fv))
         assert ok_e, "EqFactored n=24 proof differs from the oracle"
     res["coefficient_eqfg_n24"] = {
@@ -724,12 +764,12 @@ def run_configs(args, E, L, ctx, stream, rank):
                     "num_vars=24, r seeded uniform Fp3, 16 partial rounds + finalize, hook absorbs 0x00..0x1f per "
                     "round, label %s" % lab_c.decode(),
         "ms_per_proof": ms_c, "evals_per_s": 3 * (1 << n) / (ms_c * 1e-3), "algorithmic_bytes": by_c,
-        "hbm_gbs": by_c / (ms_c * 1e-3) / 1e9, "bit_exact_vs_oracle": ok_c}
+        "hbm_gbs": by_c / (ms_c * 1e-3) / 1e9, "bit_exact_vs_oracle": ok_c, "cpu_baseline": cpu_c}
     res["eq_factored_n24"] = {
         "workload": "EqFactoredProver, w = the same r, p = f . g (one base table), num_vars=24, 16 partial "
                     "rounds + finalize, same hook, label %s" % lab_e.decode(),
         "ms_per_proof": ms_e, "evals_per_s": (1 << n) / (ms_e * 1e-3), "algorithmic_bytes": by_e,
-        "hbm_gbs": by_e / (ms_e * 1e-3) / 1e9, "bit_exact_vs_oracle": ok_e}
+        "hbm_gbs": by_e / (ms_e * 1e-3) / 1e9, "bit_exact_vs_oracle": ok_e, "cpu_baseline": cpu_e}
     del coef, eqf
     res["gkr_k12"] = run_gkr_k12(E, L, ctx, stream, check)
     # InnerProduct LSB (pair-split), num_vars = 26: the other variant of the
@@ -746,16 +786,19 @@ def run_configs(args, E, L, ctx, stream, rank):
 
     ms_l, pf_l = time_proofs(torch, stream, lsb_proof, 10)
     by_l, _ = profile_bytes(E, L, lambda: lsb_proof(False))
-    ok_l = None
+    ok_l = cpu_l = None
     if check:
-        rp, ch, fv = O.sumcheck(O.Prover(O.IP, O.LSB, 3, [al, bl]), n, O.Transcript(3, label=lab_l))
+        pr = O.Prover(O.IP, O.LSB, 3, [al, bl])
+        t0 = time.perf_counter()
+        rp, ch, fv = O.sumcheck(pr, n, O.Transcript(3, label=lab_l))
+        cpu_l = cpu_rec(2 * (1 << n), time.perf_counter() - t0, "evals/s", "one full proof of the same workload")
         ok_l = bool(np.array_equal(pf_l.round_polys, rp) and np.array_equal(pf_l.final_value, fv))
         assert ok_l, "InnerProduct LSB n=26 proof differs from the oracle"
     res["inner_product_lsb_n26"] = {
         "workload": "InnerProductProverLSB (pairs 2k, 2k+1), num_vars=26, a, b = the headline's seeded tables, Fp3 "
                     "challenges, 26 rounds + finalize, label %s" % lab_l.decode(),
         "ms_per_proof": ms_l, "evals_per_s": 2 * (1 << n) / (ms_l * 1e-3), "algorithmic_bytes": by_l,
-        "hbm_gbs": by_l / (ms_l * 1e-3) / 1e9, "bit_exact_vs_oracle": ok_l}
+        "hbm_gbs": by_l / (ms_l * 1e-3) / 1e9, "bit_exact_vs_oracle": ok_l, "cpu_baseline": cpu_l}
     del lsb, al, bl
     # InnerProduct n = 28 over tables left in host memory and read in place
     # (the path for tables larger than HBM): only the Fp3 tables of length
@@ -771,9 +814,12 @@ def run_configs(args, E, L, ctx, stream, rank):
         return hp.prove(n, E.Transcript.keccak(E.FP3, lab_h), use_graph=use_graph)
 
     ms_h, pf_h = time_proofs(torch, stream, host_proof, 5)
-    ok_h = None
+    ok_h = cpu_h = None
     if check:
-        rp, ch, fv = O.sumcheck(O.Prover(O.IP, O.MSB, 3, [ah, bh]), n, O.Transcript(3, label=lab_h))
+        pr = O.Prover(O.IP, O.MSB, 3, [ah, bh])
+        t0 = time.perf_counter()
+        rp, ch, fv = O.sumcheck(pr, n, O.Transcript(3, label=lab_h))
+        cpu_h = cpu_rec(2 * (1 << n), time.perf_counter() - t0, "evals/s", "one full proof of the same workload")
         ok_h = bool(np.array_equal(pf_h.round_polys, rp) and np.array_equal(pf_h.final_value, fv))
         assert ok_h, "host-resident InnerProduct proof differs from the oracle"
     N = 1 << n
@@ -786,7 +832,7 @@ def run_configs(args, E, L, ctx, stream, rank):
         "host_read_gbs": 2 * 16 * N / (ms_h * 1e-3) / 1e9,
         "device_table_bytes": 2 * 3 * (N // 4) * 8,
         "device_table_bytes_if_uploaded": 2 * N * 8 + 2 * 3 * (N // 4) * 8,
-        "bit_exact_vs_oracle": ok_h}
+        "bit_exact_vs_oracle": ok_h, "cpu_baseline": cpu_h}
     del hp, ah, bh
     res["protogalaxy_fold"] = run_pg_fold(E, L, ctx, stream, check)
     return res
@@ -809,9 +855,12 @@ def run_ml_n20(E, L, ctx, stream, check, steps=200):
 
     ms, pf = time_proofs(torch, stream, ml_proof, steps)
     by, _ = profile_bytes(E, L, lambda: ml_proof(False))
-    ok = None
+    ok = cpu = None
     if check:
-        rp, ch, fv = O.sumcheck(O.Prover(O.ML, O.MSB, 1, [v]), n, O.Transcript(1, label=lab))
+        pr = O.Prover(O.ML, O.MSB, 1, [v])
+        t0 = time.perf_counter()
+        rp, ch, fv = O.sumcheck(pr, n, O.Transcript(1, label=lab))
+        cpu = cpu_rec(1 << n, time.perf_counter() - t0, "evals/s", "one full proof of the same workload")
         ok = bool(np.array_equal(pf.round_polys.reshape(n, 1), rp[:, :, 0]) and
                   np.array_equal(pf.final_value.reshape(1), fv[:1]))
         assert ok, "Multilinear n=20 proof differs from the oracle"
@@ -819,7 +868,7 @@ def run_ml_n20(E, L, ctx, stream, check, steps=200):
         "workload": "MultilinearProver MSB over Fp, num_vars=20, seeded uniform table, Fp challenges, label %s, "
                     "20 rounds + finalize; one CUDA graph per proof (L2-resident, latency-bound)" % lab.decode(),
         "us_per_proof": ms * 1e3, "evals_per_s": (1 << n) / (ms * 1e-3), "algorithmic_bytes": by,
-        "hbm_gbs": by / (ms * 1e-3) / 1e9, "bit_exact_vs_oracle": ok}
+        "hbm_gbs": by / (ms * 1e-3) / 1e9, "bit_exact_vs_oracle": ok, "cpu_baseline": cpu}
 
 
 def run_gkr_k12(E, L, ctx, stream, check, steps=20):
@@ -841,10 +890,12 @@ def run_gkr_k12(E, L, ctx, stream, check, steps=20):
 
     ms_g, pf_g = time_proofs(torch, stream, gkr_proof, steps)
     by_g, _ = profile_bytes(E, L, lambda: gkr_proof(False))
-    ok_g = None
+    ok_g = cpu_g = None
     if check:
         orc = O.Prover.gkr(3, add, mult, wv)
+        t0 = time.perf_counter()
         rp, ch, fv = O.sumcheck(orc, 2 * k, O.Transcript(3, label=lab_g))
+        cpu_g = cpu_rec(2 * (1 << (2 * k)), time.perf_counter() - t0, "evals/s", "one full proof of the same workload")
         ok_g = bool(np.array_equal(pf_g.round_polys, rp) and np.array_equal(pf_g.final_value, fv)
                     and np.array_equal(gk.claimed_w_values(), orc.claimed_w_values()))
         assert ok_g, "GkrProver k=12 proof differs from the oracle"
@@ -852,7 +903,7 @@ def run_gkr_k12(E, L, ctx, stream, check, steps=20):
         "workload": "GkrProver (MSB), k=12: add, mult seeded uniform tables of 2^24 Goldilocks values, w of 2^12, "
                     "Fp3 challenges, 24 rounds + finalize, label %s; witness kept as two 2^12 tables" % lab_g.decode(),
         "ms_per_proof": ms_g, "evals_per_s": 2 * (1 << (2 * k)) / (ms_g * 1e-3), "algorithmic_bytes": by_g,
-        "hbm_gbs": by_g / (ms_g * 1e-3) / 1e9, "bit_exact_vs_oracle": ok_g}
+        "hbm_gbs": by_g / (ms_g * 1e-3) / 1e9, "bit_exact_vs_oracle": ok_g, "cpu_baseline": cpu_g}
 
 
 def run_pg_fold(E, L, ctx, stream, check, steps=20):
@@ -908,7 +959,9 @@ def run_pg_fold(E, L, ctx, stream, check, steps=20):
                                                                      in_bytes >> 20, logn, width - 1 + logn),
             "ms_per_fold": ms, "wall_ms_per_fold": wall_ms, "coefficients_per_s": n * width / (ms * 1e-3),
             "input_bytes": in_bytes, "hbm_gbs": in_bytes / (ms * 1e-3) / 1e9, "launches_per_fold": launches,
-            "cpu_oracle_s": cpu_s, "cpu_cores": os.cpu_count(), "bit_exact_vs_oracle": ok}
+            "cpu_oracle_s": cpu_s, "cpu_cores": os.cpu_count(), "bit_exact_vs_oracle": ok,
+            "cpu_baseline": cpu_rec(n * width, cpu_s, "coefficients/s", "one fold of the same input")
+            if cpu_s else None}
         del buf
     return out
 
@@ -981,6 +1034,24 @@ def run_serving(args, E, ctx):
             np.array_equal(ref.final_value, proofs_full[i].final_value), "serving proof %d differs from alone" % i
         del p, tabs
     del srv
+    # CPU baseline: the oracle proves the same sample of the mix one request
+    # after another (bounded: the sample, not all requests)
+    cpu_s = None
+    if not args.no_cpu_baseline:
+        from oracle import oracle as O
+        O.set_threads(os.cpu_count() or 1)
+        cpu_s = 0.0
+        for i in sample:
+            n = 1 << nv[i]
+            tabs = [O.gen_table(int(seeds[i][t]), n) for t in range(2 if kinds[i] == 1 else 1)]
+            pr = O.Prover(O.IP if kinds[i] == 1 else O.ML, O.MSB, 3, tabs)
+            t0 = time.perf_counter()
+            rp, _, fv = O.sumcheck(pr, nv[i], O.Transcript(3, label=serve_label(i)))
+            cpu_s += time.perf_counter() - t0
+            assert np.array_equal(rp[:, :rp.shape[1] if kinds[i] == 1 else 1],
+                                  np.asarray(proofs_full[i].round_polys).reshape(nv[i], -1, 3)), \
+                "serving proof %d differs from the oracle" % i
+    mean_nv_sample = sum(nv[i] for i in sample) / len(sample)
     return {
         "workload": "%d requests, 70%% InnerProductProver / 30%% MultilinearProver (MSB), num_vars uniform on "
                     "14..=26 (seed 0x%X), uniform Goldilocks tables generated on the device per request, Fp3 "
@@ -990,7 +1061,12 @@ def run_serving(args, E, ctx):
                        "p99_ms": float(np.percentile(lat_sat, 99) * 1e3), "makespan_s": mk_sat},
         "rates": levels,
         "latency": "submission (arrival) to the proof in host memory",
-        "bit_exact": {"same_in_both_mixes": count, "equal_to_alone_sample": len(sample)},
+        "bit_exact": {"same_in_both_mixes": count, "equal_to_alone_sample": len(sample),
+                      "equal_to_oracle_sample": len(sample) if cpu_s is not None else 0},
+        "cpu_baseline": cpu_rec(len(sample), cpu_s, "proofs/s",
+                                "%d requests of the mix (evenly spaced indices plus the largest and smallest, "
+                                "mean num_vars %.1f) proved one after another" % (len(sample), mean_nv_sample))
+        if cpu_s else None,
     }
 
 
