@@ -87,11 +87,14 @@ __device__ __forceinline__ void ip01_body(const RoundArgs& a, u32 bid, u32 nb) {
 // (x1, x5, x3, x7) give entry m + O likewise; then round 2's pair.
 __device__ __forceinline__ F3 fold2(u64 x0, u64 x2, u64 x4, u64 x6, const F3& r0, const F3& r1, const F3& r01) {
     const u64 d1 = gl_sub(x4, x0), d2 = gl_sub(x2, x0), d3 = gl_sub(gl_sub(x6, x4), d2);
-    Acc c0 = acc_from(x0), c1 = acc_zero(), c2 = acc_zero();
-    acc_mac(c0, d1, r0.c0); acc_mac(c0, d2, r1.c0); acc_mac(c0, d3, r01.c0);
-    acc_mac(c1, d1, r0.c1); acc_mac(c1, d2, r1.c1); acc_mac(c1, d3, r01.c1);
-    acc_mac(c2, d1, r0.c2); acc_mac(c2, d2, r1.c2); acc_mac(c2, d3, r01.c2);
-    return f3_make(acc_reduce(c0), acc_reduce(c1), acc_reduce(c2));
+    AccF<FOLD_FORM> c0, c1, c2;
+    c0.from(x0);
+    c1.zero();
+    c2.zero();
+    c0.mac(d1, r0.c0); c0.mac(d2, r1.c0); c0.mac(d3, r01.c0);
+    c1.mac(d1, r0.c1); c1.mac(d2, r1.c1); c1.mac(d3, r01.c1);
+    c2.mac(d1, r0.c2); c2.mac(d2, r1.c2); c2.mac(d3, r01.c2);
+    return f3_make(c0.reduce(), c1.reduce(), c2.reduce());
 }
 
 // LSB: octet m is entries 8m .. 8m+7; entries 2m and 2m+1 of the length-L/4

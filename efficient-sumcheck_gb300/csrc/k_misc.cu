@@ -3,6 +3,7 @@
 #include "round_common.cuh"
 
 #include <atomic>
+#include <cstdlib>
 
 namespace effsc {
 
@@ -28,14 +29,23 @@ static int sms_of(int device) {
 }
 
 void kernels_init(int device) { sms_of(device); }
+
+bool pdl_on(void) {
+    static const bool on = [] {
+        const char* e = getenv("EFFSC_PDL");
+        return !(e && e[0] == '0');
+    }();
+    return on;
+}
 __global__ void k_gather_first(FirstSrc src, u64* dst) {
+    chain_enter();
     const int i = threadIdx.x;
     if (i < 12) {
         const u64* p = src.p[i / 3][i % 3];
         dst[i] = p ? p[0] : 0;
     }
 }
-void launch_gather_first(const FirstSrc& src, u64* dst, cudaStream_t s) { k_gather_first<<<1, 32, 0, s>>>(src, dst); }
+void launch_gather_first(const FirstSrc& src, u64* dst, cudaStream_t s) { launch_chain(k_gather_first, 1, 32, 0, s, src, dst); }
 
 int max_grid(void) {
     int dev = 0;
@@ -45,6 +55,7 @@ int max_grid(void) {
 
 int pol_ntables(int pol) {
     switch (pol) {
+    case POL_X1: case POL_X2: case POL_X3: return 4;
     case POL_ML: case POL_C1: return 1;
     case POL_C3: case POL_C3W: case POL_EQFL: return 3;
     case POL_GKR: return 4;
@@ -53,6 +64,7 @@ int pol_ntables(int pol) {
 }
 int pol_nraw(int pol) {
     switch (pol) {
+    case POL_X1: case POL_X2: case POL_X3: return 4;
     case POL_C2: case POL_C3W: return 3;
     case POL_C3: return 4;
     default: return 2;
@@ -60,7 +72,9 @@ int pol_nraw(int pol) {
 }
 int pol_nwire(int pol) {
     switch (pol) {
-    case POL_ML: case POL_C1: return 1;
+    case POL_ML: case POL_C1: case POL_X1: return 1;
+    case POL_X2: return 2;
+    case POL_X3: return 3;
     case POL_C3: case POL_C3W: return 3;
     default: return 2;
     }
@@ -76,7 +90,7 @@ bool launch_fused(int pol, int sem, u32 mask, bool ech, const RoundArgs& a, int 
 }
 
 #define FOLD(SEM, EI, ECH) \
-    case ((SEM) * 4 + (EI) * 2 + (ECH)): k_fold<SEM, EI, ECH><<<grid, TPB, 0, s>>>(a, t); return true;
+    case ((SEM) * 4 + (EI) * 2 + (ECH)): return launch_chain(k_fold<SEM, EI, ECH>, grid, TPB, 0, s, a, t);
 
 bool launch_fold(int sem, bool ein, bool ech, const RoundArgs& a, int t, int grid, cudaStream_t s) {
     if (ein) ech = true;
@@ -238,6 +252,78 @@ __global__ void k_fp3_chain(u64* out, u32 iters, u64 seed) {
     u64 r = 0;
     for (int c = 0; c < CH; c++) r ^= x[c].c0 ^ x[c].c1 ^ x[c].c2;
     if (r == 0x1234567) out[0] = r;
+}
+
+// Accumulate-form rate: K independent lazy sums per thread, each new 64-bit
+// operand multiplied by a per-sum constant and added unreduced -- the form of
+// every fold and round-polynomial sum in the round kernels.  FORM 1 = the
+// split accumulator of the folds, 0 = the 5-limb form of the long sums.
+template <int FORM, int K>
+__global__ void __launch_bounds__(256) k_accmac_chain(u64* out, u32 iters, u64 seed) {
+    const u64 tid = (u64)blockIdx.x * blockDim.x + threadIdx.x;
+    u64 x = splitmix64_mix_dev(seed + tid);
+    u64 y[K];
+    AccF<FORM> a[K];
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+        y[k] = splitmix64_mix_dev(seed * 31 + k) % GL_P;
+        a[k].zero();
+    }
+    for (u32 i = 0; i < iters; i++) {
+        x += 0x9E3779B97F4A7C15ULL;
+#pragma unroll
+        for (int k = 0; k < K; k++) a[k].mac(x, y[k]);
+    }
+    u64 r = 0;
+#pragma unroll
+    for (int k = 0; k < K; k++) r ^= a[k].reduce();
+    if (r == 0x1234567) out[0] = r;
+}
+// Reduction rate: one acc_reduce of a fresh 160-bit value per iteration.
+__global__ void __launch_bounds__(256) k_reduce_chain(u64* out, u32 iters, u64 seed) {
+    const u64 tid = (u64)blockIdx.x * blockDim.x + threadIdx.x;
+    u64 x = splitmix64_mix_dev(seed + tid), r = 0;
+    for (u32 i = 0; i < iters; i++) {
+        x += 0x9E3779B97F4A7C15ULL;
+        Acc a;
+        a.c0 = lo32(x); a.c1 = hi32(x); a.c2 = lo32(x) ^ i; a.c3 = hi32(x) + i; a.c4 = i & 7;
+        r ^= acc_reduce(a);
+    }
+    if (r == 0x1234567) out[0] = r;
+}
+
+bool diag_accumulate_rate(cudaStream_t s, double* mac_per_s, double* reduce_per_s) {
+    u64* out = nullptr;
+    if (cudaMallocAsync((void**)&out, sizeof(u64), s) != cudaSuccess) return false;
+    int bps = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_accmac_chain<1, 2>, 256, 0) != cudaSuccess || bps < 1) bps = 1;
+    const int blocks_mac = (max_grid() / 8) * bps;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_reduce_chain, 256, 0) != cudaSuccess || bps < 1) bps = 1;
+    const int blocks_red = (max_grid() / 8) * bps;
+    const u32 iters = 1u << 15;
+    cudaEvent_t a, b;
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    float ms1 = 0, ms2 = 0;
+    for (int rep = 0; rep < 2; rep++) {   // the first pass warms up
+        cudaEventRecord(a, s);
+        k_accmac_chain<1, 2><<<blocks_mac, 256, 0, s>>>(out, iters, 1);
+        cudaEventRecord(b, s);
+        cudaEventSynchronize(b);
+        cudaEventElapsedTime(&ms1, a, b);
+        cudaEventRecord(a, s);
+        k_reduce_chain<<<blocks_red, 256, 0, s>>>(out, iters, 1);
+        cudaEventRecord(b, s);
+        cudaEventSynchronize(b);
+        cudaEventElapsedTime(&ms2, a, b);
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    cudaFreeAsync(out, s);
+    bool ok = cudaStreamSynchronize(s) == cudaSuccess && ms1 > 0 && ms2 > 0;
+    *mac_per_s = (double)blocks_mac * 256 * iters * 2 / (ms1 * 1e-3);
+    *reduce_per_s = (double)blocks_red * 256 * iters / (ms2 * 1e-3);
+    return ok;
 }
 
 bool diag_mulmod_rate(cudaStream_t s, double* mulmod_per_s, double* fp3_mul_per_s) {

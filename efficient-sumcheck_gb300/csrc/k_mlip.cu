@@ -7,7 +7,7 @@
 namespace effsc {
 
 #define EVAL(POL, SEM, M) \
-    case ((POL) * 64 + (SEM) * 16 + (M)): k_eval<POL, SEM, M><<<grid, TPB, 0, s>>>(a); return true;
+    case ((POL) * 64 + (SEM) * 16 + (M)): return launch_chain(k_eval<POL, SEM, M>, grid, TPB, 0, s, a);
 
 bool launch_eval_mlip(int pol, int sem, u32 mask, const RoundArgs& a, int grid, cudaStream_t s) {
     switch (pol * 64 + sem * 16 + (int)mask) {
@@ -21,7 +21,7 @@ bool launch_eval_mlip(int pol, int sem, u32 mask, const RoundArgs& a, int grid, 
 }
 
 #define FUSED(POL, SEM, M, ECH) \
-    case ((POL) * 128 + (SEM) * 32 + (M) * 2 + (ECH)): k_fused<POL, SEM, M, ECH><<<grid, TPB, 0, s>>>(a); return true;
+    case ((POL) * 128 + (SEM) * 32 + (M) * 2 + (ECH)): return launch_chain(k_fused<POL, SEM, M, ECH>, grid, TPB, 0, s, a);
 
 bool launch_fused_mlip(int pol, int sem, u32 mask, bool ech, const RoundArgs& a, int grid, cudaStream_t s) {
     switch (pol * 128 + sem * 32 + (int)mask * 2 + (ech ? 1 : 0)) {
@@ -50,8 +50,7 @@ static bool launch_tma_inst(const RoundArgs& a, u32 ntiles, int grid, cudaStream
             return false;
         configured.fetch_or(bit);
     }
-    k_fused_tma<POL, SEM, M, ECH><<<grid, TPB, SM_BYTES, s>>>(a, ntiles);
-    return true;
+    return launch_chain(k_fused_tma<POL, SEM, M, ECH>, grid, TPB, SM_BYTES, s, a, ntiles);
 }
 
 bool launch_fused_tma(int pol, int sem, u32 mask, bool ech, const RoundArgs& a, u32 ntiles, int grid, cudaStream_t s) {

@@ -348,7 +348,10 @@ __global__ void __launch_bounds__(TAIL_TPB, 1) k_tail_cluster(TailArgs a, u32 cs
 }
 
 template <int POL, int FW>
-__global__ void __launch_bounds__(TAIL_TPB, 1) k_tail_one(TailArgs a) { tail_body<POL, FW>(a); }
+__global__ void __launch_bounds__(TAIL_TPB, 1) k_tail_one(TailArgs a) {
+    chain_enter();
+    tail_body<POL, FW>(a);
+}
 template <int POL, int FW>
 __global__ void __launch_bounds__(TAIL_TPB, 1) k_tail_many(const TailArgs* args) { tail_body<POL, FW>(args[blockIdx.x]); }
 
@@ -365,7 +368,7 @@ static bool tail_inst(const TailArgs* dev_args, const TailArgs* one, u32 n, u64 
     if (bytes > TAIL_SMEM_CAP) return false;
     if (one) {
         cudaFuncSetAttribute(k_tail_one<POL, FW>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TAIL_SMEM_CAP);
-        k_tail_one<POL, FW><<<1, TAIL_TPB, bytes, s>>>(*one);
+        return launch_chain(k_tail_one<POL, FW>, 1, TAIL_TPB, bytes, s, *one);
     } else {
         cudaFuncSetAttribute(k_tail_many<POL, FW>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TAIL_SMEM_CAP);
         k_tail_many<POL, FW><<<n, TAIL_TPB, bytes, s>>>(dev_args);

@@ -11,6 +11,28 @@ namespace effsc {
 
 // Threads per block of every round kernel.
 constexpr int KERNEL_TPB = 256;
+
+// Kernels of a proof's chain are launched with programmatic dependent launch:
+// a kernel may be scheduled while the previous kernel on the stream drains
+// (its last block's reduction and transcript step), and waits on the device
+// (griddepcontrol.wait, the first statement of every such kernel) before it
+// touches memory.  EFFSC_PDL=0 in the environment launches them plainly.
+bool pdl_on(void);
+template <class... KArgs, class... Args>
+inline bool launch_chain(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
+                         Args... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = pdl_on() ? 1 : 0;
+    return cudaLaunchKernelEx(&cfg, kernel, args...) == cudaSuccess;
+}
 // Value a kernel writes to RoundArgs::status when a bounded wait times out.
 constexpr unsigned EFFSC_STATUS_TIMEOUT = 4;
 
@@ -36,7 +58,27 @@ enum Sem { SEM_MSB_PAD = 0, SEM_MSB_FLOOR = 1, SEM_LSB = 2 };
 //            add (W_b + W_c) + mult W_b W_c: the wire [q(0), q(inf)]
 enum Pol {
     POL_ML = 0, POL_IP = 1, POL_C1 = 2, POL_C2 = 3, POL_C3 = 4, POL_EQFR = 5, POL_EQFL = 6, POL_IP01 = 7,
-    POL_GKR = 8, POL_C3W = 9, POL_ML01 = 10
+    POL_GKR = 8, POL_C3W = 9, POL_ML01 = 10,
+    // CoefficientProver with a declarative evaluator (ExprProgram) of degree
+    // 1, 2, 3: raw values are the coefficients c0..c3
+    POL_X1 = 11, POL_X2 = 12, POL_X3 = 13
+};
+
+// A declarative RoundPolyEvaluator (src/coefficient_sumcheck.rs:50-76): per
+// pair, coeffs[coeff] += k * prod of the factors, each factor the even (lo)
+// or odd (hi) element of a column.  Columns are the pairwise tables and the
+// columns of the tablewise tables (a tablewise row is one element of each of
+// its columns).  factor = column * 2 + (0: even, 1: odd).
+constexpr int EXPR_MAX_TERMS = 16;
+constexpr int EXPR_MAX_FACTORS = 4;
+struct ExprTerm {
+    unsigned char coeff, nf;
+    unsigned char f[EXPR_MAX_FACTORS];
+    u64 k[3];               // canonical Fp3 constant
+};
+struct ExprProgram {
+    u32 nterms, degree, ncols;
+    ExprTerm t[EXPR_MAX_TERMS];
 };
 
 struct TabIO {
@@ -163,6 +205,10 @@ int pol_nwire(int pol);
 
 // Returns false if no kernel is instantiated for this combination.
 bool launch_fold(int sem, bool ein, bool ech, const RoundArgs& a, int t, int grid, cudaStream_t s);
+// Round polynomial of a declarative evaluator on the current columns
+// (a.t[0..ncols), a.L entries each; MSB floor pairs (k, k + L/2) or LSB pairs
+// (2k, 2k+1)); the last block finalises with policy POL_X<degree>.
+bool launch_expr_eval(int sem, const RoundArgs& a, const ExprProgram& prog, int grid, cudaStream_t s);
 bool launch_eval(int pol, int sem, u32 mask, const RoundArgs& a, int grid, cudaStream_t s);
 bool launch_fused(int pol, int sem, u32 mask, bool ech, const RoundArgs& a, int grid, cudaStream_t s);
 bool launch_eqf_left(bool fused, u32 mask, bool ech, const RoundArgs& a, int grid, cudaStream_t s);
@@ -188,6 +234,14 @@ bool launch_ip2x(bool lsb, const RoundArgs& a, int grid, cudaStream_t s);
 // holds r0, r1, r2 as 9 consecutive words).
 bool launch_ip012(bool lsb, const RoundArgs& a, int grid, cudaStream_t s);
 bool launch_ip3x(bool lsb, const RoundArgs& a, int grid, cudaStream_t s);
+// The same passes with the tables streamed through shared memory by bulk
+// copies: ntiles = (L/8) / ip012_tile_octets() tiles of the first pass,
+// (L/16) / ip3x_tile_items() of the second; device-memory tables, 16-byte
+// aligned; at most two blocks per SM for the first pass's partials.
+bool launch_ip012_staged(bool lsb, const RoundArgs& a, u32 ntiles, int grid, cudaStream_t s);
+bool launch_ip3x_staged(bool lsb, const RoundArgs& a, u32 ntiles, int grid, cudaStream_t s);
+u32 ip012_tile_octets(void);
+u32 ip3x_tile_items(void);
 bool launch_ml01(const RoundArgs& a, int grid, cudaStream_t s);
 bool launch_ml2x(bool ech, const RoundArgs& a, int grid, cudaStream_t s);
 bool launch_gkr01(const RoundArgs& a, int grid, cudaStream_t s);
@@ -210,6 +264,7 @@ void launch_fill(u64* dst, u64 n, u64 v, cudaStream_t s);
 bool launch_build_eq(const u64* w, u32 v, int ext, u64* c0, u64* c1, u64* c2, cudaStream_t s);
 void launch_gen_uniform(u64 seed, u64 n, u64* out, cudaStream_t s);
 bool diag_mulmod_rate(cudaStream_t s, double* mulmod_per_s, double* fp3_mul_per_s);
+bool diag_accumulate_rate(cudaStream_t s, double* mac_per_s, double* reduce_per_s);
 // One thread waits on an mbarrier with the round kernels' bounded wait;
 // `arrive`: complete the phase first.  *status = 0 or EFFSC_STATUS_TIMEOUT.
 void launch_diag_bounded_wait(u64 limit_ns, int arrive, u32* status, cudaStream_t s);

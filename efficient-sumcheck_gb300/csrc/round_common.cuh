@@ -24,6 +24,14 @@ constexpr int RAW_WORDS = 12;   // up to 4 Fp3 raw values per block partial
 template <u32 M>
 __device__ __forceinline__ constexpr bool ext_of(int t) { return (M >> t) & 1u; }
 
+// Start of every kernel launched by launch_chain: wait until the previous
+// kernel on the stream has completed and its writes are visible, then let the
+// next kernel be scheduled (it waits the same way before it reads anything).
+__device__ __forceinline__ void chain_enter() {
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
 template <bool E>
 __device__ __forceinline__ F3 ld(const u64* const* p, u64 i) {
     F3 r;
@@ -198,7 +206,9 @@ __device__ __forceinline__ F3 ld_scalar(const u64* const* p) {
 
 __device__ __forceinline__ int pol_nwire_dev(int pol) {
     switch (pol) {
-    case POL_ML: case POL_C1: return 1;
+    case POL_ML: case POL_C1: case POL_X1: return 1;
+    case POL_X2: return 2;
+    case POL_X3: return 3;
     case POL_C3: case POL_C3W: return 3;
     default: return 2;
     }
@@ -333,6 +343,20 @@ static __device__ __noinline__ void finalize_warp(int pol, const u64* raw, const
             w[0] = r[0]; w[1] = r[2]; w[2] = r[1];
             r[1] = f3_zero();
             break;
+        case POL_X1: case POL_X2: case POL_X3: {
+            // r = the coefficients c0..c3 of h; the EvalsInfty wire
+            // (src/provers/coefficient.rs:272-294): [h(0)] for degree 1,
+            // [h(0), h(inf)] for 2, [h(0), h(inf), h(2)] for 3; aux (c0, c1)
+            w[0] = r[0];
+            if (pol == POL_X2) w[1] = r[2];
+            if (pol == POL_X3) {
+                w[1] = r[3];
+                const F3 two = f3_make(2, 0, 0);
+                w[2] = f3_add<true>(f3_mul<true, true>(f3_add<true>(f3_mul<true, true>(
+                    f3_add<true>(f3_mul<true, true>(r[3], two), r[2]), two), r[1]), two), r[0]);
+            }
+            break;
+        }
         case POL_GKR:
             // r = q(0), c2: q is quadratic, so the reference's
             // q(inf) = (q(0) + q(2) - 2 q(1)) / 2 (src/provers/gkr.rs:185-189) is c2
@@ -514,6 +538,7 @@ __device__ __forceinline__ void eval_body(const RoundArgs& a, u32 bid, u32 nb) {
 }
 template <int POL, int SEM, u32 M>
 __global__ void __launch_bounds__(TPB) k_eval(RoundArgs a) {
+    chain_enter();
     eval_body<POL, SEM, M>(a, blockIdx.x, gridDim.x);
 }
 
@@ -595,12 +620,14 @@ __device__ __forceinline__ void fused_body(const RoundArgs& a, u32 bid, u32 nb) 
 }
 template <int POL, int SEM, u32 M, bool ECH>
 __global__ void __launch_bounds__(TPB, 2) k_fused(RoundArgs a) {
+    chain_enter();
     fused_body<POL, SEM, M, ECH>(a, blockIdx.x, gridDim.x);
 }
 // Policies whose accumulators do not fit 128 registers (the degree-3 product
 // evaluator): one block per SM, no spills.
 template <int POL, int SEM, u32 M, bool ECH>
 __global__ void __launch_bounds__(TPB, 1) k_fused_wide(RoundArgs a) {
+    chain_enter();
     fused_body<POL, SEM, M, ECH>(a, blockIdx.x, gridDim.x);
 }
 
@@ -675,6 +702,7 @@ struct TmaLayout {
 
 template <int POL, int SEM, u32 M, bool ECH>
 __global__ void __launch_bounds__(TPB, 2) k_fused_tma(RoundArgs a, u32 ntiles) {
+    chain_enter();
     constexpr int NT = Policy<POL, 0>::NT;
     constexpr u32 FULL = (1u << NT) - 1;
     constexpr u32 MO = ECH ? FULL : M;
@@ -821,6 +849,7 @@ __global__ void __launch_bounds__(TPB, 2) k_fused_tma(RoundArgs a, u32 ntiles) {
 // finalize(), and the standalone fold.
 template <int SEM, bool EI, bool ECH>
 __global__ void __launch_bounds__(TPB) k_fold(RoundArgs a, int t) {
+    chain_enter();
     constexpr bool EO = EI || ECH;
     F3 rr;
     Mul3 r = load_challenge_mul(a, rr);

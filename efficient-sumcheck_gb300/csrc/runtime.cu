@@ -298,6 +298,13 @@ struct effsc_prover {
     // EqFactored left phase from the inner sums (k_eqf.cu); 2 = as 1, with
     // InnerProduct rounds 0-3 in two passes (k_ip012.cu) where they apply
     int fuse_first = 2;
+    // CoefficientProver with a declarative evaluator: the term program over
+    // the columns (pairwise tables, then the tablewise tables' columns);
+    // bit c of tw_cols: column c belongs to a tablewise table
+    bool expr = false;
+    ExprProgram prog;
+    u32 tw_cols = 0;
+    int n_pairwise = 0;
     u64* eqf_scratch = nullptr;               // inner sums, eq weights, partial sums
     size_t eqf_cap = 0;
     // effsc_prove outputs: pinned staging (wire | challenges | transcript |
@@ -312,7 +319,7 @@ namespace {
 int degree_of(const effsc_prover* p) {
     switch (p->kind) {
     case EFFSC_ML: return 1;
-    case EFFSC_COEF: return p->ntab;
+    case EFFSC_COEF: return p->expr ? (int)p->prog.degree : p->ntab;
     default: return 2;
     }
 }
@@ -482,7 +489,32 @@ u32 mask_of(const effsc_prover* P, const int* idx, int n) {
 // (src/provers/multilinear.rs:58-67, multilinear_lsb.rs:180-189,
 // inner_product.rs:61-113, inner_product_lsb.rs:156-164,
 // coefficient.rs:272-294, coefficient_lsb.rs:180-203).
+// One round of a CoefficientProver[LSB] with a declarative evaluator
+// (src/provers/coefficient.rs:272-294, coefficient_lsb.rs:180-203): fold
+// every column with the challenge (MSB floor or LSB pairs), then evaluate the
+// term program over the pairs.
+int round_expr(effsc_prover* P, const Chal& ch, const TxIO& tx, bool dry) {
+    const int sem = sem_of(P), nt = P->ntab;
+    if (ch.has && P->t[0].len > 1) {
+        bool ech = ch.ext;
+        for (int i = 0; i < nt; i++) ech |= P->t[i].ext;
+        for (int i = 0; i < nt; i++) TRY(fold_table(P, i, sem, ch, ech, dry));
+    }
+    RoundArgs a = base_args(P);
+    a.tx = tx;
+    const size_t L = P->t[0].len;
+    for (int i = 0; i < nt; i++) set_in(a, i, P->t[i]);
+    a.L = L;
+    uint64_t bytes = 0;
+    for (int i = 0; i < nt; i++) bytes += L * wbytes(P->t[i].ext);
+    if (!dry) TRY(timed_launch(P->ctx->stream, "expr_evaluate", bytes, [&] {
+        return launch_expr_eval(sem, a, P->prog, grid_for(L > 1 ? L / 2 : 1), P->ctx->stream);
+    }));
+    return EFFSC_OK;
+}
+
 int round_std(effsc_prover* P, const Chal& ch, const TxIO& tx, bool dry) {
+    if (P->expr) return round_expr(P, ch, tx, dry);
     // the device protocol needs only the wire, not the legacy pair: the
     // degree-3 evaluator then skips h(1)
     const int pol = (pol_of(P) == POL_C3 && tx.tx) ? POL_C3W : pol_of(P), sem = sem_of(P), nt = P->ntab;
@@ -679,10 +711,24 @@ int do_fuse3(effsc_prover* P, const TxIO& tx0, const TxIO& tx3, const u64* chals
     a.tx = tx0;
     a.L = L;
     for (int i = 0; i < 2; i++) set_in(a, i, P->t[i]);
-    // a block takes 128 octets per step; one wave of two blocks per SM at most
-    // (the partials hold 32 words for each of them)
-    const int g1 = std::min<int>(grid_for(L / 8, 2), (max_grid() / 8) * 2);
-    if (!dry) TRY(timed_launch(P->ctx->stream, "ip_rounds_0_2", 16 * (uint64_t)L, [&] { return launch_ip012(lsb, a, g1, P->ctx->stream); }));
+    // MSB: staged through shared memory for device tables (16-byte aligned,
+    // as the allocator gives).  LSB keeps direct loads: a thread's octet is 64
+    // contiguous bytes, and reading those from a staged tile conflicts on the
+    // shared-memory banks (measured slower: 0.51 against 0.40 ms at n = 26).
+    // A block takes 128 octets per step; one wave of two blocks per SM at most
+    // (the partials hold 32 words for each).
+    bool staged = !lsb;
+    for (int i = 0; i < 2; i++) {
+        const Buf& b0 = P->t[i].bufs[0];
+        staged &= !b0.host && ((uintptr_t)b0.p[0] & 15) == 0;
+    }
+    const u32 nt1 = (u32)((L / 8) / ip012_tile_octets()), nt2 = (u32)((L / 16) / ip3x_tile_items());
+    staged &= nt1 >= 1 && nt2 >= 1;
+    const int two_per_sm = (max_grid() / 8) * 2;
+    const int g1 = staged ? std::min<int>((int)nt1, two_per_sm) : std::min<int>(grid_for(L / 8, 2), two_per_sm);
+    if (!dry) TRY(timed_launch(P->ctx->stream, "ip_rounds_0_2", 16 * (uint64_t)L, [&] {
+        return staged ? launch_ip012_staged(lsb, a, nt1, g1, P->ctx->stream) : launch_ip012(lsb, a, g1, P->ctx->stream);
+    }));
     int bi[2];
     for (int i = 0; i < 2; i++) TRY(out_buffer(P, P->t[i], true, L / 8, true, &bi[i]));
     RoundArgs b = base_args(P);
@@ -693,7 +739,10 @@ int do_fuse3(effsc_prover* P, const TxIO& tx0, const TxIO& tx3, const u64* chals
         set_in(b, i, P->t[i]);
         set_out(b, i, P->t[i].bufs[bi[i]]);
     }
-    if (!dry) TRY(timed_launch(P->ctx->stream, "ip_round_3_triple_fold", 16 * (uint64_t)L + 6 * (uint64_t)L, [&] { return launch_ip3x(lsb, b, grid_for(L / 16), P->ctx->stream); }));
+    if (!dry) TRY(timed_launch(P->ctx->stream, "ip_round_3_triple_fold", 16 * (uint64_t)L + 6 * (uint64_t)L, [&] {
+        return staged ? launch_ip3x_staged(lsb, b, nt2, std::min<int>((int)nt2, two_per_sm), P->ctx->stream)
+                      : launch_ip3x(lsb, b, grid_for(L / 16), P->ctx->stream);
+    }));
     for (int i = 0; i < 2; i++) {
         Table& T = P->t[i];
         T.cur = bi[i];
@@ -1196,6 +1245,40 @@ int read_first(effsc_prover* P, int ti, HF* out) {
 }
 
 // SumcheckProver::final_value of every prover.
+// final_value of a declarative evaluator (src/provers/coefficient.rs:300-329,
+// coefficient_lsb.rs:215-236): the evaluator on (singleton, 0) pairs, then
+// h(0) + h(1).  A lone pairwise table's singleton is returned as is (MSB: any
+// degree; LSB: degree 1).  A tablewise table's odd row is an empty slice in
+// the reference, so a term reading it panics there.
+int final_value_expr(effsc_prover* P, HF* out) {
+    const ExprProgram& g = P->prog;
+    const int nt = P->ntab;
+    const bool lone = P->n_pairwise == 1 && P->tw_cols == 0 && P->t[0].len == 1;
+    if (lone && (P->order == EFFSC_MSB || g.degree == 1)) return read_first(P, 0, out);
+    HF even[4];
+    for (int c = 0; c < nt; c++) {
+        even[c] = hf(0);
+        if (P->t[c].len == 1) TRY(read_first(P, c, &even[c]));
+    }
+    HF coef[4] = {hf(0), hf(0), hf(0), hf(0)};
+    for (u32 t = 0; t < g.nterms; t++) {
+        const ExprTerm& T = g.t[t];
+        HF p = hf(T.k[0], T.k[1], T.k[2]);
+        for (u32 f = 0; f < T.nf; f++) {
+            const int col = T.f[f] >> 1, odd = T.f[f] & 1;
+            if (odd && ((P->tw_cols >> col) & 1))
+                return fail(EFFSC_PANIC, "final_value: the evaluator reads a tablewise odd row, an empty slice "
+                                         "after the last fold (the reference panics)");
+            p = hf_mul(p, odd ? hf(0) : even[col]);
+        }
+        coef[T.coeff] = hf_add(coef[T.coeff], p);
+    }
+    HF h1 = hf(0);
+    for (u32 j = 0; j <= g.degree && j < 4; j++) h1 = hf_add(h1, coef[j]);
+    *out = hf_add(coef[0], h1);
+    return EFFSC_OK;
+}
+
 int final_value(effsc_prover* P, HF* out) {
     *out = hf(0);
     switch (P->kind) {
@@ -1212,6 +1295,7 @@ int final_value(effsc_prover* P, HF* out) {
     }
     case EFFSC_COEF: { // src/provers/coefficient.rs:300-329: h(0) + h(1) of the
         // product evaluator on (singleton, 0) pairs = product of the singletons
+        if (P->expr) return final_value_expr(P, out);
         if (P->ntab == 1 && P->t[0].len == 1) return read_first(P, 0, out);
         HF acc = hf(1);
         for (int i = 0; i < P->ntab; i++) {
@@ -1480,6 +1564,16 @@ int effsc_diag_mulmod_rate(effsc_ctx* ctx, double* mulmod_per_s, double* fp3_mul
     return EFFSC_OK;
 }
 
+int effsc_diag_accumulate_rate(effsc_ctx* ctx, double* mac_per_s, double* reduce_per_s) {
+    if (!ctx) return fail(EFFSC_INVALID_ARG, "ctx is NULL");
+    CK(cudaSetDevice(ctx->device));
+    double a = 0, b = 0;
+    if (!diag_accumulate_rate(ctx->stream, &a, &b)) return fail(EFFSC_CUDA_ERROR, "accumulate microbenchmark failed");
+    if (mac_per_s) *mac_per_s = a;
+    if (reduce_per_s) *reduce_per_s = b;
+    return EFFSC_OK;
+}
+
 int effsc_diag_transcript_latency(effsc_ctx* ctx, double* ns_per_permutation, double* ns_per_round_step) {
     if (!ctx) return fail(EFFSC_INVALID_ARG, "ctx is NULL");
     CK(cudaSetDevice(ctx->device));
@@ -1566,6 +1660,81 @@ int effsc_prover_create(effsc_ctx* ctx, int kind, int order, int field, int repr
     int rc = prover_common_init(P);
     for (int i = 0; i < n_tables && rc == EFFSC_OK; i++) rc = upload_table(P, P->t[i], tables[i], lens[i], ncomp[i], repr);
     if (rc == EFFSC_OK) rc = normalize_masks(P);
+    if (rc == EFFSC_OK) { cudaError_t e = cudaStreamSynchronize(ctx->stream); if (e != cudaSuccess) rc = fail(EFFSC_CUDA_ERROR, "upload: %s", cudaGetErrorString(e)); }
+    if (rc != EFFSC_OK) { release_prover(P); return rc; }
+    snapshot_initial(P);
+    *out = P;
+    return EFFSC_OK;
+}
+
+int effsc_coef_expr_create(effsc_ctx* ctx, int order, int field, int repr, int degree, int n_pairwise,
+                           const uint64_t* const* pairwise, const int* pw_ncomp, int n_tablewise,
+                           const uint64_t* const* tablewise, const size_t* tw_widths, const int* tw_ncomp,
+                           size_t len, const effsc_term* terms, size_t n_terms, effsc_prover** out) {
+    if (!ctx || !out || (n_terms && !terms)) return fail(EFFSC_INVALID_ARG, "NULL argument");
+    TRY(check_field(field));
+    if (order != EFFSC_MSB && order != EFFSC_LSB) return fail(EFFSC_INVALID_ARG, "order must be MSB or LSB");
+    if (degree < 0 || degree > 3) return fail(EFFSC_UNSUPPORTED, "declarative evaluators of degree 0..3 (got %d)", degree);
+    if (n_pairwise < 0 || n_tablewise < 0 || (n_pairwise && (!pairwise || !pw_ncomp)) ||
+        (n_tablewise && (!tablewise || !tw_widths || !tw_ncomp)))
+        return fail(EFFSC_INVALID_ARG, "NULL table arrays");
+    size_t ncols = (size_t)n_pairwise;
+    for (int i = 0; i < n_tablewise; i++) ncols += tw_widths[i];
+    if (ncols < 1 || ncols > 4)
+        return fail(EFFSC_UNSUPPORTED, "declarative evaluators read 1..4 columns (pairwise tables plus tablewise "
+                                       "columns); got %zu", ncols);
+    if (n_terms > (size_t)EXPR_MAX_TERMS) return fail(EFFSC_UNSUPPORTED, "at most %d terms", EXPR_MAX_TERMS);
+    ExprProgram prog;
+    memset(&prog, 0, sizeof prog);
+    prog.nterms = (u32)n_terms;
+    prog.degree = (u32)(degree < 1 ? 1 : degree);    // degree 0 sends [h(0)] like degree 1
+    prog.ncols = (u32)ncols;
+    for (size_t t = 0; t < n_terms; t++) {
+        const effsc_term& T = terms[t];
+        if ((int)T.coeff > degree || T.n_factors > (u32)EXPR_MAX_FACTORS)
+            return fail(EFFSC_INVALID_ARG, "term %zu: coefficient %u or %u factors out of range", t, T.coeff, T.n_factors);
+        prog.t[t].coeff = (unsigned char)T.coeff;
+        prog.t[t].nf = (unsigned char)T.n_factors;
+        for (u32 f = 0; f < T.n_factors; f++) {
+            if (T.factors[f] >= 2 * ncols) return fail(EFFSC_INVALID_ARG, "term %zu: factor %u names no column", t, T.factors[f]);
+            prog.t[t].f[f] = (unsigned char)T.factors[f];
+        }
+        const HF k = load_elem(T.k, field, repr);
+        for (int c = 0; c < 3; c++) prog.t[t].k[c] = k.c[c];
+    }
+    for (int i = 0; i < n_pairwise; i++) {
+        if (pw_ncomp[i] != 1 && pw_ncomp[i] != 3) return fail(EFFSC_INVALID_ARG, "ncomp must be 1 or 3");
+        if (pw_ncomp[i] == 3 && field != EFFSC_FP3) return fail(EFFSC_INVALID_ARG, "Fp3 table for an Fp prover");
+        if (len && !pairwise[i]) return fail(EFFSC_INVALID_ARG, "pairwise table %d is NULL", i);
+    }
+    for (int i = 0; i < n_tablewise; i++) {
+        if (tw_ncomp[i] != 1 && tw_ncomp[i] != 3) return fail(EFFSC_INVALID_ARG, "ncomp must be 1 or 3");
+        if (tw_ncomp[i] == 3 && field != EFFSC_FP3) return fail(EFFSC_INVALID_ARG, "Fp3 table for an Fp prover");
+        if (len && tw_widths[i] && !tablewise[i]) return fail(EFFSC_INVALID_ARG, "tablewise table %d is NULL", i);
+    }
+    CK(cudaSetDevice(ctx->device));
+    effsc_prover* P = new effsc_prover();
+    P->ctx = ctx; P->kind = EFFSC_COEF; P->order = order; P->field = field; P->repr = repr; P->ntab = (int)ncols;
+    P->expr = true;
+    P->prog = prog;
+    P->n_pairwise = n_pairwise;
+    int rc = prover_common_init(P);
+    int col = 0;
+    for (int i = 0; i < n_pairwise && rc == EFFSC_OK; i++, col++)
+        rc = upload_table(P, P->t[col], pairwise[i], len, pw_ncomp[i], repr);
+    // a tablewise table is len rows of width w (row-major, ncomp words per
+    // element); column c of it becomes its own table of len elements
+    for (int i = 0; i < n_tablewise && rc == EFFSC_OK; i++) {
+        const size_t w = tw_widths[i], nc = (size_t)tw_ncomp[i];
+        std::vector<uint64_t> colbuf(len * nc);
+        for (size_t c = 0; c < w && rc == EFFSC_OK; c++, col++) {
+            for (size_t r = 0; r < len; r++)
+                for (size_t k = 0; k < nc; k++) colbuf[r * nc + k] = tablewise[i][(r * w + c) * nc + k];
+            rc = upload_table(P, P->t[col], colbuf.data(), len, (int)nc, repr);
+            P->tw_cols |= 1u << col;
+            if (rc == EFFSC_OK) { cudaError_t e = cudaStreamSynchronize(ctx->stream); if (e != cudaSuccess) rc = fail(EFFSC_CUDA_ERROR, "upload: %s", cudaGetErrorString(e)); }
+        }
+    }
     if (rc == EFFSC_OK) { cudaError_t e = cudaStreamSynchronize(ctx->stream); if (e != cudaSuccess) rc = fail(EFFSC_CUDA_ERROR, "upload: %s", cudaGetErrorString(e)); }
     if (rc != EFFSC_OK) { release_prover(P); return rc; }
     snapshot_initial(P);
@@ -2222,6 +2391,52 @@ int effsc_fold(effsc_ctx* ctx, int field, int repr, const uint64_t* values, size
     effsc_prover* P = nullptr;
     TRY(effsc_prover_create(ctx, EFFSC_ML, EFFSC_MSB, field, repr, 1, tabs, lens, nc, &P));
     int rc = do_finalize(P, host_chal(P, weight), false);
+    if (rc == EFFSC_OK) {
+        *out_len = P->t[0].len;
+        rc = effsc_prover_read_table(P, 0, out);
+    }
+    release_prover(P);
+    return rc;
+}
+
+int effsc_compute_sumcheck_polynomial(effsc_ctx* ctx, int field, int repr, const uint64_t* values, size_t len,
+                                      int ncomp, uint64_t* out_s0_s1) {
+    if (!ctx || !out_s0_s1 || (len && !values)) return fail(EFFSC_INVALID_ARG, "NULL argument");
+    TRY(check_field(field));
+    if (!len) {
+        // src/multilinear_sumcheck.rs:110-112: an empty table gives (0, 0)
+        memset(out_s0_s1, 0, 2 * (size_t)field * sizeof(uint64_t));
+        return EFFSC_OK;
+    }
+    const uint64_t* tabs[1] = {values};
+    size_t lens[1] = {len};
+    int nc[1] = {ncomp};
+    effsc_prover* P = nullptr;
+    TRY(effsc_prover_create(ctx, EFFSC_ML, EFFSC_MSB, field, repr, 1, tabs, lens, nc, &P));
+    int rc = effsc_prover_round(P, nullptr, nullptr, out_s0_s1);
+    release_prover(P);
+    return rc;
+}
+
+int effsc_fused_fold_and_compute_polynomial(effsc_ctx* ctx, int field, int repr, const uint64_t* values, size_t len,
+                                            int ncomp, const uint64_t* weight, uint64_t* out, size_t* out_len,
+                                            uint64_t* out_s0_s1) {
+    if (!ctx || !weight || !out_len || !out_s0_s1 || (len && (!values || !out)))
+        return fail(EFFSC_INVALID_ARG, "NULL argument");
+    TRY(check_field(field));
+    if (!len) {
+        *out_len = 0;
+        memset(out_s0_s1, 0, 2 * (size_t)field * sizeof(uint64_t));
+        return EFFSC_OK;
+    }
+    const uint64_t* tabs[1] = {values};
+    size_t lens[1] = {len};
+    int nc[1] = {ncomp};
+    effsc_prover* P = nullptr;
+    TRY(effsc_prover_create(ctx, EFFSC_ML, EFFSC_MSB, field, repr, 1, tabs, lens, nc, &P));
+    // a round with a challenge: the fold (fused with the evaluation for
+    // power-of-two lengths >= 4, else fold then evaluate) and the new (s0, s1)
+    int rc = effsc_prover_round(P, weight, nullptr, out_s0_s1);
     if (rc == EFFSC_OK) {
         *out_len = P->t[0].len;
         rc = effsc_prover_read_table(P, 0, out);

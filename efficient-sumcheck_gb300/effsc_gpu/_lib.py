@@ -28,6 +28,7 @@ SIGNATURES = {
     "effsc_profile_get": (ci, [sz, ctypes.c_char_p, sz, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_uint64)]),
     "effsc_profile_clear": (None, []),
     "effsc_diag_mulmod_rate": (ci, [vp, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]),
+    "effsc_diag_accumulate_rate": (ci, [vp, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]),
     "effsc_ctx_create": (ci, [ci, ctypes.POINTER(vp)]),
     "effsc_ctx_destroy": (ci, [vp]),
     "effsc_ctx_set_stream": (ci, [vp, vp]),
@@ -55,6 +56,11 @@ SIGNATURES = {
     "effsc_transcript_challenge": (ci, [vp, u64p]),
     "effsc_verify": (ci, [ci, ci, u64p, sz, sz, vp, u8p, sz, u64p, u64p, u64p]),
     "effsc_fold": (ci, [vp, ci, ci, u64p, sz, ci, u64p, u64p, ctypes.POINTER(sz)]),
+    "effsc_compute_sumcheck_polynomial": (ci, [vp, ci, ci, u64p, sz, ci, u64p]),
+    "effsc_coef_expr_create": (ci, [vp, ci, ci, ci, ci, ci, ctypes.POINTER(u64p), ctypes.POINTER(ci), ci,
+                                    ctypes.POINTER(u64p), ctypes.POINTER(sz), ctypes.POINTER(ci), sz, vp, sz,
+                                    ctypes.POINTER(vp)]),
+    "effsc_fused_fold_and_compute_polynomial": (ci, [vp, ci, ci, u64p, sz, ci, u64p, u64p, ctypes.POINTER(sz), u64p]),
     "effsc_build_eq_table": (ci, [vp, ci, ci, u64p, sz, u64p]),
     "effsc_gen_uniform": (ci, [vp, ctypes.c_uint64, ctypes.c_uint64, u64p, u64p]),
     "effsc_table_seed": (ctypes.c_uint64, [ctypes.c_uint64, ctypes.c_uint64]),

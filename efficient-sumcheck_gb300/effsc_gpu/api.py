@@ -344,17 +344,110 @@ class InnerProductProverLSB(InnerProductProver):
     kind, order = IP, LSB
 
 
+class _Term(ctypes.Structure):
+    _fields_ = [("coeff", ctypes.c_uint32), ("n_factors", ctypes.c_uint32),
+                ("factors", ctypes.c_uint32 * 4), ("k", ctypes.c_uint64 * 3)]
+
+
+def pw_even(i):
+    """Factor: the even (lo) element of pairwise table i."""
+    return ("pw", i, 0, 0)
+
+
+def pw_odd(i):
+    return ("pw", i, 0, 1)
+
+
+def tw_even(t, col):
+    """Factor: column `col` of the even (lo) row of tablewise table t."""
+    return ("tw", t, col, 0)
+
+
+def tw_odd(t, col):
+    return ("tw", t, col, 1)
+
+
+class Evaluator:
+    """A declarative RoundPolyEvaluator (src/coefficient_sumcheck.rs:50-76):
+    accumulate_pair adds, for every term (coeff, k, factors), k times the
+    product of the factors into coefficient `coeff`.  Factors are pw_even(i),
+    pw_odd(i), tw_even(t, c), tw_odd(t, c); k is a field element (an int, or
+    3 words for Fp3), in the prover's representation."""
+
+    def __init__(self, degree, terms):
+        self.deg = int(degree)
+        self.terms = [(int(c), k, list(f)) for c, k, f in terms]
+
+    def degree(self):
+        return self.deg
+
+    def _program(self, n_pairwise, widths, field):
+        base = [0]
+        for w in widths:
+            base.append(base[-1] + w)
+        arr = (_Term * max(1, len(self.terms)))()
+        for i, (c, k, fs) in enumerate(self.terms):
+            arr[i].coeff = c
+            arr[i].n_factors = len(fs)
+            for j, (kind, t, col, odd) in enumerate(fs):
+                column = t if kind == "pw" else n_pairwise + base[t] + col
+                arr[i].factors[j] = 2 * column + odd
+            kv = _elem(k, field)
+            for j in range(field):
+                arr[i].k[j] = int(kv[j])
+        return arr
+
+
 class CoefficientProver(_Prover):
-    """src/provers/coefficient.rs:18-330 with the device product evaluator:
-    accumulate_pair adds the coefficients of prod_i (lo_i + x (hi_i - lo_i))
-    over the pairwise tables (1 to 3 of them; degree = number of tables)."""
+    """src/provers/coefficient.rs:18-330.  Without `evaluator`: the device
+    product evaluator -- accumulate_pair adds the coefficients of
+    prod_i (lo_i + x (hi_i - lo_i)) over the pairwise tables (1 to 3 of them;
+    degree = number of tables).  With `evaluator` (an Evaluator) and optional
+    `tablewise` tables (each an (n, w) array of rows, or (n, w, 3) for Fp3):
+    that evaluator over pairwise and tablewise tables; table(i) reads column i
+    (the pairwise tables, then every tablewise column)."""
     kind, order = COEF, MSB
 
-    def __init__(self, pairwise, field=FP3, repr=CANONICAL, ctx=None):
-        super().__init__(list(pairwise), field, repr, ctx)
+    def __init__(self, pairwise, field=FP3, repr=CANONICAL, ctx=None, evaluator=None, tablewise=()):
+        if evaluator is None and not len(tablewise):
+            super().__init__(list(pairwise), field, repr, ctx)
+            self.n_pairwise = len(pairwise)
+            return
+        if evaluator is None:
+            raise ValueError("tablewise tables need an evaluator")
+        self.ctx = ctx or Context.default()
+        self.field, self.repr = field, repr
+        self.evaluator = evaluator
+        pws = [_as_table(t, field) for t in pairwise]
+        tws, widths, tnc = [], [], []
+        for t in tablewise:
+            a = np.ascontiguousarray(np.asarray(t, dtype=np.uint64))
+            if a.ndim == 2:
+                tnc.append(1)
+            elif a.ndim == 3 and a.shape[2] == 3 and field == FP3:
+                tnc.append(3)
+            else:
+                raise ValueError("tablewise table must be (n, w) or (n, w, 3)")
+            tws.append(a)
+            widths.append(a.shape[1])
+        lens = {a.shape[0] for a, _ in pws} | {a.shape[0] for a in tws}
+        if len(lens) != 1:
+            raise ValueError("every table must have the same number of entries / rows")
+        n = lens.pop()
+        prog = evaluator._program(len(pws), widths, field)
+        np_, nt = len(pws), len(tws)
+        h = vp()
+        check(load().effsc_coef_expr_create(
+            self.ctx.h, self.order, field, repr, evaluator.degree(), np_,
+            (u64p * max(np_, 1))(*[_p(a) for a, _ in pws]), (ctypes.c_int * max(np_, 1))(*[c for _, c in pws]), nt,
+            (u64p * max(nt, 1))(*[_p(a) for a in tws]), (ctypes.c_size_t * max(nt, 1))(*widths),
+            (ctypes.c_int * max(nt, 1))(*tnc), n, ctypes.cast(prog, vp), len(evaluator.terms), ctypes.byref(h)))
+        self.h = h
+        self.n_pairwise = np_
+        self._keep = (pws, tws)
 
     def pairwise(self):
-        return [self.table(i) for i in range(self.degree())]
+        return [self.table(i) for i in range(self.n_pairwise)]
 
 
 class CoefficientProverLSB(CoefficientProver):
@@ -387,7 +480,7 @@ class EqFactoredProver(_Prover):
             return z, z.copy()
         from .field import f_mul
         p0 = self.table(0)[0]
-        e = f_mul(self.table(1)[0], self.table(2)[0], self.field)
+        e = f_mul(self.table(1)[0], self.table(2)[0], self.field, self.repr)
         return p0, e
 
 
@@ -443,6 +536,52 @@ def sumcheck(prover, num_rounds, transcript, hook=None):
     if prev is not None:
         prover.finalize(prev)
     return SumcheckProof(rps, chs, prover.final_value())
+
+
+@dataclass
+class CoefficientSumcheck:
+    """Legacy return type, src/coefficient_sumcheck.rs:11-15: every round's
+    polynomial in coefficient form (degree + 1 coefficients) and challenges."""
+    prover_messages: list
+    verifier_messages: list
+
+
+def _coefficients(wire, aux, d, field, repr):
+    """The round polynomial's coefficients c0..cd from the EvalsInfty wire and
+    the (c0, c1) pair: c_d = h(inf); for degree 3, c2 from h(2)."""
+    from .field import f_add, f_sub, f_mul, f_scale
+    c0, c1 = aux[0], aux[1]
+    if d <= 1:
+        return [c0] if d == 0 else [c0, c1]
+    if d == 2:
+        return [c0, c1, wire[1]]
+    c3 = wire[1]
+    # h(2) = c0 + 2 c1 + 4 c2 + 8 c3
+    t = f_sub(f_sub(f_sub(wire[2], c0, field, repr), f_scale(c1, 2, field, repr), field, repr),
+              f_scale(c3, 8, field, repr), field, repr)
+    return [c0, c1, f_scale(t, None, field, repr, inv=4), c3]
+
+
+def coefficient_sumcheck(evaluator, tablewise, pairwise, n_rounds, transcript, field=FP3, repr=CANONICAL):
+    """src/coefficient_sumcheck.rs:255-365: pairs (2k, 2k+1); each round sends
+    the first `degree` coefficients of the round polynomial (the leading one
+    is omitted), squeezes the challenge and reduces every table with it.
+    Returns CoefficientSumcheck and the prover (its tables are the reduced
+    tables)."""
+    pr = CoefficientProverLSB(pairwise, field=field, repr=repr, evaluator=evaluator, tablewise=tablewise)
+    d = evaluator.degree()
+    msgs, chals, prev = [], [], None
+    for _ in range(n_rounds):
+        wire, aux = pr.round(prev, aux=True)
+        coeffs = _coefficients(wire, aux, d, field, repr)
+        for c in coeffs[:d]:
+            transcript.send(c)
+        msgs.append(np.array(coeffs, dtype=np.uint64).reshape(len(coeffs), field))
+        prev = transcript.challenge()
+        chals.append(prev)
+    if prev is not None:
+        pr.finalize(prev)
+    return CoefficientSumcheck(msgs, chals), pr
 
 
 def noop_hook(_round, _transcript):
@@ -535,6 +674,35 @@ def fold(values, weight, field=FP3, repr=CANONICAL, ctx=None):
     check(load().effsc_fold(ctx.h, field, repr, _p(a), n, nc, _p(w), _p(out), ctypes.byref(ol)))
     out = out[: ol.value]
     return out if field == FP3 else out.reshape(-1)
+
+
+def compute_sumcheck_polynomial(values, field=FP3, repr=CANONICAL, ctx=None):
+    """src/multilinear_sumcheck.rs:86-124: (s0, s1) of a half-split table with
+    implicit zero padding (s0 = low half plus the unpaired tail, s1 = high half)."""
+    ctx = ctx or Context.default()
+    a, nc = _as_table(values, field)
+    out = np.zeros((2, field), dtype=np.uint64)
+    check(load().effsc_compute_sumcheck_polynomial(ctx.h, field, repr, _p(a) if a.shape[0] else None, a.shape[0],
+                                                   nc, _p(out)))
+    return (out[0], out[1]) if field == FP3 else (out[0, 0], out[1, 0])
+
+
+def fused_fold_and_compute_polynomial(values, weight, field=FP3, repr=CANONICAL, ctx=None):
+    """src/multilinear_sumcheck.rs:189-254: the table folded by weight (as
+    `fold`) and the folded table's (s0, s1).  The reference folds its Vec in
+    place; here the folded table is returned: (folded, (s0, s1))."""
+    ctx = ctx or Context.default()
+    a, nc = _as_table(values, field)
+    w = _elem(weight, field)
+    n = a.shape[0]
+    out = np.zeros((max(n, 1), field), dtype=np.uint64)
+    ol = ctypes.c_size_t()
+    s = np.zeros((2, field), dtype=np.uint64)
+    check(load().effsc_fused_fold_and_compute_polynomial(ctx.h, field, repr, _p(a) if n else None, n, nc, _p(w),
+                                                         _p(out), ctypes.byref(ol), _p(s)))
+    out = out[: ol.value]
+    folded = out if field == FP3 else out.reshape(-1)
+    return folded, ((s[0], s[1]) if field == FP3 else (s[0, 0], s[1, 0]))
 
 
 def build_eq_table(w, field=FP3, repr=CANONICAL, ctx=None):

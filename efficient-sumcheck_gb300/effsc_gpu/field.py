@@ -27,3 +27,23 @@ def f_mul(a, b, field=3, repr=0):
             prod[i + j] += a[i] * b[j]
     c = [(prod[0] + W * prod[3]) % P, (prod[1] + W * prod[4]) % P, prod[2] % P]
     return np.array([from_canonical(x, repr) for x in c], dtype=np.uint64)
+
+
+def _elem_list(a, field, repr):
+    return [to_canonical(x, repr) for x in np.asarray(a).reshape(-1)[:field]]
+
+
+def f_add(a, b, field=3, repr=0):
+    x, y = _elem_list(a, field, repr), _elem_list(b, field, repr)
+    return np.array([from_canonical((u + v) % P, repr) for u, v in zip(x, y)], dtype=np.uint64)
+
+
+def f_sub(a, b, field=3, repr=0):
+    x, y = _elem_list(a, field, repr), _elem_list(b, field, repr)
+    return np.array([from_canonical((u - v) % P, repr) for u, v in zip(x, y)], dtype=np.uint64)
+
+
+def f_scale(a, s, field=3, repr=0, inv=None):
+    """a times the integer s, or times 1/inv."""
+    m = pow(inv, -1, P) if inv is not None else s % P
+    return np.array([from_canonical(u * m % P, repr) for u in _elem_list(a, field, repr)], dtype=np.uint64)

@@ -137,6 +137,34 @@ int effsc_gkr_create(effsc_ctx* ctx, int field, int repr, const uint64_t* add, c
 /* GkrProver::claimed_w_values, src/provers/gkr.rs:87-93: (W(b*), W(c*)) once
  * all 2 log2(n) variables are bound, else zeros; out = 2 elements. */
 int effsc_gkr_claimed_w_values(effsc_prover* p, uint64_t* out);
+/* CoefficientProver::new / CoefficientProverLSB::new (src/provers/coefficient.rs:28-40,
+ * coefficient_lsb.rs:37-99) with a declarative RoundPolyEvaluator
+ * (src/coefficient_sumcheck.rs:50-76): per pair of rows, every term adds
+ *   k * (product of its factors)
+ * into coefficient `coeff` of the round polynomial.  A factor names the even
+ * (lo) or odd (hi) element of a column: factor = column * 2 + (0 | 1), the
+ * columns being the pairwise tables (0 .. n_pairwise-1) and then the columns
+ * of each tablewise table in order (a tablewise table of width w is len rows
+ * of w elements, row-major, tw_ncomp words each; its row pair is its columns'
+ * element pairs).  Every table has len entries (rows).  Degree 0..3, at most
+ * 4 columns, 16 terms, 4 factors per term; k is one field element in the
+ * prover's representation.  The prover is then driven like the others
+ * (effsc_prover_round, effsc_prove, finalize, final_value, read_table of
+ * column i); out_aux of a round holds (c0, c1).  This covers evaluators whose
+ * accumulate_pair is a sum of constant multiples of products of pair
+ * elements -- e.g. the reference's Degree1, Degree2, Mixed and InnerProduct
+ * test evaluators (src/coefficient_sumcheck.rs:379-430); a Rust closure of
+ * any other shape cannot run on the device. */
+typedef struct {
+    uint32_t coeff;        /* coefficient index, 0..degree */
+    uint32_t n_factors;    /* 0..4; 0 adds k once per pair */
+    uint32_t factors[4];   /* column * 2 + (0: even element, 1: odd element) */
+    uint64_t k[3];         /* the constant, `field` words */
+} effsc_term;
+int effsc_coef_expr_create(effsc_ctx* ctx, int order, int field, int repr, int degree, int n_pairwise,
+                           const uint64_t* const* pairwise, const int* pw_ncomp, int n_tablewise,
+                           const uint64_t* const* tablewise, const size_t* tw_widths, const int* tw_ncomp,
+                           size_t len, const effsc_term* terms, size_t n_terms, effsc_prover** out);
 /* Same constructors with the tables already in device memory (canonical,
  * structure-of-arrays: c0 of every element, then c1, then c2 when ncomp = 3);
  * the prover copies nothing and does not take ownership: the caller keeps the
@@ -244,6 +272,24 @@ int effsc_verify(int field, int repr, const uint64_t* claimed_sum, size_t degree
 int effsc_fold(effsc_ctx* ctx, int field, int repr, const uint64_t* values, size_t len, int ncomp,
                const uint64_t* weight, uint64_t* out, size_t* out_len);
 
+/* ---- round polynomial of a multilinear table (the WHIR-facing helpers) -----
+ * compute_sumcheck_polynomial (src/multilinear_sumcheck.rs:86-124):
+ * out_s0_s1 = (s0, s1) of values with implicit zero padding to the next
+ * power of two -- s0 = sum of the low half (plus the unpaired tail), s1 = sum
+ * of the high half; (v[0], 0) for one element, (0, 0) for none.  2 elements
+ * of `field` words. */
+int effsc_compute_sumcheck_polynomial(effsc_ctx* ctx, int field, int repr, const uint64_t* values, size_t len,
+                                      int ncomp, uint64_t* out_s0_s1);
+/* fused_fold_and_compute_polynomial (src/multilinear_sumcheck.rs:189-254):
+ * folds values by weight exactly as effsc_fold does (*out_len elements of
+ * `field` words to out) and returns the folded table's (s0, s1) as
+ * effsc_compute_sumcheck_polynomial would.  Power-of-two lengths >= 4 run as
+ * one fused pass over the quadruples (k, k+L/4, k+L/2, k+3L/4); other lengths
+ * fold then evaluate, as the reference falls back to (:194-196). */
+int effsc_fused_fold_and_compute_polynomial(effsc_ctx* ctx, int field, int repr, const uint64_t* values, size_t len,
+                                            int ncomp, const uint64_t* weight, uint64_t* out, size_t* out_len,
+                                            uint64_t* out_s0_s1);
+
 /* ---- eq table ----------------------------------------------------------------
  * eq(w, .) over {0,1}^num_vars in MSB layout (EqFactored's build_eq_table,
  * src/provers/eq_factored.rs:217-239), written to host `out`
@@ -263,6 +309,14 @@ uint64_t effsc_table_seed(uint64_t seed, uint64_t table);
  * Fp3 x Fp3 products, each from independent dependency chains in every
  * thread of a full grid; the denominator of the integer-multiply roofline. */
 int effsc_diag_mulmod_rate(effsc_ctx* ctx, double* mulmod_per_s, double* fp3_mul_per_s);
+/* Accumulate-form integer rates (no reference counterpart): products of
+ * 64-bit operands added unreduced into independent lazy sums (two per
+ * thread, the split accumulator of the folds) per second, and reductions of
+ * a 160-bit sum to a canonical residue per second, each on a full grid.
+ * These are the operations the round kernels execute (a product costs no
+ * reduction until its sum is stored), so they bound the integer roofline:
+ * products / mac_per_s + reductions / reduce_per_s. */
+int effsc_diag_accumulate_rate(effsc_ctx* ctx, double* mac_per_s, double* reduce_per_s);
 
 /* Transcript latency probe (no reference counterpart): one warp runs 1000
  * Keccak-f[1600] permutations, then 1000 round steps (send one Fp3 element,
