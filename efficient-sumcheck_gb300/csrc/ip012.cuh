@@ -396,25 +396,10 @@ __device__ __forceinline__ void ring_drain(StageRing<S>& R, u32 i, u32* status) 
     }
 }
 
-// Barrier 1..4 of warps w and w + 4 (64 threads); immediate IDs so that the
-// kernel reserves 5 barriers, not all 16.
-__device__ __forceinline__ void pair_sync(int id) {
-    switch (id) {
-    case 1: asm volatile("bar.sync 1, 64;" ::: "memory"); break;
-    case 2: asm volatile("bar.sync 2, 64;" ::: "memory"); break;
-    case 3: asm volatile("bar.sync 3, 64;" ::: "memory"); break;
-    default: asm volatile("bar.sync 4, 64;" ::: "memory"); break;
-    }
-}
-
 constexpr int IP012_TQ = 128;    // octets per tile of the first pass
 constexpr int IP012_S = 4;       // its stages: 4 x 16 KB
-constexpr int IP3X_TQ = 128;     // items (octet pairs) per tile of the second pass
-constexpr int IP3X_S = 3;        // its stages: 3 x 32 KB
 constexpr int IP012_STAGE_WORDS = 2 * 8 * IP012_TQ;
-constexpr int IP3X_STAGE_WORDS = 2 * 16 * IP3X_TQ;
 constexpr int IP012_SMEM = IP012_S * IP012_STAGE_WORDS * 8;
-constexpr int IP3X_SMEM = IP3X_S * IP3X_STAGE_WORDS * 8;
 
 // Pass 1, staged.  Tile = IP012_TQ octets; a stage holds, per table, the
 // tile's 8 entries of each octet (MSB: 8 chunks, one per j, of TQ words; LSB:
@@ -476,99 +461,6 @@ __device__ __forceinline__ void ip012_staged_body(const RoundArgs& a, u32 ntiles
         return;
     }
     ip012_reduce_and_finalize(sums, group, a, gridDim.x, blockIdx.x);
-}
-
-// Pass 2, staged.  Tile = IP3X_TQ items; warps 0..3 fold table a, warps 4..7
-// table b (thread item ml = threadIdx.x % TQ): each folds its item's two
-// octets (the round-3 pair) and stores them, then the two warps holding the
-// same items exchange the folded pairs through shared memory (a named barrier
-// per warp pair) and split round 3's products: warps 0..3 accumulate
-// q0 = lo_a lo_b, warps 4..7 qinf = (hi_a - lo_a)(hi_b - lo_b).
-// Stage layout per table: MSB 16 chunks (octet m then m + H, j = 0..7) of TQ
-// words; LSB the tile's 16 TQ consecutive entries.
-template <bool LSB>
-__device__ __forceinline__ void ip3x_staged_body(const RoundArgs& a, u32 ntiles) {
-    extern __shared__ __align__(128) u64 stg[];
-    __shared__ StageRing<IP3X_S> R;
-    __shared__ u64 xch[2][6][IP3X_TQ];
-    constexpr int TQ = IP3X_TQ, S = IP3X_S, SW = IP3X_STAGE_WORDS;
-    const u64 O = a.L >> 3, H = O >> 1;
-    const u64* X[2] = {a.t[0].in[0], a.t[1].in[0]};
-    auto issue = [&](u32 tile, int s) {
-        mbar_expect_tx(&R.bar[s], (u32)(SW * 8));
-        u64* dst = stg + (size_t)s * SW;
-#pragma unroll
-        for (int t = 0; t < 2; t++) {
-            if (LSB) {
-                tma_load_1d(dst + t * 16 * TQ, X[t] + (u64)tile * 16 * TQ, 16 * TQ * 8, &R.bar[s]);
-            } else {
-#pragma unroll
-                for (int h = 0; h < 2; h++)
-#pragma unroll
-                    for (int j = 0; j < 8; j++)
-                        tma_load_1d(dst + ((t * 2 + h) * 8 + j) * TQ, X[t] + h * H + j * O + (u64)tile * TQ, TQ * 8,
-                                    &R.bar[s]);
-            }
-        }
-    };
-    ring_start<S>(R, ntiles, issue);
-    const int t = threadIdx.x >= TPB / 2;     // the table this thread folds
-    const int ml = threadIdx.x & (TQ - 1);
-    const int pairbar = 1 + ((threadIdx.x >> 5) & 3);
-    const Fold3K K = fold3_prepare(f3_make(a.chal_ptr[0], a.chal_ptr[1], a.chal_ptr[2]),
-                                   f3_make(a.chal_ptr[3], a.chal_ptr[4], a.chal_ptr[5]),
-                                   f3_make(a.chal_ptr[6], a.chal_ptr[7], a.chal_ptr[8]));
-    u64* const* out = a.t[t].out;
-    ProdAcc<true, true> q;
-    q.init();
-    bool abort = false;
-    u32 i = 0;
-    for (u32 tile = blockIdx.x; tile < ntiles; tile += gridDim.x, i++) {
-        if (!mbar_wait_bounded(&R.bar[i % S], (i / S) & 1u)) { abort = true; break; }
-        const u64* st_ = stg + (size_t)(i % S) * SW + (size_t)t * 16 * TQ;
-        u64 x[8], y[8];
-        if (LSB) {
-            const ulonglong2* p = (const ulonglong2*)(st_ + 16 * ml);
-            const ulonglong2 a01 = p[0], a23 = p[1], a45 = p[2], a67 = p[3];
-            const ulonglong2 b01 = p[4], b23 = p[5], b45 = p[6], b67 = p[7];
-            x[0] = a01.x; x[4] = a01.y; x[2] = a23.x; x[6] = a23.y; x[1] = a45.x; x[5] = a45.y; x[3] = a67.x; x[7] = a67.y;
-            y[0] = b01.x; y[4] = b01.y; y[2] = b23.x; y[6] = b23.y; y[1] = b45.x; y[5] = b45.y; y[3] = b67.x; y[7] = b67.y;
-        } else {
-#pragma unroll
-            for (int j = 0; j < 8; j++) {
-                x[j] = st_[j * TQ + ml];
-                y[j] = st_[(8 + j) * TQ + ml];
-            }
-        }
-        ring_release<S>(R, i, ntiles, issue);
-        const F3 lo = fold3(x, K), hi = fold3(y, K);
-        const u64 m = (u64)tile * TQ + ml;
-        if (LSB) {
-            ((ulonglong2*)out[0])[m] = make_ulonglong2(lo.c0, hi.c0);
-            ((ulonglong2*)out[1])[m] = make_ulonglong2(lo.c1, hi.c1);
-            ((ulonglong2*)out[2])[m] = make_ulonglong2(lo.c2, hi.c2);
-        } else {
-            st<true>(out, m, lo);
-            st<true>(out, m + H, hi);
-        }
-        xch[t][0][ml] = lo.c0; xch[t][1][ml] = lo.c1; xch[t][2][ml] = lo.c2;
-        xch[t][3][ml] = hi.c0; xch[t][4][ml] = hi.c1; xch[t][5][ml] = hi.c2;
-        pair_sync(pairbar);
-        const int u = 1 - t;
-        const F3 plo = f3_make(xch[u][0][ml], xch[u][1][ml], xch[u][2][ml]);
-        const F3 phi = f3_make(xch[u][3][ml], xch[u][4][ml], xch[u][5][ml]);
-        pair_sync(pairbar);
-        if (t == 0) q.mac(lo, plo);
-        else q.mac(f3_sub<true>(hi, lo), f3_sub<true>(phi, plo));
-    }
-    if (__syncthreads_or(abort)) {
-        ring_drain<S>(R, i, a.status);
-        return;
-    }
-    F3 raw[2];
-    raw[t] = q.result();
-    raw[1 - t] = f3_zero();
-    reduce_and_finalize_seg<2>(raw, a, POL_IP, gridDim.x, blockIdx.x);
 }
 
 }  // namespace effsc

@@ -22,11 +22,6 @@ __global__ void __launch_bounds__(TPB, 2) k_ip_r012s(RoundArgs a, u32 ntiles) {
     chain_enter();
     ip012_staged_body<LSB>(a, ntiles);
 }
-template <bool LSB>
-__global__ void __launch_bounds__(TPB, 2) k_ip_r3xs(RoundArgs a, u32 ntiles) {
-    chain_enter();
-    ip3x_staged_body<LSB>(a, ntiles);
-}
 
 // The dynamic shared-memory limit is a per-device function attribute: set
 // once per device (one bit each), safe when threads race to set it.
@@ -51,17 +46,7 @@ bool launch_ip012_staged(bool lsb, const RoundArgs& a, u32 ntiles, int grid, cud
     if (!allow_smem(k_ip_r012s<false>, IP012_SMEM, cfg[0])) return false;
     return launch_chain(k_ip_r012s<false>, grid, TPB, IP012_SMEM, s, a, ntiles);
 }
-bool launch_ip3x_staged(bool lsb, const RoundArgs& a, u32 ntiles, int grid, cudaStream_t s) {
-    static std::atomic<uint64_t> cfg[2];
-    if (lsb) {
-        if (!allow_smem(k_ip_r3xs<true>, IP3X_SMEM, cfg[1])) return false;
-        return launch_chain(k_ip_r3xs<true>, grid, TPB, IP3X_SMEM, s, a, ntiles);
-    }
-    if (!allow_smem(k_ip_r3xs<false>, IP3X_SMEM, cfg[0])) return false;
-    return launch_chain(k_ip_r3xs<false>, grid, TPB, IP3X_SMEM, s, a, ntiles);
-}
 u32 ip012_tile_octets(void) { return IP012_TQ; }
-u32 ip3x_tile_items(void) { return IP3X_TQ; }
 
 bool launch_ip012(bool lsb, const RoundArgs& a, int grid, cudaStream_t s) {
     return lsb ? launch_chain(k_ip_r012<true>, grid, TPB, 0, s, a) : launch_chain(k_ip_r012<false>, grid, TPB, 0, s, a);

@@ -234,14 +234,12 @@ bool launch_ip2x(bool lsb, const RoundArgs& a, int grid, cudaStream_t s);
 // holds r0, r1, r2 as 9 consecutive words).
 bool launch_ip012(bool lsb, const RoundArgs& a, int grid, cudaStream_t s);
 bool launch_ip3x(bool lsb, const RoundArgs& a, int grid, cudaStream_t s);
-// The same passes with the tables streamed through shared memory by bulk
-// copies: ntiles = (L/8) / ip012_tile_octets() tiles of the first pass,
-// (L/16) / ip3x_tile_items() of the second; device-memory tables, 16-byte
-// aligned; at most two blocks per SM for the first pass's partials.
+// The first pass with the tables streamed through shared memory by bulk
+// copies: ntiles = (L/8) / ip012_tile_octets() tiles; device-memory tables,
+// 16-byte aligned; at most two blocks per SM for the partials.  (The second
+// pass keeps direct loads: staged, it measured slower.)
 bool launch_ip012_staged(bool lsb, const RoundArgs& a, u32 ntiles, int grid, cudaStream_t s);
-bool launch_ip3x_staged(bool lsb, const RoundArgs& a, u32 ntiles, int grid, cudaStream_t s);
 u32 ip012_tile_octets(void);
-u32 ip3x_tile_items(void);
 bool launch_ml01(const RoundArgs& a, int grid, cudaStream_t s);
 bool launch_ml2x(bool ech, const RoundArgs& a, int grid, cudaStream_t s);
 bool launch_gkr01(const RoundArgs& a, int grid, cudaStream_t s);

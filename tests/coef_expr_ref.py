@@ -75,6 +75,10 @@ def horner(c, x):
     return r
 
 
+class RefPanic(Exception):
+    """Where the reference panics."""
+
+
 class RefCoefProver:
     """CoefficientProver / CoefficientProverLSB with a callback evaluator."""
 
@@ -130,5 +134,9 @@ class RefCoefProver:
         coeffs = [R.ZERO] * (self.deg + 1)
         tw = [(t[0], None) if len(t) == 1 else (None, None) for t in self.tw]
         pw = [(t[0], R.ZERO) if len(t) == 1 else (R.ZERO, R.ZERO) for t in self.pw]
-        self.evaluate(coeffs, tw, pw)
+        try:
+            self.evaluate(coeffs, tw, pw)
+        except TypeError:
+            # the reference indexes an empty slice here and panics
+            raise RefPanic("final_value reads an empty tablewise row")
         return R.add(horner(coeffs, R.ZERO), horner(coeffs, R.ONE))
