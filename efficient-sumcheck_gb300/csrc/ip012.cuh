@@ -106,6 +106,21 @@ __device__ __forceinline__ void load_octet(u64 (&v)[8], const u64* X, u64 m, u64
     }
 }
 
+// The inverse of load_octet: octet m back to its table positions.
+template <bool LSB>
+__device__ __forceinline__ void store_octet(const u64 (&v)[8], u64* X, u64 m, u64 O) {
+    if (LSB) {
+        ulonglong2* X2 = (ulonglong2*)X + 4 * m;
+        X2[0] = make_ulonglong2(v[0], v[4]);
+        X2[1] = make_ulonglong2(v[2], v[6]);
+        X2[2] = make_ulonglong2(v[1], v[5]);
+        X2[3] = make_ulonglong2(v[3], v[7]);
+    } else {
+#pragma unroll
+        for (int j = 0; j < 8; j++) X[m + j * O] = v[j];
+    }
+}
+
 static __device__ __noinline__ void finalize_ip012(const u64* S, const RoundArgs& a);
 
 // Block and grid reduction of the 26 sums (each warp holds its group's
@@ -166,7 +181,11 @@ __device__ __forceinline__ void ip012_reduce_and_finalize(const Acc (&s)[IP012_G
 // 14..25 of the same octets (13-14 accumulators per thread instead of 26);
 // the second group's loads of an octet hit what the first group's brought
 // into the caches.  The last block interpolates and runs rounds 0-2.
-template <bool LSB>
+// MIRROR: the tables are in host memory and a.t[0].out[0], a.t[1].out[0]
+// are device buffers of the same length; group 0 writes each octet it loads
+// there, so the tables cross the host link once and the second pass reads
+// HBM.
+template <bool LSB, bool MIRROR = false>
 __device__ __forceinline__ void ip012_body(const RoundArgs& a, u32 bid, u32 nb) {
     constexpr int HALF = TPB / 2;
     const int group = threadIdx.x >= HALF;
@@ -181,6 +200,10 @@ __device__ __forceinline__ void ip012_body(const RoundArgs& a, u32 bid, u32 nb) 
         u64 x[8], y[8];
         load_octet<LSB>(x, A, m, O);
         load_octet<LSB>(y, B, m, O);
+        if (MIRROR && group == 0) {
+            store_octet<LSB>(x, a.t[0].out[0], m, O);
+            store_octet<LSB>(y, a.t[1].out[0], m, O);
+        }
         if (group == 0) ip012_sums<0>(s, x, y);
         else ip012_sums<1>(s, x, y);
     }

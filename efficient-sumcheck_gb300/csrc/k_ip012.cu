@@ -12,6 +12,11 @@ __global__ void __launch_bounds__(TPB, 2) k_ip_r012(RoundArgs a) {
     ip012_body<LSB>(a, blockIdx.x, gridDim.x);
 }
 template <bool LSB>
+__global__ void __launch_bounds__(TPB, 2) k_ip_r012m(RoundArgs a) {
+    chain_enter();
+    ip012_body<LSB, true>(a, blockIdx.x, gridDim.x);
+}
+template <bool LSB>
 __global__ void __launch_bounds__(TPB, 2) k_ip_r3x(RoundArgs a) {
     chain_enter();
     ip3x_body<LSB>(a, blockIdx.x, gridDim.x);
@@ -48,6 +53,9 @@ bool launch_ip012_staged(bool lsb, const RoundArgs& a, u32 ntiles, int grid, cud
 }
 u32 ip012_tile_octets(void) { return IP012_TQ; }
 
+bool launch_ip012_mirror(bool lsb, const RoundArgs& a, int grid, cudaStream_t s) {
+    return lsb ? launch_chain(k_ip_r012m<true>, grid, TPB, 0, s, a) : launch_chain(k_ip_r012m<false>, grid, TPB, 0, s, a);
+}
 bool launch_ip012(bool lsb, const RoundArgs& a, int grid, cudaStream_t s) {
     return lsb ? launch_chain(k_ip_r012<true>, grid, TPB, 0, s, a) : launch_chain(k_ip_r012<false>, grid, TPB, 0, s, a);
 }

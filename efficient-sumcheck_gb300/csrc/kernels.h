@@ -233,6 +233,10 @@ bool launch_ip2x(bool lsb, const RoundArgs& a, int grid, cudaStream_t s);
 // r1, r2 at once and round 3 from a second read (launch_ip3x; a.chal_ptr
 // holds r0, r1, r2 as 9 consecutive words).
 bool launch_ip012(bool lsb, const RoundArgs& a, int grid, cudaStream_t s);
+// The first pass over tables in host memory that also copies them to the
+// device buffers a.t[0].out[0], a.t[1].out[0] (L words each, 16-byte aligned)
+// for the second pass.
+bool launch_ip012_mirror(bool lsb, const RoundArgs& a, int grid, cudaStream_t s);
 bool launch_ip3x(bool lsb, const RoundArgs& a, int grid, cudaStream_t s);
 // The first pass with the tables streamed through shared memory by bulk
 // copies: ntiles = (L/8) / ip012_tile_octets() tiles; device-memory tables,
@@ -240,6 +244,23 @@ bool launch_ip3x(bool lsb, const RoundArgs& a, int grid, cudaStream_t s);
 // pass keeps direct loads: staged, it measured slower.)
 bool launch_ip012_staged(bool lsb, const RoundArgs& a, u32 ntiles, int grid, cudaStream_t s);
 u32 ip012_tile_octets(void);
+// Consecutive InnerProduct rounds over Fp3 tables in one cooperative launch
+// (k_persist.cu): round k of the launch folds tables of length L0 >> k with
+// the previous challenge and evaluates; the last block to reach the grid
+// barrier runs the transcript step.  a.tx carries the transcript and hook,
+// a.partials (grid * RAW_WORDS words) and a.status as for the other round
+// kernels.
+struct PersistArgs {
+    u32 nrounds;          // rounds run by this launch
+    u64 L0;               // table length before the first round's fold
+    const u64* chal_in;   // the challenge before the first round (3 words)
+    u64* proof_wire;      // the first round's wire row (6 words per round)
+    u64* proof_chal;      // the first round's challenge (3 words per round)
+    u32* bar;             // barrier: [0] arrivals (zero between launches), [1] generation
+    u64* buf[2][2][3];    // [ping-pong][table][component]: MSB folds [0] in place
+};
+bool launch_ip_persist(bool lsb, const RoundArgs& a, const PersistArgs& p, int grid, cudaStream_t s);
+int persist_max_grid(bool lsb);
 bool launch_ml01(const RoundArgs& a, int grid, cudaStream_t s);
 bool launch_ml2x(bool ech, const RoundArgs& a, int grid, cudaStream_t s);
 bool launch_gkr01(const RoundArgs& a, int grid, cudaStream_t s);

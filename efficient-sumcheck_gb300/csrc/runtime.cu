@@ -274,6 +274,12 @@ struct effsc_prover {
     size_t len0[4] = {0, 0, 0, 0};
     bool ext0[4] = {false, false, false, false};
     u64* partials = nullptr;
+    // effsc_prove: InnerProduct Fp3 rounds whose tables hold at most this
+    // many entries run in one cooperative launch (0: never); its grid barrier
+    u64 persist_len = 0;
+    u32* d_bar = nullptr;
+    // host tables: copy to the device during the first pass (-1 undecided)
+    int mirror = -1;
     u32* counter = nullptr;
     u32* status = nullptr;
     u64* h_res = nullptr;                      // mapped pinned: wire (9 words) + aux (6 words)
@@ -629,6 +635,77 @@ bool cluster_tail_ok(const effsc_prover* P, size_t r, size_t num_rounds, const C
     return true;
 }
 
+// Rounds r .. r + *nr - 1 of effsc_prove in one cooperative launch
+// (k_persist.cu): an InnerProduct prover over Fp3 with equal power-of-two
+// device tables of at most persist_len entries, already folded once (so in
+// buffers of the prover's own), and a challenge in device memory; the rounds run while the tables are larger than the one-block
+// tail takes (at least two rounds, else the per-round kernels stay).
+bool persist_ok(const effsc_prover* P, size_t r, size_t num_rounds, const Chal& ch, size_t* nr) {
+    if (P->kind != EFFSC_IP || P->field != EFFSC_FP3 || !P->persist_len || !ch.has || !ch.dev) return false;
+    const size_t L = P->t[0].len;
+    if (P->t[1].len != L || !is_pow2(L) || L < 4 || L > P->persist_len) return false;
+    // folds write the current buffers (MSB in place, LSB ping-pong), so
+    // never the caller's input tables (bufs[0]); 16-byte loads and stores
+    for (int i = 0; i < 2; i++) {
+        const Table& T = P->t[i];
+        if (!T.ext || T.cur == 0 || T.bufs[T.cur].host) return false;
+        for (int c = 0; c < 3; c++)
+            if ((uintptr_t)T.bufs[T.cur].p[c] & 15) return false;
+    }
+    const size_t lim = P->tail_len ? std::min<size_t>(P->tail_len, (size_t)tail_max_len(POL_IP, 3, TAIL_SMEM_CAP)) : 0;
+    size_t n = 0, l = L;
+    while (r + n < num_rounds && l > lim && l >= 4) { n++; l >>= 1; }
+    *nr = n;
+    return n >= 2 && persist_max_grid(P->order == EFFSC_LSB) > 0;
+}
+
+int do_persist(effsc_prover* P, size_t r, size_t nr, const Chal& ch, size_t hook_len, bool dry) {
+    const bool lsb = P->order == EFFSC_LSB;
+    const size_t L = P->t[0].len;
+    cudaStream_t s = P->ctx->stream;
+    if (!P->d_bar) {
+        CK(cudaMallocAsync((void**)&P->d_bar, 2 * sizeof(u32), s));
+        CK(cudaMemsetAsync(P->d_bar, 0, 2 * sizeof(u32), s));
+    }
+    PersistArgs p;
+    memset(&p, 0, sizeof p);
+    int other[2] = {0, 0};
+    for (int i = 0; i < 2; i++) {
+        Table& T = P->t[i];
+        // LSB ping-pongs between the current buffer and another of L / 2
+        if (lsb) TRY(out_buffer(P, T, true, L / 2, false, &other[i]));
+        for (int c = 0; c < 3; c++) {
+            p.buf[0][i][c] = T.bufs[T.cur].p[c];
+            p.buf[1][i][c] = lsb ? T.bufs[other[i]].p[c] : nullptr;
+        }
+    }
+    uint64_t bytes = 0;
+    for (size_t k = 0; k < nr; k++) bytes += 2 * ((L >> k) * 24 + (L >> (k + 1)) * 24);
+    if (!dry) {
+        RoundArgs a = base_args(P);
+        a.tx.tx = P->d_tx;
+        a.tx.hook = P->d_hook;
+        a.tx.hook_len = (u32)hook_len;
+        p.nrounds = (u32)nr;
+        p.L0 = L;
+        p.chal_in = ch.dev;
+        p.proof_wire = P->d_wire + r * 6;
+        p.proof_chal = P->d_chals + 3 * r;
+        p.bar = P->d_bar;
+        const u64 want = (L / 4 + KERNEL_TPB - 1) / KERNEL_TPB;
+        const int cap = std::min(persist_max_grid(lsb), max_grid());
+        const int g = (int)std::max<u64>(1, std::min<u64>(want, (u64)cap));
+        TRY(timed_launch(s, "ip_rounds_persistent", bytes, [&] { return launch_ip_persist(lsb, a, p, g, s); }));
+    }
+    for (int i = 0; i < 2; i++) {
+        Table& T = P->t[i];
+        if (lsb && (nr & 1)) T.cur = other[i];
+        T.len = L >> nr;
+    }
+    P->rounds += nr;
+    return EFFSC_OK;
+}
+
 // fin: the tail also runs the runner's finalize (the last challenge's fold)
 // and writes the tables' first entries to `first` (the proof read-back).
 int do_tail(effsc_prover* P, size_t r, size_t num_rounds, const Chal& ch, const TxIO& tx, bool dry, u32 cs_log = 0,
@@ -704,6 +781,23 @@ bool fuse3_ok(const effsc_prover* P, size_t num_rounds) {
     return P->t[0].len >= FUSE3_MIN_LEN;
 }
 
+// The mirror of host tables for the two-pass start: both tables in host
+// memory, unfolded, and 16 L bytes free on the device beside the Fp3 tables
+// the second pass writes (decided once per prover, when no mirror exists).
+bool mirror_ok(effsc_prover* P, size_t L) {
+    for (int i = 0; i < 2; i++) {
+        const Table& T = P->t[i];
+        if (T.cur != 0 || !T.bufs[0].host || T.ext) return false;
+    }
+    if (P->mirror < 0) {
+        size_t fr = 0, tot = 0;
+        const size_t need = 2 * L * sizeof(u64) + 2 * (L / 8) * 24 + ((size_t)1 << 28);
+        P->mirror = cudaMemGetInfo(&fr, &tot) == cudaSuccess && fr >= need ? 1 : 0;
+        cudaGetLastError();
+    }
+    return P->mirror == 1;
+}
+
 int do_fuse3(effsc_prover* P, const TxIO& tx0, const TxIO& tx3, const u64* chals, bool dry) {
     const size_t L = P->t[0].len;
     const bool lsb = P->order == EFFSC_LSB;
@@ -728,9 +822,21 @@ int do_fuse3(effsc_prover* P, const TxIO& tx0, const TxIO& tx3, const u64* chals
     staged &= nt1 >= 1;
     const int two_per_sm = (max_grid() / 8) * 2;
     const int g1 = staged ? std::min<int>((int)nt1, two_per_sm) : std::min<int>(grid_for(L / 8, 2), two_per_sm);
-    if (!dry) TRY(timed_launch(P->ctx->stream, "ip_rounds_0_2", 16 * (uint64_t)L, [&] {
+    // Tables in host memory: when the device has room, the first pass also
+    // copies them into device buffers (the mirror), so they cross the host
+    // link once and the second pass reads HBM.
+    int mi[2] = {-1, -1};
+    if (mirror_ok(P, L))
+        for (int i = 0; i < 2; i++) {
+            TRY(out_buffer(P, P->t[i], false, L, false, &mi[i]));
+            a.t[i].out[0] = P->t[i].bufs[mi[i]].p[0];
+        }
+    if (!dry) TRY(timed_launch(P->ctx->stream, mi[0] >= 0 ? "ip_rounds_0_2_from_host" : "ip_rounds_0_2", 16 * (uint64_t)L, [&] {
+        if (mi[0] >= 0) return launch_ip012_mirror(lsb, a, g1, P->ctx->stream);
         return staged ? launch_ip012_staged(lsb, a, nt1, g1, P->ctx->stream) : launch_ip012(lsb, a, g1, P->ctx->stream);
     }));
+    if (mi[0] >= 0)
+        for (int i = 0; i < 2; i++) P->t[i].cur = mi[i];
     int bi[2];
     for (int i = 0; i < 2; i++) TRY(out_buffer(P, P->t[i], true, L / 8, true, &bi[i]));
     RoundArgs b = base_args(P);
@@ -1138,7 +1244,8 @@ int check_status(effsc_prover* P) {
     if (!v) return EFFSC_OK;
     *st = 0;
     cudaMemsetAsync(P->counter, 0, sizeof(u32), P->ctx->stream);
-    return fail(EFFSC_TIMEOUT, "a round kernel timed out waiting for its staged loads (status %u)", v);
+    if (P->d_bar) cudaMemsetAsync(P->d_bar, 0, sizeof(u32), P->ctx->stream);
+    return fail(EFFSC_TIMEOUT, "a round kernel timed out waiting for its staged loads or grid barrier (status %u)", v);
 }
 
 // One round of GkrProver (src/provers/gkr.rs:105-190) on the compact witness
@@ -1454,6 +1561,7 @@ void release_prover(effsc_prover* P) {
         cudaStream_t s = P->ctx->stream;
         if (P->partials) cudaFreeAsync(P->partials, s);
         if (P->counter) cudaFreeAsync(P->counter, s);
+        if (P->d_bar) cudaFreeAsync(P->d_bar, s);
         if (P->d_tx) cudaFreeAsync(P->d_tx, s);
         if (P->d_hook) cudaFreeAsync(P->d_hook, s);
         if (P->d_wire) cudaFreeAsync(P->d_wire, s);
@@ -2022,6 +2130,13 @@ int effsc_prover_set_first_rounds(effsc_prover* P, int fused) {
     return EFFSC_OK;
 }
 
+int effsc_prover_set_persistent(effsc_prover* P, size_t max_len) {
+    if (!P) return fail(EFFSC_INVALID_ARG, "prover is NULL");
+    if (max_len != P->persist_len && P->gexec) { cudaGraphExecDestroy(P->gexec); P->gexec = nullptr; }
+    P->persist_len = max_len;
+    return EFFSC_OK;
+}
+
 int effsc_prover_set_tail(effsc_prover* P, size_t max_len) {
     if (!P) return fail(EFFSC_INVALID_ARG, "prover is NULL");
     if (max_len != P->tail_len && P->gexec) { cudaGraphExecDestroy(P->gexec); P->gexec = nullptr; }
@@ -2168,6 +2283,12 @@ int effsc_prove(effsc_prover* P, size_t num_rounds, effsc_transcript* T, const u
                 TRY(do_gkr_tail(P, r, num_rounds, ch, tx, dry, P->d_first));
                 tail_done = true;
                 break;
+            }
+            size_t nr = 0;
+            if (persist_ok(P, r, num_rounds, ch, &nr)) {
+                TRY(do_persist(P, r, nr, ch, hook_len, dry));
+                r += nr - 1;
+                continue;
             }
             u32 cs_log = 0;
             if (cluster_tail_ok(P, r, num_rounds, ch, &cs_log)) {

@@ -663,11 +663,15 @@ int effsc_server_take(effsc_server* s, uint64_t* id, uint32_t* num_vars, uint64_
     return EFFSC_OK;
 }
 
-int effsc_server_run_trace(effsc_server* s, size_t n, const int* kinds, int field, const uint32_t* num_vars,
-                           const uint64_t* seeds, const effsc_transcript* const* transcripts, const double* arrival_s,
-                           double* latency_s, double* makespan_s, uint64_t* round_polys, uint64_t* challenges,
-                           uint64_t* final_values) {
-    if (!s || !kinds || !num_vars || !seeds || !transcripts || !arrival_s || !latency_s)
+}  // extern "C"
+
+// The open-loop driver behind both trace entry points: request i's tables
+// come from seeds[2i..2i+1] or, with seeds NULL, from host_tables[2i..2i+1].
+static int run_trace_impl(effsc_server* s, size_t n, const int* kinds, int field, const uint32_t* num_vars,
+                          const uint64_t* seeds, const uint64_t* const* host_tables,
+                          const effsc_transcript* const* transcripts, const double* arrival_s, double* latency_s,
+                          double* makespan_s, uint64_t* round_polys, uint64_t* challenges, uint64_t* final_values) {
+    if (!s || !kinds || !num_vars || (!seeds && !host_tables) || !transcripts || !arrival_s || !latency_s)
         return effsc_set_error(EFFSC_INVALID_ARG, "NULL argument");
     if (n_queued(s) || s->n_active || !s->finishing.empty() || !s->done.empty())
         return effsc_set_error(EFFSC_INVALID_ARG, "run_trace needs an idle server");
@@ -687,8 +691,8 @@ int effsc_server_run_trace(effsc_server* s, size_t n, const int* kinds, int fiel
         while (next < n && arrival_s[order[next]] <= t) {
             const size_t i = order[next];
             uint64_t id;
-            int rc = submit_one(s, kinds[i], field, num_vars[i], nullptr, seeds + 2 * i, transcripts[i],
-                                t0 + arrival_s[i], &id);
+            int rc = submit_one(s, kinds[i], field, num_vars[i], seeds ? nullptr : host_tables + 2 * i,
+                                seeds ? seeds + 2 * i : nullptr, transcripts[i], t0 + arrival_s[i], &id);
             if (rc != EFFSC_OK) return rc;
             if (of_id.size() <= id - id0) of_id.resize(id - id0 + 1);
             of_id[id - id0] = i;
@@ -719,6 +723,26 @@ int effsc_server_run_trace(effsc_server* s, size_t n, const int* kinds, int fiel
     }
     if (makespan_s) *makespan_s = now_s() - t0;
     return EFFSC_OK;
+}
+
+extern "C" {
+
+int effsc_server_run_trace(effsc_server* s, size_t n, const int* kinds, int field, const uint32_t* num_vars,
+                           const uint64_t* seeds, const effsc_transcript* const* transcripts, const double* arrival_s,
+                           double* latency_s, double* makespan_s, uint64_t* round_polys, uint64_t* challenges,
+                           uint64_t* final_values) {
+    if (!seeds) return effsc_set_error(EFFSC_INVALID_ARG, "NULL argument");
+    return run_trace_impl(s, n, kinds, field, num_vars, seeds, nullptr, transcripts, arrival_s, latency_s,
+                          makespan_s, round_polys, challenges, final_values);
+}
+
+int effsc_server_run_trace_host(effsc_server* s, size_t n, const int* kinds, int field, const uint32_t* num_vars,
+                                const uint64_t* const* host_tables, const effsc_transcript* const* transcripts,
+                                const double* arrival_s, double* latency_s, double* makespan_s, uint64_t* round_polys,
+                                uint64_t* challenges, uint64_t* final_values) {
+    if (!host_tables) return effsc_set_error(EFFSC_INVALID_ARG, "NULL argument");
+    return run_trace_impl(s, n, kinds, field, num_vars, nullptr, host_tables, transcripts, arrival_s, latency_s,
+                          makespan_s, round_polys, challenges, final_values);
 }
 
 }  // extern "C"

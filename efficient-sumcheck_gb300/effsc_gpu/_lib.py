@@ -77,6 +77,7 @@ SIGNATURES = {
     "effsc_diag_bounded_wait": (ci, [vp, ctypes.c_uint64, ci, ctypes.POINTER(ctypes.c_uint32)]),
     "effsc_prover_set_tail": (ci, [vp, sz]),
     "effsc_prover_set_first_rounds": (ci, [vp, ci]),
+    "effsc_prover_set_persistent": (ci, [vp, sz]),
     "effsc_batch_create": (ci, [vp, ci, ci, sz, ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(u64p), u64p,
                                 ctypes.POINTER(vp)]),
     "effsc_batch_destroy": (ci, [vp]),
@@ -95,6 +96,10 @@ SIGNATURES = {
                                     ctypes.POINTER(vp), ctypes.POINTER(ctypes.c_double),
                                     ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double), u64p, u64p,
                                     u64p]),
+    "effsc_server_run_trace_host": (ci, [vp, sz, ctypes.POINTER(ci), ci, ctypes.POINTER(ctypes.c_uint32),
+                                         ctypes.POINTER(u64p), ctypes.POINTER(vp), ctypes.POINTER(ctypes.c_double),
+                                         ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double), u64p, u64p,
+                                         u64p]),
     "effsc_ip_round_noalloc": (ci, [vp, vp, vp, vp, sz, u64p, vp, ci, vp]),
     "effsc_device_alloc": (ci, [vp, sz, ctypes.POINTER(vp)]),
     "effsc_device_free": (ci, [vp, vp]),

@@ -290,6 +290,11 @@ class _Prover:
         tail kernel (None: as large as shared memory allows, 0: never)."""
         check(load().effsc_prover_set_tail(self.h, (1 << 64) - 1 if max_len is None else int(max_len)))
 
+    def set_persistent(self, max_len):
+        """prove(): InnerProduct rounds over Fp3 whose tables hold at most
+        max_len entries run in one cooperative launch (0: never)."""
+        check(load().effsc_prover_set_persistent(self.h, int(max_len)))
+
     def prove(self, num_rounds, transcript, hook=b"", use_graph=True):
         """Whole protocol on the device (effsc_prove) with the device transcript."""
         d = self.degree()
@@ -903,15 +908,28 @@ class Server:
             if pending == 0 and not self._meta:
                 return out
 
-    def run_trace(self, kinds, num_vars, seeds, transcripts, arrival_s, field=FP3, proofs=True):
+    def run_trace(self, kinds, num_vars, seeds, transcripts, arrival_s, field=FP3, proofs=True, host_tables=None):
         """Open-loop trace: request i arrives arrival_s[i] seconds after the
-        start.  Returns (latency_s array, makespan_s, proofs or None) with the
-        proofs concatenated as in Batch.prove_raw."""
+        start.  Tables from seeds[i] (generated on the device) or, with
+        host_tables given, from host_tables[i] (one or two arrays of 2^n
+        canonical words in host memory, uploaded on admission).  Returns
+        (latency_s array, makespan_s, proofs or None) with the proofs
+        concatenated as in Batch.prove_raw."""
         n = len(kinds)
         k = (ctypes.c_int * n)(*[int(x) for x in kinds])
         nv = (ctypes.c_uint32 * n)(*[int(x) for x in num_vars])
-        sd = np.ascontiguousarray(np.asarray(seeds, dtype=np.uint64).reshape(-1))
         tx = (vp * n)(*[t.h for t in transcripts])
+        if host_tables is not None:
+            keep = []
+            ptrs = (u64p * (2 * n))()
+            for i, tabs in enumerate(host_tables):
+                for j, t in enumerate(tabs):
+                    if isinstance(t, np.ndarray):
+                        a = np.ascontiguousarray(t, dtype=np.uint64)
+                        keep.append(a)
+                        ptrs[2 * i + j] = _p(a)
+                    else:   # a host address (e.g. a pinned torch tensor's data_ptr())
+                        ptrs[2 * i + j] = ctypes.cast(ctypes.c_void_p(int(t)), u64p)
         arr = np.ascontiguousarray(np.asarray(arrival_s, dtype=np.float64))
         lat = np.zeros(n, dtype=np.float64)
         mk = ctypes.c_double()
@@ -922,10 +940,14 @@ class Server:
             rp = np.zeros(rows * 2 * field, dtype=np.uint64)
             ch = np.zeros(rows * field, dtype=np.uint64)
             fv = np.zeros(n * field, dtype=np.uint64)
-        check(load().effsc_server_run_trace(self.h, n, k, field, nv, _p(sd), tx, arr.ctypes.data_as(dpc),
-                                            lat.ctypes.data_as(dpc), ctypes.byref(mk),
-                                            _p(rp) if proofs else None, _p(ch) if proofs else None,
-                                            _p(fv) if proofs else None))
+        outs = (_p(rp) if proofs else None, _p(ch) if proofs else None, _p(fv) if proofs else None)
+        if host_tables is not None:
+            check(load().effsc_server_run_trace_host(self.h, n, k, field, nv, ptrs, tx, arr.ctypes.data_as(dpc),
+                                                     lat.ctypes.data_as(dpc), ctypes.byref(mk), *outs))
+        else:
+            sd = np.ascontiguousarray(np.asarray(seeds, dtype=np.uint64).reshape(-1))
+            check(load().effsc_server_run_trace(self.h, n, k, field, nv, _p(sd), tx, arr.ctypes.data_as(dpc),
+                                                lat.ctypes.data_as(dpc), ctypes.byref(mk), *outs))
         out = None
         if proofs:
             out = []

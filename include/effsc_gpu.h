@@ -215,6 +215,13 @@ int effsc_prover_set_tail(effsc_prover* p, size_t max_len);
  * interpolation sums of one pass; round 3 folds with three challenges).
  * 0 runs one pass per round.  Proofs are identical. */
 int effsc_prover_set_first_rounds(effsc_prover* p, int fused);
+/* effsc_prove only (no reference counterpart; a tuning knob): for an
+ * InnerProduct prover over Fp3 challenges, consecutive rounds whose tables
+ * hold at most max_len entries (after the first fold, down to the tail) run
+ * in one cooperative launch with a grid barrier between rounds, the last
+ * block to arrive running the transcript step.  Default 0 (off); 2^21 covers
+ * the rounds after the two-pass start of a 2^26 proof.  Proofs are identical. */
+int effsc_prover_set_persistent(effsc_prover* p, size_t max_len);
 
 /* Restore the state right after construction (the input tables are never
  * written by the rounds), so a proof can be recomputed without re-upload. */
@@ -440,6 +447,15 @@ int effsc_server_run_trace(effsc_server* s, size_t n, const int* kinds, int fiel
                            const uint64_t* seeds, const effsc_transcript* const* transcripts, const double* arrival_s,
                            double* latency_s, double* makespan_s, uint64_t* round_polys, uint64_t* challenges,
                            uint64_t* final_values);
+/* The same driver with every request's tables in host memory (the serving
+ * case where inputs arrive over the host link): request i's tables are
+ * host_tables[2i] and, for an InnerProduct request, host_tables[2i + 1]
+ * (2^num_vars[i] canonical words each; pinned memory uploads fastest), and
+ * the upload joins the request's latency. */
+int effsc_server_run_trace_host(effsc_server* s, size_t n, const int* kinds, int field, const uint32_t* num_vars,
+                                const uint64_t* const* host_tables, const effsc_transcript* const* transcripts,
+                                const double* arrival_s, double* latency_s, double* makespan_s, uint64_t* round_polys,
+                                uint64_t* challenges, uint64_t* final_values);
 
 /* ---- one round without allocation -----------------------------------------
  * No counterpart in the reference.  For callers that must not allocate device

@@ -254,8 +254,14 @@ def test_kernels_launch(E):
     a = rand_table(rng, 1 << 12, False)
     p = E.InnerProductProver(a, a)
     p.set_tail(0)        # one kernel per round
+    p.set_persistent(0)
     p.prove(12, E.Transcript.keccak(3, b"k"), use_graph=False)
     assert E.launch_count() >= 12
+    E.launch_count_reset()
+    p.reset()
+    p.set_persistent(1 << 21)   # rounds 3..11 in one cooperative launch
+    p.prove(12, E.Transcript.keccak(3, b"k"), use_graph=False)
+    assert 2 <= E.launch_count() <= 8
     E.launch_count_reset()
     p.reset()
     p.set_tail(None)     # all 12 rounds in the one-block tail kernel, the final folds, the read-back gather

@@ -135,6 +135,23 @@ def test_trace_poisson(E):
         assert same(proofs[i], solo(E, kind, n, seeds, 3, i)), i
 
 
+def test_trace_host_tables(E):
+    """The same trace with every request's tables in host memory (uploaded on
+    admission): the proofs equal the solo proofs."""
+    reqs = workload(33, 40, 4, 14)
+    rng = np.random.default_rng(1)
+    arrivals = np.cumsum(rng.exponential(2e-4, size=len(reqs)))
+    host = [[np.asarray(E.gen_uniform(s[t], 1 << n)) for t in range(2 if k == "ip" else 1)] for k, n, s in reqs]
+    srv = E.Server(hbm_budget=1 << 33, max_active=12)
+    kinds = [E.IP if k == "ip" else E.ML for k, _, _ in reqs]
+    lat, makespan, proofs = srv.run_trace(kinds, [n for _, n, _ in reqs], None,
+                                          [E.Transcript.keccak(3, label(i)) for i in range(len(reqs))], arrivals,
+                                          host_tables=host)
+    assert (lat > 0).all() and makespan >= arrivals[-1]
+    for i, (kind, n, seeds) in enumerate(reqs):
+        assert same(proofs[i], solo(E, kind, n, seeds, 3, i)), i
+
+
 def test_two_lanes_mix(E):
     """Requests of 2^22 entries and more go to the second lane (own stream,
     queue and steps); a mix of both lanes, with small requests finishing in

@@ -59,25 +59,52 @@ def test_claims_match_bigint(E, ntab, ext):
         assert tuple(int(x) for x in E.multivariate_claim(E.MemoryStream(tabs[0]), field=3)) == want
 
 
-@pytest.mark.parametrize("n", [8, 12, 17])
+@pytest.mark.parametrize("n", [8, 12, 14, 15, 17])
 @pytest.mark.parametrize("tail", [None, 0])
-def test_ip_over_host_tables(E, n, tail):
+@pytest.mark.parametrize("order", ["msb", "lsb"])
+def test_ip_over_host_tables(E, n, tail, order):
+    """From 2^14 entries the two-pass start's first pass reads the host
+    tables once and copies them to the device for the second."""
     g = np.random.default_rng(n)
     a = g.integers(0, O.P, size=1 << n, dtype=np.uint64)
     b = g.integers(0, O.P, size=1 << n, dtype=np.uint64)
-    p = E.InnerProductProver.from_host([a, b], field=3)
+    a0, b0 = a.copy(), b.copy()
+    cls = E.InnerProductProver if order == "msb" else E.InnerProductProverLSB
+    p = cls.from_host([a, b], field=3)
     p.set_tail(tail)
-    rp, ch, fv = O.sumcheck(O.Prover(O.IP, O.MSB, 3, [a, b]), n, O.Transcript(3, label=b"host"))
-    for use_graph in (True, False):
+    rp, ch, fv = O.sumcheck(O.Prover(O.IP, O.MSB if order == "msb" else O.LSB, 3, [a, b]), n,
+                            O.Transcript(3, label=b"host"))
+    for use_graph in (True, True, False):
         p.reset()
         proof = p.prove(n, E.Transcript.keccak(3, b"host"), use_graph=use_graph)
         assert np.array_equal(proof.round_polys, rp)
         assert np.array_equal(proof.final_value, fv)
+    assert np.array_equal(a, a0) and np.array_equal(b, b0)
     # the per-round API over the same host tables
-    q = E.InnerProductProver.from_host([a, b], field=3)
+    q = cls.from_host([a, b], field=3)
     proof = E.sumcheck(q, n, E.Transcript.keccak(3, b"host"))
     assert np.array_equal(proof.round_polys, rp)
     assert np.array_equal(proof.final_value, fv)
+
+
+@pytest.mark.parametrize("rounds", [4, 5, 9])
+@pytest.mark.parametrize("order", ["msb", "lsb"])
+def test_ip_host_tables_partial_post_state(E, rounds, order):
+    """Partial runs over host tables leave the tables a device-table prover
+    leaves."""
+    n = 15
+    g = np.random.default_rng(rounds)
+    a = g.integers(0, O.P, size=1 << n, dtype=np.uint64)
+    b = g.integers(0, O.P, size=1 << n, dtype=np.uint64)
+    cls = E.InnerProductProver if order == "msb" else E.InnerProductProverLSB
+    p = cls.from_host([a, b], field=3)
+    q = cls(a, b, field=3)
+    x = p.prove(rounds, E.Transcript.keccak(3, b"hp"))
+    y = q.prove(rounds, E.Transcript.keccak(3, b"hp"))
+    assert np.array_equal(x.round_polys, y.round_polys)
+    assert np.array_equal(x.final_value, y.final_value)
+    for t in range(2):
+        assert np.array_equal(p.table(t), q.table(t))
 
 
 def test_ip_fp_field_over_host_tables_uses_plain_loads(E):
