@@ -13,6 +13,8 @@
 #pragma once
 #include <cstdint>
 
+#include "gl_w.h"
+
 typedef unsigned long long u64;
 typedef unsigned int u32;
 
@@ -241,7 +243,7 @@ template <bool E>
 __device__ __forceinline__ Mul3 mul3_prepare(const F3& m) {
     Mul3 r;
     r.m0 = m.c0;
-    if (E) { r.m1 = m.c1; r.m2 = m.c2; r.w1 = gl_mul(GL_W, m.c1); r.w2 = gl_mul(GL_W, m.c2); }
+    if (E) { r.m1 = m.c1; r.m2 = m.c2; r.w1 = gl_mul_w(m.c1); r.w2 = gl_mul_w(m.c2); }
     else { r.m1 = r.m2 = r.w1 = r.w2 = 0; }
     return r;
 }
@@ -310,8 +312,8 @@ struct ProdAcc {
             r.c1 = s1.reduce();
             r.c2 = s2.reduce();
             if (EA && EB) {
-                r.c0 = gl_add(r.c0, gl_mul(GL_W, s0w.reduce()));
-                r.c1 = gl_add(r.c1, gl_mul(GL_W, s1w.reduce()));
+                r.c0 = gl_add(r.c0, gl_mul_w(s0w.reduce()));
+                r.c1 = gl_add(r.c1, gl_mul_w(s1w.reduce()));
             }
         } else {
             r.c1 = r.c2 = 0;
@@ -319,6 +321,29 @@ struct ProdAcc {
         return r;
     }
 };
+// Lazy sum of products (ab) c with both Fp3: c prepared with W per product
+// (two multiplications by W, no general product) so that three accumulators
+// hold the sum instead of five; the same value as ProdAcc<true, true>.
+template <bool EA, bool EB>
+struct PointAcc {
+    ProdAcc<EA, EB> p;
+    __device__ __forceinline__ void init() { p.init(); }
+    __device__ __forceinline__ void mac(const F3& a, const F3& b) { p.mac(a, b); }
+    __device__ __forceinline__ F3 result() const { return p.result(); }
+};
+template <>
+struct PointAcc<true, true> {
+    AccF<0> s0, s1, s2;
+    __device__ __forceinline__ void init() { s0.zero(); s1.zero(); s2.zero(); }
+    __device__ __forceinline__ void mac(const F3& a, const F3& b) {
+        const Mul3 m = mul3_prepare<true>(b);
+        s0.mac(a.c0, m.m0); s0.mac(a.c1, m.w2); s0.mac(a.c2, m.w1);
+        s1.mac(a.c0, m.m1); s1.mac(a.c1, m.m0); s1.mac(a.c2, m.w2);
+        s2.mac(a.c0, m.m2); s2.mac(a.c1, m.m1); s2.mac(a.c2, m.m0);
+    }
+    __device__ __forceinline__ F3 result() const { return f3_make(s0.reduce(), s1.reduce(), s2.reduce()); }
+};
+
 // Lazy sum of field elements.
 template <bool E>
 struct SumAcc {

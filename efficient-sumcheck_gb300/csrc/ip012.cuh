@@ -160,9 +160,20 @@ __device__ __forceinline__ void ip012_reduce_and_finalize(const Acc (&s)[IP012_G
         __threadfence();
         // thread t sums word t % 32 over the blocks t / 32, t / 32 + 8, ...
         const int wd = threadIdx.x & 31, part = threadIdx.x >> 5;
+        // four independent sums so that four loads are in flight at once
         u64 v = 0;
-        if (wd < IP012_WORDS)
-            for (u32 b = part; b < nb; b += NWARP) v = gl_add(v, __ldcg(&a.partials[(u64)b * 32 + wd]));
+        if (wd < IP012_WORDS) {
+            u64 v1 = 0, v2 = 0, v3 = 0;
+            u32 b = part;
+            for (; b + 3 * NWARP < nb; b += 4 * NWARP) {
+                v = gl_add(v, __ldcg(&a.partials[(u64)b * 32 + wd]));
+                v1 = gl_add(v1, __ldcg(&a.partials[(u64)(b + NWARP) * 32 + wd]));
+                v2 = gl_add(v2, __ldcg(&a.partials[(u64)(b + 2 * NWARP) * 32 + wd]));
+                v3 = gl_add(v3, __ldcg(&a.partials[(u64)(b + 3 * NWARP) * 32 + wd]));
+            }
+            for (; b < nb; b += NWARP) v = gl_add(v, __ldcg(&a.partials[(u64)b * 32 + wd]));
+            v = gl_add(gl_add(v, v1), gl_add(v2, v3));
+        }
         s_fin[part][wd] = v;
         __syncthreads();
         if (threadIdx.x < IP012_WORDS) {
@@ -216,22 +227,26 @@ __device__ __forceinline__ F3 quad_at(const F3& s0, const F3& s1, const F3& sinf
     const F3 c1 = f3_sub<true>(f3_sub<true>(s1, s0), sinf);
     return f3_add<true>(f3_mul<true, true>(f3_add<true>(f3_mul<true, true>(sinf, r), c1), r), s0);
 }
+// The same with base-field values: r sinf is three products, (.. + c1) r nine.
 __device__ __forceinline__ F3 quad_base(u64 s0, u64 s1, u64 sinf, const F3& r) {
-    return quad_at(f3_make(s0, 0, 0), f3_make(s1, 0, 0), f3_make(sinf, 0, 0), r);
-}
-// The biquadratic with values G[3u + v] on {0, 1, inf}^2 at (r0, r1).
-__device__ __forceinline__ F3 biquad_at(const u64* G, const F3& r0, const F3& r1) {
-    F3 g[3];
-#pragma unroll
-    for (int v = 0; v < 3; v++) g[v] = quad_base(G[v], G[3 + v], G[6 + v], r0);
-    return quad_at(g[0], g[1], g[2], r1);
+    const u64 c1 = gl_sub(gl_sub(s1, s0), sinf);
+    F3 t = f3_mul<true, false>(r, f3_make(sinf, 0, 0));
+    t.c0 = gl_add(t.c0, c1);
+    t = f3_mul<true, true>(t, r);
+    t.c0 = gl_add(t.c0, s0);
+    return t;
 }
 
 // Rounds 0, 1, 2 from the 26 sums: for each, the wire [q0, qinf], the hook,
 // the challenge (src/runner.rs:39-55).  Run by warp 0 of the last block.
+// The interpolations run on separate lanes as soon as their challenges are
+// known: after r0, lanes 0-1 evaluate round 1's two quadratics and lanes 2-7
+// the six quadratics in r0 that round 2's biquadratics reduce to; after r1,
+// lanes 0-1 finish round 2 with one quadratic in r1 each.
 static __device__ __noinline__ void finalize_ip012(const u64* S, const RoundArgs& a) {
     __shared__ u64 s_w[3][6];
     __shared__ u64 s_c[3][3];
+    __shared__ u64 s_g[2][3][3];   // round 2: [P0 / Pd][v][component], the quadratics in r0 at r0
     __shared__ __align__(8) uint8_t s_scr[64];
     const int lane = threadIdx.x & 31;
     if (lane == 0) {
@@ -244,19 +259,25 @@ static __device__ __noinline__ void finalize_ip012(const u64* S, const RoundArgs
     DevTranscript* T = (DevTranscript*)a.tx.tx;
     WarpTx w = tx_load(T, lane);
     for (int rd = 0; rd < 3; rd++) {
-        if (rd > 0 && lane == 0) {
+        if (rd == 1 && lane < 8) {
             const F3 r0 = f3_make(s_c[0][0], s_c[0][1], s_c[0][2]);
-            F3 q0, qi;
-            if (rd == 1) {
-                q0 = quad_base(gl_add(S[0], S[9]), gl_add(S[3], S[10]), gl_add(S[6], S[11]), r0);
-                qi = quad_base(gl_add(S[2], S[23]), gl_add(S[5], S[24]), gl_add(S[8], S[25]), r0);
+            if (lane < 2) {
+                const F3 q = lane == 0 ? quad_base(gl_add(S[0], S[9]), gl_add(S[3], S[10]), gl_add(S[6], S[11]), r0)
+                                       : quad_base(gl_add(S[2], S[23]), gl_add(S[5], S[24]), gl_add(S[8], S[25]), r0);
+                s_w[1][3 * lane] = q.c0; s_w[1][3 * lane + 1] = q.c1; s_w[1][3 * lane + 2] = q.c2;
             } else {
-                const F3 r1 = f3_make(s_c[1][0], s_c[1][1], s_c[1][2]);
-                q0 = biquad_at(S, r0, r1);
-                qi = biquad_at(S + 14, r0, r1);
+                const int j = lane - 2, h = j / 3, v = j % 3;
+                const u64* G = S + 14 * h;
+                const F3 g = quad_base(G[v], G[3 + v], G[6 + v], r0);
+                s_g[h][v][0] = g.c0; s_g[h][v][1] = g.c1; s_g[h][v][2] = g.c2;
             }
-            s_w[rd][0] = q0.c0; s_w[rd][1] = q0.c1; s_w[rd][2] = q0.c2;
-            s_w[rd][3] = qi.c0; s_w[rd][4] = qi.c1; s_w[rd][5] = qi.c2;
+        }
+        if (rd == 2 && lane < 2) {
+            const F3 r1 = f3_make(s_c[1][0], s_c[1][1], s_c[1][2]);
+            const F3 q = quad_at(f3_make(s_g[lane][0][0], s_g[lane][0][1], s_g[lane][0][2]),
+                                 f3_make(s_g[lane][1][0], s_g[lane][1][1], s_g[lane][1][2]),
+                                 f3_make(s_g[lane][2][0], s_g[lane][2][1], s_g[lane][2][2]), r1);
+            s_w[2][3 * lane] = q.c0; s_w[2][3 * lane + 1] = q.c1; s_w[2][3 * lane + 2] = q.c2;
         }
         __syncwarp();
         tx_send_elems(w, lane, s_w[rd], 2);

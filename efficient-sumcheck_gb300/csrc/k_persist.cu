@@ -11,14 +11,15 @@
 // (4q+2, 4q+3) into the other of two buffers) and accumulates the next round
 // polynomial (the same per-pair policy as the single-round kernels,
 // src/provers/inner_product.rs:61-113), writes its partial sums and arrives
-// at a grid barrier.  The last block to arrive sums the partials, builds the
-// wire, runs the transcript step (absorb, hook, squeeze; src/runner.rs:39-55)
-// and only then releases the barrier, so the next round starts with its
-// challenge in memory.  Data written by other blocks of the same launch is
+// at a grid barrier.  Block 0 waits for the others, sums the partials,
+// builds the wire, runs the transcript step (absorb, hook, squeeze;
+// src/runner.rs:39-55) and only then releases the barrier, so the next round
+// starts with its challenge in memory.  Data written by other blocks of the same launch is
 // read through L2 (ld.cg) and written through to it (st.cg).
 // The barrier's waits are bounded (1 s of the global timer): a block that
 // gives up records EFFSC_STATUS_TIMEOUT and returns, and so do the others
-// at their next wait.
+// at their next wait.  Every block is resident at once (a cooperative
+// launch), so block 0's wait for the others ends.
 #include "round_common.cuh"
 
 namespace effsc {
@@ -108,22 +109,47 @@ __device__ __forceinline__ bool persist_round(const RoundArgs& a, const PersistA
         for (int w = 0; w < NWARP; w++) v = gl_add(v, s_red[w][threadIdx.x]);
         a.partials[(u64)blockIdx.x * RAW_WORDS + threadIdx.x] = v;
     }
-    // arrive; the last block finalises the round and releases the rest
+    // arrive: block 0 waits for the others, finalises the round and releases
+    // them (always the same block, so that the transcript code stays in one
+    // SM's instruction cache across the rounds)
     __threadfence();
     __syncthreads();
-    u32 g0 = 0;
-    if (threadIdx.x == 0) {
-        g0 = ld_volatile_u32(p.bar + 1);
-        __threadfence();
-        s_flag = atomicAdd(p.bar, 1u) == nb - 1;
-    }
-    __syncthreads();
     bool ok = true;
-    if (s_flag) {
-        __threadfence();
+    if (blockIdx.x != 0) {
+        if (threadIdx.x == 0) {
+            const u32 g0 = ld_volatile_u32(p.bar + 1);
+            __threadfence();
+            atomicAdd(p.bar, 1u);
+            bool done = true;
+            if (ld_volatile_u32(p.bar + 1) == g0) {
+                const u64 t0 = global_ns();
+                while (ld_volatile_u32(p.bar + 1) == g0)
+                    if (global_ns() - t0 > 1000000000ULL) { done = false; break; }
+            }
+            s_flag = done ? 0 : -1;
+            if (!done && a.status) *(volatile u32*)a.status = EFFSC_STATUS_TIMEOUT;
+            __threadfence();
+        }
+        __syncthreads();
+        ok = s_flag >= 0;
+    } else {
+        if (threadIdx.x == 0) {
+            bool done = true;
+            if (ld_volatile_u32(p.bar) != nb - 1) {
+                const u64 t0 = global_ns();
+                while (ld_volatile_u32(p.bar) != nb - 1)
+                    if (global_ns() - t0 > 1000000000ULL) { done = false; break; }
+            }
+            s_flag = done ? 0 : -1;
+            if (!done && a.status) *(volatile u32*)a.status = EFFSC_STATUS_TIMEOUT;
+            __threadfence();
+        }
+        __syncthreads();
+        if (s_flag < 0) return false;
         // every thread walks a stride of the blocks' partials, then warp and
         // block sums
         u64 t6[6] = {0, 0, 0, 0, 0, 0};
+#pragma unroll 2
         for (u32 b = threadIdx.x; b < nb; b += TPB)
 #pragma unroll
             for (int i = 0; i < 6; i++) t6[i] = gl_add(t6[i], __ldcg(&a.partials[(u64)b * RAW_WORDS + i]));
@@ -159,20 +185,6 @@ __device__ __forceinline__ bool persist_round(const RoundArgs& a, const PersistA
             __threadfence();
             atomicAdd(p.bar + 1, 1u);
         }
-    } else {
-        if (threadIdx.x == 0) {
-            bool done = true;
-            if (ld_volatile_u32(p.bar + 1) == g0) {
-                const u64 t0 = global_ns();
-                while (ld_volatile_u32(p.bar + 1) == g0)
-                    if (global_ns() - t0 > 1000000000ULL) { done = false; break; }
-            }
-            s_flag = done ? 0 : -1;
-            if (!done && a.status) *(volatile u32*)a.status = EFFSC_STATUS_TIMEOUT;
-            __threadfence();
-        }
-        __syncthreads();
-        ok = s_flag >= 0;
     }
     __syncthreads();
     return ok;

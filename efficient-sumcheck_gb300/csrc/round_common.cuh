@@ -150,9 +150,9 @@ struct Policy<POL_C3, M> {
     static constexpr bool LSB_REMAINDER = false;
     static constexpr bool E0 = ext_of<M>(0), E1 = ext_of<M>(1), E2 = ext_of<M>(2);
     static constexpr bool EU = E0 || E1;
-    ProdAcc<EU, E2> h0, h1, h2, hi;
+    PointAcc<EU, E2> h0, h1, h2, hi;
     __device__ __forceinline__ void init() { h0.init(); h1.init(); h2.init(); hi.init(); }
-    __device__ __forceinline__ void point(ProdAcc<EU, E2>& acc, const F3& a, const F3& b, const F3& c) {
+    __device__ __forceinline__ void point(PointAcc<EU, E2>& acc, const F3& a, const F3& b, const F3& c) {
         acc.mac(f3_mul<E0, E1>(a, b), c);
     }
     __device__ __forceinline__ void pair(const F3* lo, const F3* hi_) {
@@ -177,9 +177,9 @@ struct Policy<POL_C3W, M> {
     static constexpr bool LSB_REMAINDER = false;
     static constexpr bool E0 = ext_of<M>(0), E1 = ext_of<M>(1), E2 = ext_of<M>(2);
     static constexpr bool EU = E0 || E1;
-    ProdAcc<EU, E2> h0, h2, hi;
+    PointAcc<EU, E2> h0, h2, hi;
     __device__ __forceinline__ void init() { h0.init(); h2.init(); hi.init(); }
-    __device__ __forceinline__ void point(ProdAcc<EU, E2>& acc, const F3& a, const F3& b, const F3& c) {
+    __device__ __forceinline__ void point(PointAcc<EU, E2>& acc, const F3& a, const F3& b, const F3& c) {
         acc.mac(f3_mul<E0, E1>(a, b), c);
     }
     __device__ __forceinline__ void pair(const F3* lo, const F3* hi_) {
@@ -439,9 +439,13 @@ __device__ __forceinline__ void reduce_and_finalize_seg(F3 (&v)[NRAW], const Rou
         if (!s_last) return;
         __threadfence();
         // every thread owns one of the 3*NRAW words and walks the partials
+        // (unrolled so that several blocks' loads are in flight at once)
         u64 acc[RAW_WORDS];
+#pragma unroll
         for (int i = 0; i < 3 * NRAW; i++) acc[i] = 0;
+#pragma unroll 4
         for (u32 b = threadIdx.x; b < nb; b += TPB)
+#pragma unroll
             for (int i = 0; i < 3 * NRAW; i++) acc[i] = gl_add(acc[i], __ldcg(&a.partials[(u64)b * RAW_WORDS + i]));
 #pragma unroll
         for (int off = 16; off; off >>= 1)
@@ -623,10 +627,15 @@ __global__ void __launch_bounds__(TPB, 2) k_fused(RoundArgs a) {
     chain_enter();
     fused_body<POL, SEM, M, ECH>(a, blockIdx.x, gridDim.x);
 }
-// Policies whose accumulators do not fit 128 registers (the degree-3 product
-// evaluator): one block per SM, no spills.
+// The degree-3 product evaluator.  POL_C3 (four points, the per-round
+// path's h(1) included) does not fit 128 registers: one block per SM.
+// POL_C3W (the device protocol's three points, each an Fp3 x Fp3 sum in
+// three accumulators with the multiplier prepared by W) fits at two blocks
+// per SM without spills in MSB order (measured at one block: 8 warps per
+// SM, issue 38 %, ALU pipe 45 %).
+constexpr int wide_min_blocks(int pol) { return pol == POL_C3W ? 2 : 1; }
 template <int POL, int SEM, u32 M, bool ECH>
-__global__ void __launch_bounds__(TPB, 1) k_fused_wide(RoundArgs a) {
+__global__ void __launch_bounds__(TPB, wide_min_blocks(POL)) k_fused_wide(RoundArgs a) {
     chain_enter();
     fused_body<POL, SEM, M, ECH>(a, blockIdx.x, gridDim.x);
 }
