@@ -63,8 +63,10 @@ def parse():
     ap.add_argument("--serve-host-requests", type=int, default=2000,
                     help="requests of the host-fed serving leg (tables in pinned host memory)")
     ap.add_argument("--serve-budget-gb", type=float, default=150.0)
-    ap.add_argument("--only", choices=["protogalaxy_fold", "multilinear_n20", "gkr_k12"],
-                    help="run one secondary workload alone and print its record (for profiling)")
+    ap.add_argument("--only", choices=["protogalaxy_fold", "multilinear_n20", "gkr_k12", "inner_product_msb",
+                                       "inner_product_lsb", "coefficient_eqfg"],
+                    help="run one workload alone and print its record (for profiling); the last three run "
+                         "--steps proofs at --num-vars without a CUDA graph, one launch per kernel")
     return ap.parse_args()
 
 
@@ -734,14 +736,32 @@ def cpu_rec(work, seconds, unit, sample, scale=1.0):
 
 
 def cpu_model():
+    """The host CPU's model name: /proc/cpuinfo's model name (x86), else
+    lscpu's (Arm: e.g. Neoverse-V2), else the Arm part number."""
     try:
         for line in open("/proc/cpuinfo"):
             if line.lower().startswith(("model name", "cpu model")):
                 return line.split(":", 1)[1].strip()
-        import platform
-        return platform.machine()
     except OSError:
-        return None
+        pass
+    try:
+        import subprocess
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.strip().lower().startswith("model name"):
+                return line.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    try:
+        parts = {"0xd4f": "Neoverse-V2", "0xd40": "Neoverse-V1", "0xd0c": "Neoverse-N1", "0xd49": "Neoverse-N2"}
+        for line in open("/proc/cpuinfo"):
+            if line.lower().startswith("cpu part"):
+                v = line.split(":", 1)[1].strip().lower()
+                return "Arm " + parts.get(v, "part " + v)
+    except OSError:
+        pass
+    import platform
+    return platform.machine()
 
 
 def run_configs(args, E, L, ctx, stream, rank):
@@ -1184,6 +1204,36 @@ def main():
         run_ours(args)
 
 
+def run_plain_proofs(E, ctx, stream, which, n, steps):
+    """`steps` proofs of one workload at num_vars = n, launched kernel by
+    kernel (no graph), for launch lists and kernel captures: the headline's
+    InnerProduct (MSB or LSB, seeded tables, Fp3 challenges) or the
+    Coefficient eq * f * g workload (16 rounds, or n - 1 when n <= 16, with
+    the 32-byte hook)."""
+    import time
+    import torch
+    if which == "coefficient_eqfg":
+        w = E.gen_uniform(E.table_seed(0x3C03_2026, 0), 3 * n, ctx=ctx).reshape(n, 3)
+        f = E.gen_uniform(E.table_seed(0x3C03_2026, 1), 1 << n, ctx=ctx)
+        g = E.gen_uniform(E.table_seed(0x3C03_2026, 2), 1 << n, ctx=ctx)
+        prover = E.CoefficientProver([E.build_eq_table(w, ctx=ctx), f, g], ctx=ctx)
+        rounds, hook, label = min(16, n - 1), bytes(range(32)), b"effsc-gpu/coef3/v1"
+    else:
+        a = E.gen_uniform(E.table_seed(SEED, 0), 1 << n, ctx=ctx)
+        b = E.gen_uniform(E.table_seed(SEED, 1), 1 << n, ctx=ctx)
+        cls = E.InnerProductProver if which == "inner_product_msb" else E.InnerProductProverLSB
+        prover = cls(a, b, field=E.FP3, ctx=ctx)
+        rounds, hook, label = n, b"", LABEL
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        prover.reset()
+        pf = prover.prove(rounds, E.Transcript.keccak(E.FP3, label), hook=hook, use_graph=False)
+    torch.cuda.synchronize()
+    return {"workload": which, "num_vars": n, "rounds": rounds, "proofs": steps,
+            "wall_ms_per_proof": (time.perf_counter() - t0) * 1e3 / steps,
+            "final_value": [int(x) for x in pf.final_value.reshape(-1)]}
+
+
 def run_only(args):
     import torch
     import effsc_gpu as E
@@ -1192,7 +1242,9 @@ def run_only(args):
     stream = torch.cuda.current_stream()
     ctx.set_stream(stream.cuda_stream)
     check = not args.no_cpu_baseline
-    if args.only == "protogalaxy_fold":
+    if args.only in ("inner_product_msb", "inner_product_lsb", "coefficient_eqfg"):
+        rec = run_plain_proofs(E, ctx, stream, args.only, args.num_vars, max(args.steps, 1))
+    elif args.only == "protogalaxy_fold":
         rec = run_pg_fold(E, L, ctx, stream, check, steps=max(args.steps, 1))
     elif args.only == "multilinear_n20":
         rec = run_ml_n20(E, L, ctx, stream, check, steps=max(args.steps, 1))

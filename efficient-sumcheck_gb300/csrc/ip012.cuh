@@ -440,15 +440,17 @@ __device__ __forceinline__ void ring_drain(StageRing<S>& R, u32 i, u32* status) 
     }
 }
 
-constexpr int IP012_TQ = 128;    // octets per tile of the first pass
-constexpr int IP012_S = 4;       // its stages: 4 x 16 KB
+constexpr int IP012_TQ = 256;    // octets per tile of the first pass (two per thread)
+constexpr int IP012_S = 3;       // its stages: 3 x 32 KB
 constexpr int IP012_STAGE_WORDS = 2 * 8 * IP012_TQ;
 constexpr int IP012_SMEM = IP012_S * IP012_STAGE_WORDS * 8;
 
 // Pass 1, staged.  Tile = IP012_TQ octets; a stage holds, per table, the
 // tile's 8 entries of each octet (MSB: 8 chunks, one per j, of TQ words; LSB:
 // the 8 TQ consecutive entries).  Warps 0..3 accumulate sums 0..13, warps
-// 4..7 sums 14..25, both from the same stage.
+// 4..7 sums 14..25, both from the same stage; each thread takes TQ / 128
+// octets of a tile, so the stage wait and release are paid once per two
+// octets.
 template <bool LSB>
 __device__ __forceinline__ void ip012_staged_body(const RoundArgs& a, u32 ntiles) {
     extern __shared__ __align__(128) u64 stg[];
@@ -471,8 +473,9 @@ __device__ __forceinline__ void ip012_staged_body(const RoundArgs& a, u32 ntiles
         }
     };
     ring_start<S>(R, ntiles, issue);
-    const int group = threadIdx.x >= TPB / 2;
-    const int ml = threadIdx.x & (TQ - 1);
+    constexpr int HALF = TPB / 2, PER = TQ / HALF;
+    static_assert(TQ % HALF == 0, "a tile holds whole rows of octets for a warp group");
+    const int group = threadIdx.x >= HALF;
     Acc sums[IP012_G1];
 #pragma unroll
     for (int i = 0; i < IP012_G1; i++) sums[i] = acc_zero();
@@ -481,24 +484,29 @@ __device__ __forceinline__ void ip012_staged_body(const RoundArgs& a, u32 ntiles
     for (u32 tile = blockIdx.x; tile < ntiles; tile += gridDim.x, i++) {
         if (!mbar_wait_bounded(&R.bar[i % S], (i / S) & 1u)) { abort = true; break; }
         const u64* st_ = stg + (size_t)(i % S) * SW;
-        u64 x[8], y[8];
-        if (LSB) {
-            const ulonglong2* px = (const ulonglong2*)(st_ + 8 * ml);
-            const ulonglong2* py = (const ulonglong2*)(st_ + 8 * TQ + 8 * ml);
-            const ulonglong2 a01 = px[0], a23 = px[1], a45 = px[2], a67 = px[3];
-            const ulonglong2 b01 = py[0], b23 = py[1], b45 = py[2], b67 = py[3];
-            x[0] = a01.x; x[4] = a01.y; x[2] = a23.x; x[6] = a23.y; x[1] = a45.x; x[5] = a45.y; x[3] = a67.x; x[7] = a67.y;
-            y[0] = b01.x; y[4] = b01.y; y[2] = b23.x; y[6] = b23.y; y[1] = b45.x; y[5] = b45.y; y[3] = b67.x; y[7] = b67.y;
-        } else {
 #pragma unroll
-            for (int j = 0; j < 8; j++) {
-                x[j] = st_[j * TQ + ml];
-                y[j] = st_[(8 + j) * TQ + ml];
+        for (int h = 0; h < PER; h++) {
+            const int ml = (threadIdx.x & (HALF - 1)) + h * HALF;
+            u64 x[8], y[8];
+            if (LSB) {
+                const ulonglong2* px = (const ulonglong2*)(st_ + 8 * ml);
+                const ulonglong2* py = (const ulonglong2*)(st_ + 8 * TQ + 8 * ml);
+                const ulonglong2 a01 = px[0], a23 = px[1], a45 = px[2], a67 = px[3];
+                const ulonglong2 b01 = py[0], b23 = py[1], b45 = py[2], b67 = py[3];
+                x[0] = a01.x; x[4] = a01.y; x[2] = a23.x; x[6] = a23.y; x[1] = a45.x; x[5] = a45.y; x[3] = a67.x; x[7] = a67.y;
+                y[0] = b01.x; y[4] = b01.y; y[2] = b23.x; y[6] = b23.y; y[1] = b45.x; y[5] = b45.y; y[3] = b67.x; y[7] = b67.y;
+            } else {
+#pragma unroll
+                for (int j = 0; j < 8; j++) {
+                    x[j] = st_[j * TQ + ml];
+                    y[j] = st_[(8 + j) * TQ + ml];
+                }
             }
+            // the stage is free once the tile's last octets are in registers
+            if (h == PER - 1) ring_release<S>(R, i, ntiles, issue);
+            if (group == 0) ip012_sums<0>(sums, x, y);
+            else ip012_sums<1>(sums, x, y);
         }
-        ring_release<S>(R, i, ntiles, issue);
-        if (group == 0) ip012_sums<0>(sums, x, y);
-        else ip012_sums<1>(sums, x, y);
     }
     if (__syncthreads_or(abort)) {
         ring_drain<S>(R, i, a.status);

@@ -819,7 +819,7 @@ int do_fuse3(effsc_prover* P, const TxIO& tx0, const TxIO& tx3, const u64* chals
         staged &= !b0.host && ((uintptr_t)b0.p[0] & 15) == 0;
     }
     const u32 nt1 = (u32)((L / 8) / ip012_tile_octets());
-    staged &= nt1 >= 1;
+    staged &= nt1 >= 1 && (L / 8) % ip012_tile_octets() == 0;
     const int two_per_sm = (max_grid() / 8) * 2;
     const int g1 = staged ? std::min<int>((int)nt1, two_per_sm) : std::min<int>(grid_for(L / 8, 2), two_per_sm);
     // Tables in host memory: when the device has room, the first pass also

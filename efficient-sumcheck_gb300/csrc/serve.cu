@@ -4,7 +4,9 @@
 // Requests queue on the host (FIFO).  Between steps the scheduler admits as
 // many as the slot limit and the HBM budget allow: it reserves the request's
 // device memory (tables, Fp3 work buffers, proof and transcript state) from
-// the server's own stream-ordered pool, generates or uploads its tables and
+// the server's own stream-ordered pool, generates its tables or starts their
+// upload on the lane's upload stream (a request with host tables joins the
+// first step after they have arrived, so uploads overlap the steps) and
 // writes its initial transcript state.  A step is ONE kernel launch in which
 // every admitted request advances by one round -- whatever its kind, size or
 // round -- or finalises; requests admitted while others are mid-proof join the
@@ -46,6 +48,12 @@ uint64_t effsc_internal_add_launches(uint64_t k);
         if (e_ != cudaSuccess) return effsc_set_error(EFFSC_CUDA_ERROR, "%s: %s", #call, cudaGetErrorString(e_)); \
     } while (0)
 
+#define TRYS(call)                           \
+    do {                                     \
+        const int rc_ = (call);              \
+        if (rc_ != EFFSC_OK) return rc_;     \
+    } while (0)
+
 namespace {
 
 constexpr int SERVE_INFLIGHT = 4;        // steps queued ahead of the GPU
@@ -74,6 +82,7 @@ struct Req {
     bool two_pass = false; // InnerProduct over Fp3, n >= 3: rounds 0-2 in two steps (ip01.cuh)
     bool in_tail = false;  // the remaining rounds are running in a tail launch
     cudaEvent_t tail_ev = nullptr;
+    cudaEvent_t up_ev = nullptr;   // host tables: their upload on the lane's upload stream
     int slot = -1;         // pinned result slot
     cudaEvent_t ev = nullptr;
     u64* in(int t) const { return mem + (size_t)t * words_per_table(); }
@@ -110,7 +119,9 @@ struct Lane {
     cudaStream_t stream = nullptr;
     bool own_stream = false;
     cudaStream_t tail_stream = nullptr;
+    cudaStream_t up_stream = nullptr;   // uploads of host tables, beside the steps
     std::deque<Req*> queue;
+    std::vector<Req*> uploading;        // admitted, tables still crossing the host link
     std::vector<Req*> active;
     // step staging: pinned host + device copies of segments and args
     struct Stage {
@@ -201,8 +212,34 @@ int retire(effsc_server* s, bool wait_one) {
 // Admit the lane's queued requests (FIFO) while a slot and the HBM budget
 // allow.  Initial transcript states go through the pinned staging of the
 // lane's next step.
+int activate(effsc_server* s, Lane& ln, Req* r, Lane::Stage& st, u32* ntx, std::vector<Req*>& fresh) {
+    st.h_tx[*ntx] = r->tx0;
+    (*ntx)++;
+    fresh.push_back(r);
+    r->round = 0;
+    ln.active.push_back(r);
+    return EFFSC_OK;
+}
+
+// Requests whose host tables have arrived join the next step.
+int join_uploaded(effsc_server* s, Lane& ln, Lane::Stage& st, u32* ntx, std::vector<Req*>& fresh) {
+    size_t keep = 0;
+    for (size_t i = 0; i < ln.uploading.size(); i++) {
+        Req* r = ln.uploading[i];
+        const cudaError_t q = cudaEventQuery(r->up_ev);
+        if (q == cudaErrorNotReady) { ln.uploading[keep++] = r; continue; }
+        if (q != cudaSuccess) return effsc_set_error(EFFSC_CUDA_ERROR, "serving: %s", cudaGetErrorString(q));
+        s->free_events.push_back(r->up_ev);
+        r->up_ev = nullptr;
+        TRYS(activate(s, ln, r, st, ntx, fresh));
+    }
+    ln.uploading.resize(keep);
+    return EFFSC_OK;
+}
+
 int admit(effsc_server* s, Lane& ln, Lane::Stage& st, u32* ntx, std::vector<Req*>& fresh) {
     cudaStream_t cs = ln.stream;
+    TRYS(join_uploaded(s, ln, st, ntx, fresh));
     while (!ln.queue.empty() && s->n_active < s->max_active) {
         Req* r = ln.queue.front();
         if (s->reserved + r->bytes > s->budget) break;
@@ -217,20 +254,28 @@ int admit(effsc_server* s, Lane& ln, Lane::Stage& st, u32* ntx, std::vector<Req*
         r->mem = (u64*)mem;
         r->res = (u64*)res;
         s->reserved += r->bytes;
-        for (int t = 0; t < r->ntab; t++) {
-            const size_t L = 1ULL << r->n;
-            if (r->htab[t]) SCK(cudaMemcpyAsync(r->in(t), r->htab[t], L * sizeof(u64), cudaMemcpyHostToDevice, cs));
-            else launch_gen_uniform(r->seeds[t], L, r->in(t), cs);
-        }
         SCK(cudaMemsetAsync(r->counter(), 0, sizeof(u32), cs));
-        st.h_tx[*ntx] = r->tx0;
-        (*ntx)++;
-        fresh.push_back(r);
-        r->round = 0;
         r->t_admit = now_s();
         ln.queue.pop_front();
-        ln.active.push_back(r);
         s->n_active++;
+        if (r->htab[0]) {
+            // host tables cross the link on the upload stream (after the
+            // allocation in the lane stream's order) while the steps run;
+            // the request joins a step once they have arrived
+            cudaEvent_t e = get_event(s);
+            SCK(cudaEventRecord(e, cs));
+            SCK(cudaStreamWaitEvent(ln.up_stream, e, 0));
+            s->free_events.push_back(e);
+            for (int t = 0; t < r->ntab; t++)
+                SCK(cudaMemcpyAsync(r->in(t), r->htab[t], (1ULL << r->n) * sizeof(u64), cudaMemcpyHostToDevice,
+                                    ln.up_stream));
+            r->up_ev = get_event(s);
+            SCK(cudaEventRecord(r->up_ev, ln.up_stream));
+            ln.uploading.push_back(r);
+            continue;
+        }
+        for (int t = 0; t < r->ntab; t++) launch_gen_uniform(r->seeds[t], 1ULL << r->n, r->in(t), cs);
+        TRYS(activate(s, ln, r, st, ntx, fresh));
     }
     return EFFSC_OK;
 }
@@ -551,7 +596,8 @@ int effsc_server_create(effsc_ctx* ctx, uint64_t hbm_budget_bytes, uint32_t max_
         else if (cudaStreamCreateWithFlags(&ln.stream, cudaStreamNonBlocking) != cudaSuccess)
             return bail(effsc_set_error(EFFSC_CUDA_ERROR, "serving: stream creation failed"));
         else ln.own_stream = true;
-        if (cudaStreamCreateWithFlags(&ln.tail_stream, cudaStreamNonBlocking) != cudaSuccess)
+        if (cudaStreamCreateWithFlags(&ln.tail_stream, cudaStreamNonBlocking) != cudaSuccess ||
+            cudaStreamCreateWithFlags(&ln.up_stream, cudaStreamNonBlocking) != cudaSuccess)
             return bail(effsc_set_error(EFFSC_CUDA_ERROR, "serving: stream creation failed"));
         for (int k = 0; k < SERVE_INFLIGHT; k++) {
             Lane::Stage& st = ln.stage[k];
@@ -585,11 +631,15 @@ int effsc_server_destroy(effsc_server* s) {
     if (!s) return EFFSC_OK;
     cudaSetDevice(s->device);
     for (Lane& ln : s->lane) {
+        if (ln.up_stream) cudaStreamSynchronize(ln.up_stream);
         if (ln.tail_stream) cudaStreamSynchronize(ln.tail_stream);
         if (ln.stream) cudaStreamSynchronize(ln.stream);
     }
     for (Lane& ln : s->lane) {
+        for (Req* r : ln.uploading) ln.active.push_back(r);
+        ln.uploading.clear();
         for (Req* r : ln.active) {
+            if (r->up_ev) cudaEventDestroy(r->up_ev);
             if (r->mem) cudaFreeAsync(r->mem, ln.stream);
             if (r->res) cudaFreeAsync(r->res, ln.stream);
             if (r->tail_ev) cudaEventDestroy(r->tail_ev);
@@ -616,6 +666,7 @@ int effsc_server_destroy(effsc_server* s) {
         if (ln.d_args) cudaFree(ln.d_args);
         if (ln.d_partials) cudaFree(ln.d_partials);
         if (ln.tail_stream) cudaStreamDestroy(ln.tail_stream);
+        if (ln.up_stream) cudaStreamDestroy(ln.up_stream);
         if (ln.own_stream) cudaStreamDestroy(ln.stream);
     }
     if (s->h_results) cudaFreeHost(s->h_results);
@@ -637,7 +688,7 @@ int effsc_server_progress(effsc_server* s, int wait, uint32_t* pending) {
     int rc = retire(s, false);
     if (rc != EFFSC_OK) return rc;
     for (Lane& ln : s->lane)
-        if (!ln.active.empty() || !ln.queue.empty()) {
+        if (!ln.active.empty() || !ln.queue.empty() || !ln.uploading.empty()) {
             rc = step(s, ln);
             if (rc != EFFSC_OK) return rc;
         }
