@@ -185,6 +185,17 @@ __device__ __forceinline__ void ip012_reduce_and_finalize(const Acc (&s)[IP012_G
         if (threadIdx.x == 0) *a.counter = 0;
     }
     __syncthreads();
+    if (a.acc_mode != ACC_NONE) {
+        // one chunk of the tables: carry the sums to the next chunk's launch
+        if (threadIdx.x < IP012_WORDS) {
+            const u64 v = s_tot[threadIdx.x];
+            if (a.acc_mode == ACC_FIRST) a.acc[threadIdx.x] = v;
+            else if (a.acc_mode == ACC_MID) a.acc[threadIdx.x] = gl_add(a.acc[threadIdx.x], v);
+            else s_tot[threadIdx.x] = gl_add(a.acc[threadIdx.x], v);
+        }
+        if (a.acc_mode != ACC_LAST) return;
+        __syncthreads();
+    }
     if (warp == 0) finalize_ip012(s_tot, a);
 }
 
@@ -222,27 +233,22 @@ __device__ __forceinline__ void ip012_body(const RoundArgs& a, u32 bid, u32 nb) 
 }
 
 // q(r) of the quadratic with q(0) = s0, q(1) = s1 and leading coefficient
-// sinf: s0 + r (s1 - s0 - sinf) + r^2 sinf.
-__device__ __forceinline__ F3 quad_at(const F3& s0, const F3& s1, const F3& sinf, const F3& r) {
+// sinf: s0 + r (s1 - s0 - sinf) + r^2 sinf.  Not inlined: the finalize runs
+// it on one warp of one block, where straight-line code is bound by
+// instruction fetch (a cold SM, one warp): every call site shares this body.
+static __device__ __noinline__ F3 quad_at(F3 s0, F3 s1, F3 sinf, F3 r) {
     const F3 c1 = f3_sub<true>(f3_sub<true>(s1, s0), sinf);
     return f3_add<true>(f3_mul<true, true>(f3_add<true>(f3_mul<true, true>(sinf, r), c1), r), s0);
-}
-// The same with base-field values: r sinf is three products, (.. + c1) r nine.
-__device__ __forceinline__ F3 quad_base(u64 s0, u64 s1, u64 sinf, const F3& r) {
-    const u64 c1 = gl_sub(gl_sub(s1, s0), sinf);
-    F3 t = f3_mul<true, false>(r, f3_make(sinf, 0, 0));
-    t.c0 = gl_add(t.c0, c1);
-    t = f3_mul<true, true>(t, r);
-    t.c0 = gl_add(t.c0, s0);
-    return t;
 }
 
 // Rounds 0, 1, 2 from the 26 sums: for each, the wire [q0, qinf], the hook,
 // the challenge (src/runner.rs:39-55).  Run by warp 0 of the last block.
 // The interpolations run on separate lanes as soon as their challenges are
-// known: after r0, lanes 0-1 evaluate round 1's two quadratics and lanes 2-7
-// the six quadratics in r0 that round 2's biquadratics reduce to; after r1,
-// lanes 0-1 finish round 2 with one quadratic in r1 each.
+// known, each lane gathering its own quadratic's three values so that all
+// of them make one call: after r0, lanes 0-1 evaluate round 1's two
+// quadratics and lanes 2-7 the six quadratics in r0 that round 2's
+// biquadratics reduce to; after r1, lanes 0-1 finish round 2 with one
+// quadratic in r1 each.
 static __device__ __noinline__ void finalize_ip012(const u64* S, const RoundArgs& a) {
     __shared__ u64 s_w[3][6];
     __shared__ u64 s_c[3][3];
@@ -259,25 +265,38 @@ static __device__ __noinline__ void finalize_ip012(const u64* S, const RoundArgs
     DevTranscript* T = (DevTranscript*)a.tx.tx;
     WarpTx w = tx_load(T, lane);
     for (int rd = 0; rd < 3; rd++) {
-        if (rd == 1 && lane < 8) {
-            const F3 r0 = f3_make(s_c[0][0], s_c[0][1], s_c[0][2]);
-            if (lane < 2) {
-                const F3 q = lane == 0 ? quad_base(gl_add(S[0], S[9]), gl_add(S[3], S[10]), gl_add(S[6], S[11]), r0)
-                                       : quad_base(gl_add(S[2], S[23]), gl_add(S[5], S[24]), gl_add(S[8], S[25]), r0);
-                s_w[1][3 * lane] = q.c0; s_w[1][3 * lane + 1] = q.c1; s_w[1][3 * lane + 2] = q.c2;
+        if (rd > 0 && lane < (rd == 1 ? 8 : 2)) {
+            // this lane's quadratic: values at 0, 1 and its leading coefficient
+            F3 q0, q1, qi, r;
+            if (rd == 1) {
+                r = f3_make(s_c[0][0], s_c[0][1], s_c[0][2]);
+                u64 b0, b1, bi;
+                if (lane < 2) {
+                    // round 1: sum_t2 A(r0, 0; t2) B(.., ..) and A(r0, inf; t2) B(..)
+                    const int o = lane == 0 ? 0 : 2, p = lane == 0 ? 9 : 23;
+                    b0 = gl_add(S[o], S[p]);
+                    b1 = gl_add(S[o + 3], S[p + 1]);
+                    bi = gl_add(S[o + 6], S[p + 2]);
+                } else {
+                    // round 2: the biquadratic's row v (P0 or Pd) as a quadratic in r0
+                    const int j = lane - 2, h = j / 3, v = j % 3;
+                    const u64* G = S + 14 * h;
+                    b0 = G[v]; b1 = G[3 + v]; bi = G[6 + v];
+                }
+                q0 = f3_make(b0, 0, 0); q1 = f3_make(b1, 0, 0); qi = f3_make(bi, 0, 0);
+            } else {
+                r = f3_make(s_c[1][0], s_c[1][1], s_c[1][2]);
+                q0 = f3_make(s_g[lane][0][0], s_g[lane][0][1], s_g[lane][0][2]);
+                q1 = f3_make(s_g[lane][1][0], s_g[lane][1][1], s_g[lane][1][2]);
+                qi = f3_make(s_g[lane][2][0], s_g[lane][2][1], s_g[lane][2][2]);
+            }
+            const F3 q = quad_at(q0, q1, qi, r);
+            if (rd == 2 || lane < 2) {
+                s_w[rd][3 * lane] = q.c0; s_w[rd][3 * lane + 1] = q.c1; s_w[rd][3 * lane + 2] = q.c2;
             } else {
                 const int j = lane - 2, h = j / 3, v = j % 3;
-                const u64* G = S + 14 * h;
-                const F3 g = quad_base(G[v], G[3 + v], G[6 + v], r0);
-                s_g[h][v][0] = g.c0; s_g[h][v][1] = g.c1; s_g[h][v][2] = g.c2;
+                s_g[h][v][0] = q.c0; s_g[h][v][1] = q.c1; s_g[h][v][2] = q.c2;
             }
-        }
-        if (rd == 2 && lane < 2) {
-            const F3 r1 = f3_make(s_c[1][0], s_c[1][1], s_c[1][2]);
-            const F3 q = quad_at(f3_make(s_g[lane][0][0], s_g[lane][0][1], s_g[lane][0][2]),
-                                 f3_make(s_g[lane][1][0], s_g[lane][1][1], s_g[lane][1][2]),
-                                 f3_make(s_g[lane][2][0], s_g[lane][2][1], s_g[lane][2][2]), r1);
-            s_w[2][3 * lane] = q.c0; s_w[2][3 * lane + 1] = q.c1; s_w[2][3 * lane + 2] = q.c2;
         }
         __syncwarp();
         tx_send_elems(w, lane, s_w[rd], 2);
@@ -461,6 +480,7 @@ __device__ __forceinline__ void ip012_staged_body(const RoundArgs& a, u32 ntiles
     auto issue = [&](u32 tile, int s) {
         mbar_expect_tx(&R.bar[s], (u32)(SW * 8));
         u64* dst = stg + (size_t)s * SW;
+        tile += a.tile0;
 #pragma unroll
         for (int t = 0; t < 2; t++) {
             if (LSB) {

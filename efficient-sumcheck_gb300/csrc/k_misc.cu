@@ -30,10 +30,13 @@ static int sms_of(int device) {
 
 void kernels_init(int device) { sms_of(device); }
 
+// Programmatic dependent launch of the round kernels: off unless EFFSC_PDL=1
+// (measured at n = 26 in a CUDA graph: 1.273 ms per proof with it, 1.251
+// without).
 bool pdl_on(void) {
     static const bool on = [] {
         const char* e = getenv("EFFSC_PDL");
-        return !(e && e[0] == '0');
+        return e && e[0] == '1';
     }();
     return on;
 }

@@ -110,7 +110,14 @@ struct RoundArgs {
     u64* result;           // wire (d*3 words) then aux pair (6 words)
     u32* status;           // device status word (non-zero: error code)
     TxIO tx;
+    // the first pass of the InnerProduct start over a chunk of the tables:
+    // its tiles start at tile0, and its 26 sums go to `acc` (ACC_FIRST),
+    // are added there (ACC_MID) or are added and finalised (ACC_LAST)
+    u32 tile0;
+    u32 acc_mode;
+    u64* acc;
 };
+enum AccMode { ACC_NONE = 0, ACC_FIRST = 1, ACC_MID = 2, ACC_LAST = 3 };
 
 
 // The last rounds of an MSB Multilinear / InnerProduct proof run by one block

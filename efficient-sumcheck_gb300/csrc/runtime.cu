@@ -264,6 +264,8 @@ struct TabState {
 };
 }  // namespace
 
+constexpr int UPLOAD_CHUNKS = 16;
+
 struct effsc_prover {
     effsc_ctx* ctx = nullptr;
     int kind = 0, order = 0, field = 1, repr = 0;
@@ -280,6 +282,11 @@ struct effsc_prover {
     u32* d_bar = nullptr;
     // host tables: copy to the device during the first pass (-1 undecided)
     int mirror = -1;
+    // pinned host tables: uploaded in chunks on a copy stream while the first
+    // pass runs over the chunks already on the device
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t chunk_ev[UPLOAD_CHUNKS + 1] = {};
+    u64* d_acc = nullptr;
     u32* counter = nullptr;
     u32* status = nullptr;
     u64* h_res = nullptr;                      // mapped pinned: wire (9 words) + aux (6 words)
@@ -798,6 +805,53 @@ bool mirror_ok(effsc_prover* P, size_t L) {
     return P->mirror == 1;
 }
 
+// Pinned host tables of an MSB prover with room on the device: upload them
+// in UPLOAD_CHUNKS chunks of whole octets (octets m in [c O/C, (c+1) O/C),
+// one 2-D copy per table: eight rows of O/C entries at stride O) on a copy
+// stream, and run the first pass on each chunk as soon as it has arrived,
+// carrying the 26 sums from chunk to chunk; the last chunk's launch
+// finalises rounds 0-2.  The copy engines then set the pace and all but the
+// last chunk's pass hide behind the transfer.
+bool upload_chunks_ok(const effsc_prover* P, size_t L) {
+    if (P->order != EFFSC_MSB) return false;
+    const size_t O = L / 8;
+    if (O % ((size_t)UPLOAD_CHUNKS * ip012_tile_octets()) != 0) return false;
+    for (int i = 0; i < 2; i++) {
+        cudaPointerAttributes at;
+        if (cudaPointerGetAttributes(&at, P->t[i].bufs[0].p[0]) != cudaSuccess) { cudaGetLastError(); return false; }
+        if (at.type != cudaMemoryTypeHost) return false;   // pageable: the kernel reads it in place
+    }
+    return true;
+}
+
+int chunked_first_pass(effsc_prover* P, RoundArgs a, const int* mi, bool dry) {
+    cudaStream_t s = P->ctx->stream;
+    const size_t L = P->t[0].len, O = L / 8, CW = O / UPLOAD_CHUNKS;
+    if (!P->copy_stream) CK(cudaStreamCreateWithFlags(&P->copy_stream, cudaStreamNonBlocking));
+    for (cudaEvent_t& e : P->chunk_ev)
+        if (!e) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    if (!P->d_acc) CK(cudaMallocAsync((void**)&P->d_acc, 32 * sizeof(u64), s));
+    if (dry) return EFFSC_OK;
+    // the copies start after the stream's earlier work (the buffers' allocation)
+    CK(cudaEventRecord(P->chunk_ev[UPLOAD_CHUNKS], s));
+    CK(cudaStreamWaitEvent(P->copy_stream, P->chunk_ev[UPLOAD_CHUNKS], 0));
+    const u32 ct = (u32)(CW / ip012_tile_octets());
+    const int g = std::min<int>((int)ct, (max_grid() / 8) * 2);
+    for (int i = 0; i < 2; i++) a.t[i].in[0] = P->t[i].bufs[mi[i]].p[0];
+    a.acc = P->d_acc;
+    for (int c = 0; c < UPLOAD_CHUNKS; c++) {
+        for (int i = 0; i < 2; i++)
+            CK(cudaMemcpy2DAsync(P->t[i].bufs[mi[i]].p[0] + c * CW, O * sizeof(u64), P->t[i].bufs[0].p[0] + c * CW,
+                                 O * sizeof(u64), CW * sizeof(u64), 8, cudaMemcpyHostToDevice, P->copy_stream));
+        CK(cudaEventRecord(P->chunk_ev[c], P->copy_stream));
+        CK(cudaStreamWaitEvent(s, P->chunk_ev[c], 0));
+        a.tile0 = (u32)c * ct;
+        a.acc_mode = c == 0 ? ACC_FIRST : c == UPLOAD_CHUNKS - 1 ? ACC_LAST : ACC_MID;
+        TRY(timed_launch(s, "ip_rounds_0_2_chunked", 16 * (uint64_t)CW * 8, [&] { return launch_ip012_staged(false, a, ct, g, s); }));
+    }
+    return EFFSC_OK;
+}
+
 int do_fuse3(effsc_prover* P, const TxIO& tx0, const TxIO& tx3, const u64* chals, bool dry) {
     const size_t L = P->t[0].len;
     const bool lsb = P->order == EFFSC_LSB;
@@ -831,10 +885,14 @@ int do_fuse3(effsc_prover* P, const TxIO& tx0, const TxIO& tx3, const u64* chals
             TRY(out_buffer(P, P->t[i], false, L, false, &mi[i]));
             a.t[i].out[0] = P->t[i].bufs[mi[i]].p[0];
         }
-    if (!dry) TRY(timed_launch(P->ctx->stream, mi[0] >= 0 ? "ip_rounds_0_2_from_host" : "ip_rounds_0_2", 16 * (uint64_t)L, [&] {
-        if (mi[0] >= 0) return launch_ip012_mirror(lsb, a, g1, P->ctx->stream);
-        return staged ? launch_ip012_staged(lsb, a, nt1, g1, P->ctx->stream) : launch_ip012(lsb, a, g1, P->ctx->stream);
-    }));
+    if (mi[0] >= 0 && upload_chunks_ok(P, L)) {
+        TRY(chunked_first_pass(P, a, mi, dry));
+    } else if (!dry) {
+        TRY(timed_launch(P->ctx->stream, mi[0] >= 0 ? "ip_rounds_0_2_from_host" : "ip_rounds_0_2", 16 * (uint64_t)L, [&] {
+            if (mi[0] >= 0) return launch_ip012_mirror(lsb, a, g1, P->ctx->stream);
+            return staged ? launch_ip012_staged(lsb, a, nt1, g1, P->ctx->stream) : launch_ip012(lsb, a, g1, P->ctx->stream);
+        }));
+    }
     if (mi[0] >= 0)
         for (int i = 0; i < 2; i++) P->t[i].cur = mi[i];
     int bi[2];
@@ -1562,6 +1620,10 @@ void release_prover(effsc_prover* P) {
         if (P->partials) cudaFreeAsync(P->partials, s);
         if (P->counter) cudaFreeAsync(P->counter, s);
         if (P->d_bar) cudaFreeAsync(P->d_bar, s);
+        if (P->d_acc) cudaFreeAsync(P->d_acc, s);
+        for (cudaEvent_t& e : P->chunk_ev)
+            if (e) { cudaEventDestroy(e); e = nullptr; }
+        if (P->copy_stream) { cudaStreamDestroy(P->copy_stream); P->copy_stream = nullptr; }
         if (P->d_tx) cudaFreeAsync(P->d_tx, s);
         if (P->d_hook) cudaFreeAsync(P->d_hook, s);
         if (P->d_wire) cudaFreeAsync(P->d_wire, s);
