@@ -39,7 +39,12 @@ UNIT = "evals/s"
 # DRAM bytes per launch of the dominant kernel, from an ncu capture of this
 # bench at full size (dram__bytes_read.sum + dram__bytes_write.sum averaged
 # over the kernel's launches in one proof); keyed by (kernel, num_vars).
-NCU_TRAFFIC = {("fused_round_fp3", 26): 181.0e6}
+# DRAM bytes (read + write) per launch of each pass at num_vars = 26, from
+# one full-size ncu capture of dram__bytes_read.sum / dram__bytes_write.sum
+# (a one-pass metric set) of `bench.py --only inner_product_msb --num-vars 26
+# --steps 1`; the fused rounds' figure is the average over their launches.
+NCU_TRAFFIC = {("ip_round_3_triple_fold", 26): 1449.9e6, ("ip_rounds_0_2", 26): 1077.2e6,
+               ("fused_round_fp3", 26): 144.4e6}
 
 
 def parse():

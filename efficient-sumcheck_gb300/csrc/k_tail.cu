@@ -434,10 +434,11 @@ u32 tail_cluster_max(void) {
 }
 
 bool launch_tail_cluster(int pol, int fw, const TailArgs& a, u32 cs_log, cudaStream_t s) {
-    // Multilinear only (InnerProduct keeps its multi-block rounds at these sizes)
     switch (pol * 4 + fw) {
     case POL_ML * 4 + 1: return tail_cluster_inst<POL_ML, 1>(a, cs_log, s);
     case POL_ML * 4 + 3: return tail_cluster_inst<POL_ML, 3>(a, cs_log, s);
+    case POL_IP * 4 + 1: return tail_cluster_inst<POL_IP, 1>(a, cs_log, s);
+    case POL_IP * 4 + 3: return tail_cluster_inst<POL_IP, 3>(a, cs_log, s);
     default: return false;
     }
 }

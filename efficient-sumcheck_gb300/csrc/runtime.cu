@@ -621,9 +621,8 @@ bool tail_ok(const effsc_prover* P, size_t r, size_t num_rounds, const Chal& ch)
 // capacity, entered mid-proof (a challenge to fold with), with at least
 // log2(CS) + 1 rounds left; *cs_log = log2(CS), CS = L / capacity.
 bool cluster_tail_ok(const effsc_prover* P, size_t r, size_t num_rounds, const Chal& ch, u32* cs_log) {
-    // Multilinear only: for InnerProduct the cluster rounds cost what the
-    // multi-block rounds they replace cost (measured), so it keeps those
-    if (P->kind != EFFSC_ML || P->order != EFFSC_MSB || !P->tail_len) return false;
+    // Multilinear and InnerProduct, MSB (the slices need MSB pairs)
+    if ((P->kind != EFFSC_ML && P->kind != EFFSC_IP) || P->order != EFFSC_MSB || !P->tail_len) return false;
     if (r >= num_rounds || !ch.has || !ch.dev) return false;
     const size_t L = P->t[0].len;
     for (int i = 1; i < P->ntab; i++)
