@@ -268,6 +268,13 @@ struct PersistArgs {
 };
 bool launch_ip_persist(bool lsb, const RoundArgs& a, const PersistArgs& p, int grid, cudaStream_t s);
 int persist_max_grid(bool lsb);
+// Coefficient rounds 0-2 in two passes (k_coef01.cu; degree-3 product
+// evaluator over three tables, table 0 in Fp (e0 false) or Fp3, tables 1-2 in
+// Fp, Fp3 challenges): rounds 0 and 1 from 15 sums of one read (partials of
+// 48 words per block, so at most max_grid() / 4 blocks), then the fold with
+// r0 and r1 at once (a.chal_ptr, a.chal2_ptr) and round 2 from a second read.
+bool launch_c3_r01(bool lsb, bool e0, const RoundArgs& a, int grid, cudaStream_t s);
+bool launch_c3_r2x(bool lsb, bool e0, const RoundArgs& a, int grid, cudaStream_t s);
 bool launch_ml01(const RoundArgs& a, int grid, cudaStream_t s);
 bool launch_ml2x(bool ech, const RoundArgs& a, int grid, cudaStream_t s);
 bool launch_gkr01(const RoundArgs& a, int grid, cudaStream_t s);

@@ -760,6 +760,61 @@ int do_tail(effsc_prover* P, size_t r, size_t num_rounds, const Chal& ch, const 
     return EFFSC_OK;
 }
 
+// effsc_prove of a Coefficient prover with the degree-3 product evaluator
+// over three device tables of one power-of-two length (table 0 in Fp or Fp3,
+// tables 1-2 in Fp, Fp3 challenges): rounds 0 and 1 from one pass (15
+// triple-product sums), round 2 with the folds by r0 and r1 from a second
+// (k_coef01.cu).  Leaves the state the per-round path leaves after round 2.
+constexpr size_t COEF3_MIN_LEN = (size_t)1 << 12;
+bool coef3_first_ok(const effsc_prover* P, size_t num_rounds) {
+    if (!P->fuse_first || P->kind != EFFSC_COEF || P->expr || P->ntab != 3 || P->field != EFFSC_FP3) return false;
+    if (num_rounds < 3) return false;
+    const size_t L = P->t[0].len;
+    if (!is_pow2(L) || L < COEF3_MIN_LEN) return false;
+    for (int i = 0; i < 3; i++) {
+        const Table& T = P->t[i];
+        if (T.len != L || T.cur != 0 || T.bufs[0].host) return false;
+        if (i > 0 && T.ext) return false;
+    }
+    return true;
+}
+
+int do_coef3_first(effsc_prover* P, const TxIO& tx0, const TxIO& tx2, const u64* chals, bool dry) {
+    const size_t L = P->t[0].len;
+    const bool lsb = P->order == EFFSC_LSB, e0 = P->t[0].ext;
+    RoundArgs a = base_args(P);
+    a.tx = tx0;
+    a.L = L;
+    for (int i = 0; i < 3; i++) set_in(a, i, P->t[i]);
+    // partials of 48 words per block: max_grid() / 4 blocks at most
+    const int g1 = std::min<int>(grid_for(L), max_grid() / 4);   // a quadruple per group thread
+    if (!dry) TRY(timed_launch(P->ctx->stream, "coef_rounds_0_1", (uint64_t)L * (e0 ? 40 : 24), [&] {
+        return launch_c3_r01(lsb, e0, a, g1, P->ctx->stream);
+    }));
+    int bi[3];
+    for (int i = 0; i < 3; i++) TRY(out_buffer(P, P->t[i], true, L / 4, true, &bi[i]));
+    RoundArgs b = base_args(P);
+    b.tx = tx2;
+    b.L = L;
+    b.chal_ptr = chals;
+    b.chal2_ptr = chals + 3;
+    for (int i = 0; i < 3; i++) {
+        set_in(b, i, P->t[i]);
+        set_out(b, i, P->t[i].bufs[bi[i]]);
+    }
+    if (!dry) TRY(timed_launch(P->ctx->stream, "coef_round_2_double_fold", (uint64_t)L * (e0 ? 40 : 24) + 18 * (uint64_t)L, [&] {
+        return launch_c3_r2x(lsb, e0, b, grid_for(L / 8), P->ctx->stream);
+    }));
+    for (int i = 0; i < 3; i++) {
+        Table& T = P->t[i];
+        T.cur = bi[i];
+        T.len = L / 4;
+        T.ext = true;
+    }
+    return EFFSC_OK;
+}
+
+
 // effsc_prove of an InnerProduct prover (MSB or LSB) over Fp3 challenges whose base
 // tables are powers of two: rounds 0 and 1 from one pass, round 2 (with the
 // folds by r0 and r1) from a second (k_ip01.cu).  Leaves the state the
@@ -2273,6 +2328,19 @@ int effsc_prove(effsc_prover* P, size_t num_rounds, effsc_transcript* T, const u
             t3.proof_chal = P->d_chals + 3 * 3;
             TRY(do_fuse3(P, t0, t3, P->d_chals, dry));
             r0 = 4;
+        } else if (coef3_first_ok(P, num_rounds)) {
+            TxIO t0, t2;
+            memset(&t0, 0, sizeof t0);
+            t0.tx = P->d_tx;
+            t0.hook = P->d_hook;
+            t0.hook_len = (u32)hook_len;
+            t2 = t0;
+            t0.proof_wire = P->d_wire;
+            t0.proof_chal = P->d_chals;
+            t2.proof_wire = P->d_wire + (size_t)2 * 3 * d;
+            t2.proof_chal = P->d_chals + 3 * 2;
+            TRY(do_coef3_first(P, t0, t2, P->d_chals, dry));
+            r0 = 3;
         } else if (fuse_first_ok(P, num_rounds)) {
             TxIO t0, t2;
             memset(&t0, 0, sizeof t0);

@@ -213,6 +213,10 @@ int effsc_prover_set_tail(effsc_prover* p, size_t max_len);
  * InnerProduct prover with base tables of 2^14 entries or more and at least
  * 4 rounds, computes rounds 0-3 in two passes instead (rounds 0-2 from 26
  * interpolation sums of one pass; round 3 folds with three challenges).
+ * For a CoefficientProver with the degree-3 product evaluator over three
+ * tables of 2^12 entries or more (table 0 in Fp or Fp3, tables 1-2 in Fp),
+ * fused >= 1 computes rounds 0-2 in two passes (rounds 0 and 1 from 15
+ * triple-product sums of one pass; round 2 folds with both challenges).
  * 0 runs one pass per round.  Proofs are identical. */
 int effsc_prover_set_first_rounds(effsc_prover* p, int fused);
 /* effsc_prove only (no reference counterpart; a tuning knob): for an
