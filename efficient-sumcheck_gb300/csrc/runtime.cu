@@ -959,8 +959,11 @@ int do_fuse3(effsc_prover* P, const TxIO& tx0, const TxIO& tx3, const u64* chals
         set_in(b, i, P->t[i]);
         set_out(b, i, P->t[i].bufs[bi[i]]);
     }
+    // one wave (two blocks per SM, the kernel's residency): n = 26 measured
+    // 0.369 against 0.377 ms (MSB) and 0.350 against 0.364 ms (LSB) for four
+    // waves of blocks
     if (!dry) TRY(timed_launch(P->ctx->stream, "ip_round_3_triple_fold", 16 * (uint64_t)L + 6 * (uint64_t)L, [&] {
-        return launch_ip3x(lsb, b, grid_for(L / 16), P->ctx->stream);
+        return launch_ip3x(lsb, b, std::min<int>(grid_for(L / 16), two_per_sm), P->ctx->stream);
     }));
     for (int i = 0; i < 2; i++) {
         Table& T = P->t[i];
