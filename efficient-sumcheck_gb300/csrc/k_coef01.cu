@@ -19,9 +19,11 @@ bool launch_c3_r01(bool lsb, bool e0, const RoundArgs& a, int grid, cudaStream_t
     if (lsb) return e0 ? launch_chain(k_c3_r01<true, true>, grid, TPB, 0, s, a) : launch_chain(k_c3_r01<true, false>, grid, TPB, 0, s, a);
     return e0 ? launch_chain(k_c3_r01<false, true>, grid, TPB, 0, s, a) : launch_chain(k_c3_r01<false, false>, grid, TPB, 0, s, a);
 }
+#define C3X(LSB, E0) launch_chain(k_c3_r2x<LSB, E0>, wave_grid<k_c3_r2x<LSB, E0>>(grid), TPB, 0, s, a)
 bool launch_c3_r2x(bool lsb, bool e0, const RoundArgs& a, int grid, cudaStream_t s) {
-    if (lsb) return e0 ? launch_chain(k_c3_r2x<true, true>, grid, TPB, 0, s, a) : launch_chain(k_c3_r2x<true, false>, grid, TPB, 0, s, a);
-    return e0 ? launch_chain(k_c3_r2x<false, true>, grid, TPB, 0, s, a) : launch_chain(k_c3_r2x<false, false>, grid, TPB, 0, s, a);
+    if (lsb) return e0 ? C3X(true, true) : C3X(true, false);
+    return e0 ? C3X(false, true) : C3X(false, false);
 }
+#undef C3X
 
 }  // namespace effsc

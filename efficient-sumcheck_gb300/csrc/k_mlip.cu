@@ -21,7 +21,7 @@ bool launch_eval_mlip(int pol, int sem, u32 mask, const RoundArgs& a, int grid, 
 }
 
 #define FUSED(POL, SEM, M, ECH) \
-    case ((POL) * 128 + (SEM) * 32 + (M) * 2 + (ECH)): return launch_chain(k_fused<POL, SEM, M, ECH>, grid, TPB, 0, s, a);
+    case ((POL) * 128 + (SEM) * 32 + (M) * 2 + (ECH)): return launch_chain(k_fused<POL, SEM, M, ECH>, wave_grid<k_fused<POL, SEM, M, ECH>>(grid), TPB, 0, s, a);
 
 bool launch_fused_mlip(int pol, int sem, u32 mask, bool ech, const RoundArgs& a, int grid, cudaStream_t s) {
     switch (pol * 128 + sem * 32 + (int)mask * 2 + (ech ? 1 : 0)) {

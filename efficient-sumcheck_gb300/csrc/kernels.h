@@ -33,6 +33,33 @@ inline bool launch_chain(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t
     cfg.numAttrs = pdl_on() ? 1 : 0;
     return cudaLaunchKernelEx(&cfg, kernel, args...) == cudaSuccess;
 }
+int max_grid(void);
+// One wave of a grid-stride kernel: the blocks the SMs hold at once (the
+// occupancy calculator's count for KERNEL_TPB threads and `smem` bytes per
+// block, cached per kernel and device, times the SM count).  The streaming
+// round kernels measured faster as one wave than as several (InnerProduct's
+// second pass, the Coefficient eq * f * g rounds).
+template <auto Kernel>
+inline int one_wave(size_t smem) {
+    static int cached[64] = {};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return max_grid();
+    int& c = cached[dev & 63];
+    if (c > 0) return c;
+    int nb = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, Kernel, KERNEL_TPB, smem) != cudaSuccess || nb < 1) {
+        cudaGetLastError();
+        return max_grid();
+    }
+    c = nb * (max_grid() / 8);
+    return c;
+}
+// A grid of at most one wave of Kernel.
+template <auto Kernel>
+inline int wave_grid(int grid, size_t smem = 0) {
+    const int w = one_wave<Kernel>(smem);
+    return grid < w ? grid : w;
+}
 // Value a kernel writes to RoundArgs::status when a bounded wait times out.
 constexpr unsigned EFFSC_STATUS_TIMEOUT = 4;
 

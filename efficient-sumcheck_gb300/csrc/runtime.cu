@@ -603,15 +603,27 @@ int round_std(effsc_prover* P, const Chal& ch, const TxIO& tx, bool dry) {
 // fit in shared memory, challenges in device memory, and every round still
 // folding to at least two entries (the length-1 cases stay on the per-round
 // path).
+// The tail kernels' policy for a prover: Multilinear and InnerProduct; -1
+// for the others.  (A tail for the Coefficient product evaluator of degree 3
+// over Fp3 measured slower than its per-round kernels: n = 24, 16 rounds,
+// 1.557 ms with the cluster tail from 2^14 entries, 1.533 ms with the
+// one-block tail from 2048, 1.519 ms without -- one SM folding and
+// evaluating 1024 triple products per round costs more than the launch it
+// saves.)
+int tail_pol(const effsc_prover* P) {
+    if (P->kind == EFFSC_ML || P->kind == EFFSC_IP) return pol_of(P);
+    return -1;
+}
+
 bool tail_ok(const effsc_prover* P, size_t r, size_t num_rounds, const Chal& ch) {
-    if ((P->kind != EFFSC_ML && P->kind != EFFSC_IP) || !P->tail_len) return false;
+    if (tail_pol(P) < 0 || !P->tail_len) return false;
     if (r >= num_rounds || (ch.has && !ch.dev)) return false;
     const size_t L = P->t[0].len;
     for (int i = 1; i < P->ntab; i++)
         if (P->t[i].len != L) return false;
     if (!is_pow2(L)) return false;
     const int fw = P->field == EFFSC_FP3 ? 3 : 1;
-    const size_t lim = std::min<size_t>(P->tail_len, (size_t)tail_max_len(pol_of(P), fw, TAIL_SMEM_CAP));
+    const size_t lim = std::min<size_t>(P->tail_len, (size_t)tail_max_len(tail_pol(P), fw, TAIL_SMEM_CAP));
     if (L > lim) return false;
     const size_t rounds = num_rounds - r, folds = rounds - (ch.has ? 0 : 1);
     return folds < 63 && (L >> folds) >= 2;
@@ -621,15 +633,15 @@ bool tail_ok(const effsc_prover* P, size_t r, size_t num_rounds, const Chal& ch)
 // capacity, entered mid-proof (a challenge to fold with), with at least
 // log2(CS) + 1 rounds left; *cs_log = log2(CS), CS = L / capacity.
 bool cluster_tail_ok(const effsc_prover* P, size_t r, size_t num_rounds, const Chal& ch, u32* cs_log) {
-    // Multilinear and InnerProduct, MSB (the slices need MSB pairs)
-    if ((P->kind != EFFSC_ML && P->kind != EFFSC_IP) || P->order != EFFSC_MSB || !P->tail_len) return false;
+    // the tail's provers, MSB (the slices need MSB pairs)
+    if (tail_pol(P) < 0 || P->order != EFFSC_MSB || !P->tail_len) return false;
     if (r >= num_rounds || !ch.has || !ch.dev) return false;
     const size_t L = P->t[0].len;
     for (int i = 1; i < P->ntab; i++)
         if (P->t[i].len != L) return false;
     if (!is_pow2(L) || L > P->tail_len) return false;
     const int fw = P->field == EFFSC_FP3 ? 3 : 1;
-    const size_t cap = (size_t)tail_max_len(pol_of(P), fw, TAIL_SMEM_CAP);
+    const size_t cap = (size_t)tail_max_len(tail_pol(P), fw, TAIL_SMEM_CAP);
     if (L <= cap) return false;
     const size_t cs = L / cap, csmax = tail_cluster_max();
     if (cs > csmax || cs < 2 || cap < 32 * cs) return false;   // slices of whole 16-entry groups
@@ -716,7 +728,7 @@ int do_persist(effsc_prover* P, size_t r, size_t nr, const Chal& ch, size_t hook
 // and writes the tables' first entries to `first` (the proof read-back).
 int do_tail(effsc_prover* P, size_t r, size_t num_rounds, const Chal& ch, const TxIO& tx, bool dry, u32 cs_log = 0,
             bool fin = false, u64* first = nullptr) {
-    const int pol = pol_of(P), fw = P->field == EFFSC_FP3 ? 3 : 1, nt = P->ntab;
+    const int pol = tail_pol(P), fw = P->field == EFFSC_FP3 ? 3 : 1, nt = P->ntab;
     const size_t L = P->t[0].len, rounds = num_rounds - r, folds = rounds - (ch.has ? 0 : 1) + (fin ? 1 : 0);
     TailArgs ta;
     memset(&ta, 0, sizeof ta);
