@@ -366,9 +366,12 @@ int grid_for(u64 work, u64 per_thread = 1) {
 
 // GkrProver passes whose b-variable pairs run in groups sharing one W_b entry
 // (k_gkr.cu): from GKR_RUNS_MIN pairs on, a grid of a quarter of the threads
-// gives each lane a run of four.
+// gives each lane a run of four.  At most one wave of two blocks per SM (the
+// kernels' residency): k = 12 measured 0.731 -> 0.694 ms per proof.
 constexpr u64 GKR_RUNS_MIN = 1ULL << 17;
-int gkr_grid(u64 pairs, bool runs) { return grid_for(pairs, runs && pairs >= GKR_RUNS_MIN ? 4 : 1); }
+int gkr_grid(u64 pairs, bool runs) {
+    return std::min<int>(grid_for(pairs, runs && pairs >= GKR_RUNS_MIN ? 4 : 1), (max_grid() / 8) * 2);
+}
 
 int alloc_buf(effsc_prover* P, Buf& b, size_t cap, bool ext) {
     b.cap = cap;
