@@ -132,6 +132,42 @@ __device__ __forceinline__ void tail_transcript(WarpTx& w, const TailArgs& a, u3
     if (lane < 3) a.proof_chal[(u64)k * 3 + lane] = sh.chal[lane];
 }
 
+// After the last round: store the transcript state, apply the runner's
+// finalize fold, write the read-back entries and the folded tables.
+template <int POL, int FW>
+__device__ __forceinline__ void tail_finish(u64* smb, u64 stride, u64 len, const TailArgs& a, WarpTx& w, TailShared& sh) {
+    constexpr int NT = Policy<POL, 0>::NT;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (warp == 0) tx_store((DevTranscript*)a.tx, w, lane);
+    if (a.final_fold && len >= 2) {
+        // SumcheckProver::finalize with the last challenge: one MSB fold
+        // (src/inner_product_sumcheck.rs:143-176, src/multilinear_sumcheck.rs:132-178)
+        constexpr bool E = FW == 3;
+        const Mul3 m = mul3_prepare<E>(f3_make(sh.chal[0], sh.chal[1], sh.chal[2]));
+        const u64 half = len >> 1;
+        for (u64 j = threadIdx.x; j < half; j += TAIL_TPB)
+#pragma unroll
+            for (int t = 0; t < NT; t++)
+                sm_st<FW>(smb, stride, t, j, f3_fold<E, E>(sm_ld<FW>(smb, stride, t, j), sm_ld<FW>(smb, stride, t, j + half), m));
+        __syncthreads();
+        len = half;
+    }
+    if (a.first_out && threadIdx.x < 12) {
+        const int t = threadIdx.x / 3, c = threadIdx.x % 3;
+        a.first_out[threadIdx.x] = (t < NT && c < FW) ? smb[(u64)(t * FW + c) * stride] : 0;
+    }
+    // write back the tables after the last fold (LSB: from the reversed layout)
+    if (a.out[0][0]) {
+        const u32 lg = tail_lg(len);
+        for (int t = 0; t < NT; t++)
+            for (int c = 0; c < FW; c++) {
+                const u64* src = smb + (u64)(t * FW + c) * stride;
+                u64* dst = a.out[t][c];
+                for (u64 i = threadIdx.x; i < len; i += TAIL_TPB) dst[i] = src[a.lsb ? tail_rev(i, lg) : i];
+            }
+    }
+}
+
 // Rounds k0 .. a.nrounds-1 in one block on tables of length `len` at smb
 // (table t, component c, element i at smb[(t*FW + c)*stride + i]); then the
 // folded tables go back to global memory and the transcript state is stored.
@@ -141,7 +177,7 @@ __device__ void tail_loop(u64* smb, u64 stride, u64 len, u32 k0, bool fold, cons
     constexpr int NT = Policy<POL, 0>::NT;
     constexpr u32 MF = FW == 3 ? (1u << NT) - 1 : 0;
     using P = Policy<POL, MF>;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int warp = threadIdx.x >> 5;
     for (u32 k = k0; k < a.nrounds; k++) {
         // warps without entries this round skip the arithmetic and the
         // reduction of their (zero) sums; every warp reaches both barriers
@@ -184,34 +220,7 @@ __device__ void tail_loop(u64* smb, u64 stride, u64 len, u32 k0, bool fold, cons
         __syncthreads();
         fold = true;
     }
-    if (warp == 0) tx_store((DevTranscript*)a.tx, w, lane);
-    if (a.final_fold && len >= 2) {
-        // SumcheckProver::finalize with the last challenge: one MSB fold
-        // (src/inner_product_sumcheck.rs:143-176, src/multilinear_sumcheck.rs:132-178)
-        constexpr bool E = FW == 3;
-        const Mul3 m = mul3_prepare<E>(f3_make(sh.chal[0], sh.chal[1], sh.chal[2]));
-        const u64 half = len >> 1;
-        for (u64 j = threadIdx.x; j < half; j += TAIL_TPB)
-#pragma unroll
-            for (int t = 0; t < NT; t++)
-                sm_st<FW>(smb, stride, t, j, f3_fold<E, E>(sm_ld<FW>(smb, stride, t, j), sm_ld<FW>(smb, stride, t, j + half), m));
-        __syncthreads();
-        len = half;
-    }
-    if (a.first_out && threadIdx.x < 12) {
-        const int t = threadIdx.x / 3, c = threadIdx.x % 3;
-        a.first_out[threadIdx.x] = (t < NT && c < FW) ? smb[(u64)(t * FW + c) * stride] : 0;
-    }
-    // write back the tables after the last fold (LSB: from the reversed layout)
-    if (a.out[0][0]) {
-        const u32 lg = tail_lg(len);
-        for (int t = 0; t < NT; t++)
-            for (int c = 0; c < FW; c++) {
-                const u64* src = smb + (u64)(t * FW + c) * stride;
-                u64* dst = a.out[t][c];
-                for (u64 i = threadIdx.x; i < len; i += TAIL_TPB) dst[i] = src[a.lsb ? tail_rev(i, lg) : i];
-            }
-    }
+    tail_finish<POL, FW>(smb, stride, len, a, w, sh);
 }
 
 // Shared-memory layout: table t, component c, element i at sm[(t*FW + c)*L0 + i]
@@ -273,30 +282,19 @@ __device__ __forceinline__ void dsmem_st(const void* p, u32 rank, u64 v) {
     asm volatile("st.shared::cluster.u64 [%0], %1;" ::"r"(remote), "l"(v) : "memory");
 }
 
+// The H = log2(CS) + 1 cluster rounds of k_tail_cluster as separate loops
+// (Multilinear: its cheap rounds measured faster this way, with CTA 0 going
+// on in tail_loop, than in the one loop InnerProduct uses: n = 20, 168
+// against 178 us per proof); the last fold hands the table to CTA 0.
 template <int POL, int FW>
-__global__ void __launch_bounds__(TAIL_TPB, 1) k_tail_cluster(TailArgs a, u32 cs_log) {
-    extern __shared__ __align__(16) u64 sm[];
+__device__ __forceinline__ void tail_cluster_rounds(u64* sm, u64 Ll, u64& len, u32 cs_log, u32 rank, const TailArgs& a,
+                                                    WarpTx& w, TailShared& sh) {
     constexpr int NT = Policy<POL, 0>::NT;
     constexpr u32 MF = FW == 3 ? (1u << NT) - 1 : 0;
     using P = Policy<POL, MF>;
     constexpr int NW3 = 3 * P::NRAW;
-    __shared__ TailShared sh;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const u32 CS = 1u << cs_log, rank = cluster_rank();
-    const u64 L0 = a.L, Ll = L0 >> cs_log;   // slice length (row stride)
-    // this CTA's slice; base tables are embedded when the field is Fp3
-    for (int t = 0; t < NT; t++)
-        for (int c = 0; c < FW; c++) {
-            const u64* src = (c == 0 || ((a.in_ext >> t) & 1u)) ? a.in[t][c] : nullptr;
-            u64* dst = sm + (u64)(t * FW + c) * Ll;
-            for (u64 j = threadIdx.x; j < Ll; j += TAIL_TPB) dst[j] = src ? src[cl_global(j, rank, cs_log)] : 0;
-        }
-    if (threadIdx.x < 3) sh.chal[threadIdx.x] = a.chal_in[threadIdx.x];
-    WarpTx w;
-    if (rank == 0 && warp == 0) w = tx_load((const DevTranscript*)a.tx, lane);
-    cluster_sync_all();   // every CTA is running before any remote store
-    const u32 H = cs_log + 1;
-    u64 len = L0;
+    const u32 CS = 1u << cs_log, H = cs_log + 1;
     for (u32 k = 0; k < H; k++) {
         const u64 ll = len >> cs_log;      // slice length this round (>= 4)
         const bool last = k + 1 == H;
@@ -343,8 +341,101 @@ __global__ void __launch_bounds__(TAIL_TPB, 1) k_tail_cluster(TailArgs a, u32 cs
         }
         cluster_sync_all();   // the challenge is in every CTA
     }
-    if (rank != 0) return;    // no remote access to this CTA follows
-    tail_loop<POL, FW>(sm + Ll / 2, Ll, len, H, true, a, w, sh);
+}
+
+template <int POL, int FW>
+__global__ void __launch_bounds__(TAIL_TPB, 1) k_tail_cluster(TailArgs a, u32 cs_log) {
+    extern __shared__ __align__(16) u64 sm[];
+    constexpr int NT = Policy<POL, 0>::NT;
+    constexpr u32 MF = FW == 3 ? (1u << NT) - 1 : 0;
+    using P = Policy<POL, MF>;
+    constexpr int NW3 = 3 * P::NRAW;
+    __shared__ TailShared sh;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const u32 CS = 1u << cs_log, rank = cluster_rank();
+    const u64 L0 = a.L, Ll = L0 >> cs_log;   // slice length (row stride)
+    // this CTA's slice; base tables are embedded when the field is Fp3
+    for (int t = 0; t < NT; t++)
+        for (int c = 0; c < FW; c++) {
+            const u64* src = (c == 0 || ((a.in_ext >> t) & 1u)) ? a.in[t][c] : nullptr;
+            u64* dst = sm + (u64)(t * FW + c) * Ll;
+            for (u64 j = threadIdx.x; j < Ll; j += TAIL_TPB) dst[j] = src ? src[cl_global(j, rank, cs_log)] : 0;
+        }
+    if (threadIdx.x < 3) sh.chal[threadIdx.x] = a.chal_in[threadIdx.x];
+    WarpTx w;
+    if (rank == 0 && warp == 0) w = tx_load((const DevTranscript*)a.tx, lane);
+    cluster_sync_all();   // every CTA is running before any remote store
+    // InnerProduct: every round runs the same loop body, the cluster rounds
+    // (k < H) and CTA 0's rounds after them -- one copy of the fold,
+    // reduction and transcript code, already in the SM's instruction cache
+    // when CTA 0 goes on alone (a separate copy measured ~15 us for CTA 0's
+    // first round against ~3 us for the next ones; n = 26: 0.170 -> 0.156 ms
+    // for the tail).
+    const u32 H = cs_log + 1;
+    u64 len = L0;
+    if constexpr (POL != POL_IP) {
+        tail_cluster_rounds<POL, FW>(sm, Ll, len, cs_log, rank, a, w, sh);
+        if (rank != 0) return;    // no remote access to this CTA follows
+        tail_loop<POL, FW>(sm + Ll / 2, Ll, len, H, true, a, w, sh);
+    } else {
+        for (u32 k = 0; k < a.nrounds; k++) {
+            const bool cl = k < H;             // a cluster round: every CTA
+            if (!cl && rank != 0) break;       // the others are done (no remote access to them follows)
+            const bool handoff = k + 1 == H;   // the fold goes to CTA 0's rows
+            u64* smb = cl ? sm : sm + Ll / 2;  // CTA 0 continues on rows from offset Ll / 2
+            const u64 ll = cl ? len >> cs_log : len;   // entries per row this round (>= 4 in cluster rounds)
+            const bool active = (u64)warp * 32 < (ll >> 2);
+            P acc;
+            F3 raw[P::NRAW];
+    #pragma unroll
+            for (int i = 0; i < P::NRAW; i++) raw[i] = f3_zero();
+            if (active) {
+                acc.init();
+                tail_fold_eval<POL, FW>(smb, Ll, ll, sh.chal, acc, [&](int t, u64 q, u64 Q, const F3& l, const F3& h) {
+                    if (!handoff) {
+                        sm_st<FW>(smb, Ll, t, q, l);
+                        sm_st<FW>(smb, Ll, t, q + Q, h);
+                        return;
+                    }
+                    // the folded table (L0 / 2^H = Ll / 2 entries) goes to CTA
+                    // 0's rows from offset Ll / 2 on, at its global index
+                    const u64 g_lo = cl_global(q, rank, cs_log), g_hi = cl_global(q + Q, rank, cs_log);
+                    u64* row = sm + (u64)(t * FW) * Ll + Ll / 2;
+                    dsmem_st(row + g_lo, 0, l.c0);
+                    dsmem_st(row + g_hi, 0, h.c0);
+                    if (FW == 3) {
+                        dsmem_st(row + Ll + g_lo, 0, l.c1);
+                        dsmem_st(row + Ll + g_hi, 0, h.c1);
+                        dsmem_st(row + 2 * Ll + g_lo, 0, l.c2);
+                        dsmem_st(row + 2 * Ll + g_hi, 0, h.c2);
+                    }
+                });
+                acc.result(raw);
+            }
+            len >>= 1;
+            tail_block_reduce<P::NRAW>(raw, active, sh);
+            if (cl) {
+                if (warp == 0 && lane < NW3) dsmem_st(&sh.cred[rank][lane], 0, sh.tot[lane]);
+                cluster_sync_all();   // all CTAs' sums (and after the hand-off the table) are in CTA 0
+            }
+            if (rank == 0 && warp == 0) {
+                if (cl && lane < NW3) {
+                    u64 v = 0;
+                    for (u32 c = 0; c < CS; c++) v = gl_add(v, sh.cred[c][lane]);
+                    sh.tot[lane] = v;
+                }
+                __syncwarp();
+                tail_transcript<POL>(w, a, k, sh);
+                __syncwarp();
+                if (cl && lane >= 1 && (u32)lane < CS)
+                    for (int c = 0; c < 3; c++) dsmem_st(&sh.chal[c], (u32)lane, sh.chal[c]);
+            }
+            if (cl) cluster_sync_all();   // the challenge is in every CTA
+            else __syncthreads();
+        }
+        if (rank != 0) return;
+        tail_finish<POL, FW>(sm + Ll / 2, Ll, len, a, w, sh);
+    }
 }
 
 template <int POL, int FW>
