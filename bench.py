@@ -24,6 +24,13 @@ import subprocess
 import sys
 import time
 
+# The CPU baselines run the oracle's OpenMP loops in this process; with
+# threads that spin after each parallel region they compete with the host
+# thread that launches the next GPU workload's graphs (Multilinear n = 20,
+# launched right after the headline's CPU baseline, measured 180 against
+# 169 us per proof).  Idle OpenMP threads sleep instead.
+os.environ.setdefault("OMP_WAIT_POLICY", "PASSIVE")
+
 ROOT = os.path.dirname(os.path.abspath(__file__))
 PKG = os.path.join(ROOT, "efficient-sumcheck_gb300")
 for _p in (ROOT, PKG):
