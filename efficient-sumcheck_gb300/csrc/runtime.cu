@@ -673,7 +673,13 @@ bool persist_ok(const effsc_prover* P, size_t r, size_t num_rounds, const Chal& 
         for (int c = 0; c < 3; c++)
             if ((uintptr_t)T.bufs[T.cur].p[c] & 15) return false;
     }
-    const size_t lim = P->tail_len ? std::min<size_t>(P->tail_len, (size_t)tail_max_len(POL_IP, 3, TAIL_SMEM_CAP)) : 0;
+    size_t lim = P->tail_len ? std::min<size_t>(P->tail_len, (size_t)tail_max_len(POL_IP, 3, TAIL_SMEM_CAP)) : 0;
+    // MSB: stop where the cluster tail takes over (tables of up to
+    // tail_cluster_max() times the one-block capacity)
+    if (lim && P->order == EFFSC_MSB && tail_cluster_max() >= 2) {
+        const size_t cl = lim * tail_cluster_max();
+        if (cl <= P->tail_len) lim = cl;
+    }
     size_t n = 0, l = L;
     while (r + n < num_rounds && l > lim && l >= 4) { n++; l >>= 1; }
     *nr = n;
